@@ -1,0 +1,251 @@
+/*
+ * plume_gpu.h -- C ABI of the GB300 (sm_103a) SPH particle step.
+ *
+ * The library replaces, for one process on one GPU, the per-step particle
+ * path of the Plume-SPH solver: neighbour search, adaptive smoothing length,
+ * momentum/energy with artificial viscosity (+ LANS turbulence and heat
+ * terms), density / mass-fraction summation with energy smoothing, the LANS
+ * velocity filter, the position update, the time-step reduction and the
+ * equation of state.  The host keeps its own input files, particle fields,
+ * inlet and ghost-wall conventions and calls these entry points instead of
+ * the reference free functions.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: PLUME_OK (0) or a PLUME_E_*
+ *     code.  No exception or CUDA error crosses the ABI; the text of the last
+ *     error of a context is available from plume_last_error().
+ *   - Host arrays are owned by the caller and copied at the call.  Device
+ *     buffers are owned by the context.  One context per host thread; each
+ *     context owns one CUDA stream.  The library keeps no global state.
+ *   - Particle identity is a caller-chosen 64-bit key (the host's TKey
+ *     packed into 64 bits).  Downloads are in the library's internal
+ *     (cell-sorted) order; the key array says which particle is which.
+ *
+ * Reference interface each entry point replaces (paths inside the Plume-SPH
+ * source tree):
+ *   plume_create / plume_destroy     compile-time switches of
+ *                                    src/plume/options.h:16-837 and the
+ *                                    constants of src/plume/parameters.h,
+ *                                    bucket grid of src/plume/dataread.cc:247
+ *   plume_upload / plume_append      particle creation in add_air.cc:37,491,
+ *                                    add_pressure_ghost.cc:37,
+ *                                    add_wall_ghost.cc:45,
+ *                                    setup_erupt.cc:44, add_new_erupt :389
+ *   plume_set_ghost_state            the state write of apply_bcond
+ *                                    (src/plume/bcond.cc:196-226)
+ *   plume_step / plume_steps         the hot loop of src/plume/main.cc:217-471
+ *                                    (3D) and :676-750 (1D): timestep
+ *                                    (timestep.cc:94,139), incrtime
+ *                                    (src/datstr/properties.h:71-83),
+ *                                    search_neighs_consth (neighs.cc:37),
+ *                                    adaptive_sml (neighs.cc:479),
+ *                                    mom_engr_update (mom_engr_update.cc:29),
+ *                                    smooth_density (density_massfrac.cc:25),
+ *                                    smooth_velocity (smooth_velocity.cc:25),
+ *                                    update_pos (update_pos.cc:34),
+ *                                    update_particles_in_bucket
+ *                                    (update_pos.cc:171), ifoutput
+ *                                    (properties.h:100-118)
+ *   plume_download                   reads of Particle fields
+ *                                    (src/datstr/particle.h:27-140)
+ *   plume_neighbor_pairs             the per-particle neighbour vectors that
+ *                                    search_neighs_consth stores with
+ *                                    put_neighs (neighs.cc:135,197)
+ */
+#ifndef PLUME_GPU_H
+#define PLUME_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PLUME_OK              0
+#define PLUME_E_INVALID       1  /* bad argument or option                   */
+#define PLUME_E_CUDA          2  /* a CUDA runtime call failed                */
+#define PLUME_E_NONFINITE     3  /* NaN/Inf density, energy or velocity       */
+#define PLUME_E_NONPOSITIVE   4  /* density, kernel normalisation or sound
+                                    speed <= 0 (the reference asserts:
+                                    density_massfrac.cc:293,
+                                    smooth_velocity.cc:139, timestep.cc:126)  */
+#define PLUME_E_CAPACITY      5  /* particle count beyond the context's
+                                    capacity                                  */
+#define PLUME_E_OUTSIDE_GRID  6  /* a particle left the bucket grid           */
+#define PLUME_E_BUCKET_FULL   7  /* more than max_per_bucket particles in one
+                                    bucket (update_pos.cc:427-454)            */
+#define PLUME_E_TIMEOUT       8  /* a bounded device wait gave up             */
+#define PLUME_E_NOT_BUILT     9  /* library built without device support      */
+
+/* ---- particle boundary-condition types (particle.h:140-150) ----------- */
+#define PLUME_BC_ERUPT        0
+#define PLUME_BC_PRESSURE     1
+#define PLUME_BC_WALL         2
+#define PLUME_BC_NOSAVE_REAL 99
+#define PLUME_BC_REAL       100
+
+/* ---- bucket flags (bucket.h:183-214 particles_type / has_involved /
+ *      bucket_type) ------------------------------------------------------ */
+#define PLUME_BUCKET_ABSORBING 0x1 /* has_involved == 0: a real particle that
+                                      moves in is deleted (update_pos.cc:289) */
+#define PLUME_BUCKET_MIXED     0x2 /* bucket_type == MIXED: escape test
+                                      against the domain faces (bucket.cc:435)*/
+#define PLUME_BUCKET_INACTIVE  0x4 /* not active: particles in it are not
+                                      re-bucketed (update_pos.cc:203)        */
+
+/* ---- arithmetic of the pair sweeps ------------------------------------ */
+#define PLUME_PREC_FP64   0  /* every pair term in FP64                       */
+#define PLUME_PREC_MIXED  1  /* FP32 pair arithmetic on cell-relative
+                                coordinates with compensated FP32 sums; FP64
+                                positions, position/energy update and
+                                conservation sums                             */
+
+/* ---- smoothing kernels ------------------------------------------------- */
+#define PLUME_KERNEL_GAUSS  0 /* sph_lib.cc:207-253: (1/(sqrt(pi) h))^D
+                                 exp(-|s|^2), zero if any |s_k| > 3          */
+#define PLUME_KERNEL_M4     1 /* cubic B-spline (Monaghan M4), radial support
+                                 2h, used by the Sod / ensemble workloads     */
+
+/* Compile-time switches and physical constants of the reference, as a
+ * runtime struct.  Field comments give the reference symbol. */
+typedef struct PlumeOptions {
+    int    dim;                 /* CODE_DIMENSION: 1 or 3                      */
+    int    precision;           /* PLUME_PREC_*                                */
+    int    kernel;              /* PLUME_KERNEL_*                              */
+    int    lans;                /* HAVE_TURBULENCE_LANS: 0 or 1                */
+    int    energy_smooth;       /* HAVE_ENERGY_SMOOTH: 0 or 1 (normalised)     */
+    int    pghost_contrib;      /* PGHOST_CONTRIBUTE_DES: 0, 1 or 2            */
+    int    adaptive_sml;        /* ADAPTIVE_SML: 0 or 1                        */
+    int    sml_interval;        /* SML_UPDATE_INT (3D); 1 = every step (1D)    */
+    int    num_loop;            /* num_loop_P                                  */
+    double thresh;              /* thresh_P                                    */
+    double c_smooth;            /* C_smooth_P                                  */
+    double eta_smooth;          /* eta_smooth_P                                */
+    double alpha, beta, ata;    /* alf_P, beta_P, ata_P                        */
+    double cfl;                 /* CFL_P                                       */
+    double cutoff2;             /* CUTOFF2 (12 in 1D, 8 in 3D)                 */
+    double list_factor;         /* 4.25, neighs.cc:84                          */
+    double g;                   /* g_P                                         */
+    double ng0, cvs, cvg, cva, rg, ra; /* ng0_P Cvs_P Cvg_P Cva_P Rg_P Ra_P    */
+    double vent_z;              /* Ll_P[2]: erupt ghosts turn real at z>=vent_z */
+    double sml_phase2;          /* matprops->smoothing_length                  */
+    /* TimeProps (properties.h:17-69); times in seconds, TIME_SCALE = 1 */
+    double max_time;
+    double timeoutput;
+    double stat_erupt, end_erupt;
+    int    max_steps;
+    int    max_per_bucket;      /* MAX_PARTICLES_PER_BUCKET                    */
+    size_t capacity;            /* device particle capacity of the context     */
+} PlumeOptions;
+
+/* Bucket grid (the background mesh of src/datstr/bucket.h).  Bucket (i,j,k)
+ * spans [mindom + i*del, mindom + (i+1)*del) per axis (preprocess.cc:167-177).
+ * 1D uses nb[1] = nb[2] = 1 and no bucket rule (every particle is a neighbour
+ * candidate, add_air.cc:470-479). */
+typedef struct PlumeGrid {
+    double mindom[3];
+    double del;                 /* bucket edge = PARTICLE_DENSITY * h0         */
+    int    nb[3];               /* buckets per axis                            */
+    int    subcells;            /* fine cells per bucket edge (GPU tiling)     */
+    const uint8_t *flags;       /* nb0*nb1*nb2 PLUME_BUCKET_* (x fastest), may
+                                   be NULL (all active, none absorbing/mixed) */
+    const int8_t  *face_index;  /* 6 per bucket: bucket_index of bucket.h:
+                                   -1/0/1 per face (x-,x+,y-,y+,z-,z+); may be
+                                   NULL                                       */
+    double domain_lo[3];        /* original domain Ll_P (escape planes)        */
+    double domain_hi[3];        /* original domain Lu_P                        */
+} PlumeGrid;
+
+/* Structure of arrays on the host.  Pointers for unused axes (1D) may be
+ * NULL on upload; on download every non-NULL pointer is filled. */
+typedef struct PlumeSoA {
+    uint64_t *key;
+    double *x, *y, *z;
+    double *vx, *vy, *vz;          /* state_vars[1..D]                          */
+    double *vsx, *vsy, *vsz;       /* smoothed_v (LANS)                         */
+    double *mass, *h;
+    double *rho, *e;               /* state_vars[0], state_vars[D+1]            */
+    double *p, *Y, *gamma, *c, *T, *cp;
+    uint8_t *phase;                /* 1 air, 2 erupted material                 */
+    uint8_t *bc_type;              /* PLUME_BC_*                                */
+    uint8_t *involved;             /* 0, 1, 2                                   */
+} PlumeSoA;
+
+typedef struct PlumeStepLog {
+    double dt;                     /* dt of the step after incrtime clipping    */
+    double time;                   /* simulated time after the step             */
+    int    step;                   /* TimeProps::step after the step            */
+    int    status;                 /* PLUME_* of the step                       */
+    uint64_t n_total;              /* particles after the step                  */
+    uint64_t n_real;               /* need_neigh particles after the step       */
+    uint64_t n_lost;               /* particles deleted during the step         */
+} PlumeStepLog;
+
+typedef struct plume_ctx plume_ctx;
+
+/* Create a context on the current CUDA device. */
+int plume_create(const PlumeOptions *opt, const PlumeGrid *grid, plume_ctx **out);
+int plume_destroy(plume_ctx *ctx);
+
+/* Replace all particles (host arrays). */
+int plume_upload(plume_ctx *ctx, const PlumeSoA *host, size_t n);
+/* Replace all particles from arrays that already live in device memory of
+ * the context's device (same layout as PlumeSoA; NULL axes allowed in 1D). */
+int plume_upload_device(plume_ctx *ctx, const PlumeSoA *dev, size_t n);
+/* Append particles (inlet injection, new ghosts). */
+int plume_append(plume_ctx *ctx, const PlumeSoA *host, size_t n);
+
+/* Overwrite the state of ghost particles identified by key: state is n rows
+ * of (rho, vx, vy, vz, e) in 3D or (rho, vx, e) in 1D; Y may be NULL.  The
+ * equation of state is re-evaluated for them (bcond.cc:214-219). */
+int plume_set_ghost_state(plume_ctx *ctx, const uint64_t *keys,
+                          const double *state, const double *Y, size_t n);
+
+/* One step in reference order; *dt_out receives the clipped dt. */
+int plume_step(plume_ctx *ctx, double *dt_out);
+/* nsteps steps without host synchronisation between them; log may be NULL
+ * or point to nsteps entries. */
+int plume_steps(plume_ctx *ctx, int nsteps, PlumeStepLog *log);
+
+/* Particle count (total and need_neigh). */
+int plume_count(plume_ctx *ctx, size_t *n_total, size_t *n_real);
+/* Copy all particles to host arrays of capacity cap; *n receives the count. */
+int plume_download(plume_ctx *ctx, PlumeSoA *host, size_t cap, size_t *n);
+/* Simulated time, step counter and output counter (TimeProps). */
+int plume_get_time(plume_ctx *ctx, double *time, int *step, int *ioutput);
+int plume_set_time(plume_ctx *ctx, double time, int step, int ioutput,
+                   double next_output);
+
+/* Neighbour pairs (key_i, key_j) for every need_neigh particle i.
+ *   mode 0: the candidate list of search_neighs_consth (3D: own bucket plus
+ *           particles of the 26 adjacent buckets inside the 4.25 h_i box;
+ *           1D: every particle), at the current positions and h;
+ *   mode 1: the pairs that the momentum sweep sums over: candidates j != i
+ *           inside the CUTOFF2*h_i box whose kernel with h_ij=(h_i+h_j)/2 is
+ *           non-zero.
+ * If cap is smaller than the pair count nothing is written and *n receives
+ * the count. */
+int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
+                         uint64_t *key_j, size_t cap, size_t *n);
+
+/* Per-phase device time of the last plume_step/plume_steps call, in ms:
+ * [0] sort+cells, [1] adaptive h, [2] momentum/energy, [3] density,
+ * [4] velocity filter, [5] position/rebucket, [6] dt reduction, [7] total. */
+int plume_phase_times(plume_ctx *ctx, float *ms, int n);
+
+/* Device kernel launches issued by the last plume_step/plume_steps call. */
+int plume_launch_count(plume_ctx *ctx, uint64_t *n);
+
+/* Text of the last error of ctx (or of the last failed create if ctx is
+ * NULL). */
+int plume_last_error(plume_ctx *ctx, char *buf, size_t len);
+
+/* Library version string "major.minor.patch". */
+const char *plume_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLUME_GPU_H */

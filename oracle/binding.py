@@ -1,0 +1,111 @@
+"""ctypes binding of liboracle.so (oracle/sph_oracle.c) -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm use it.  Builds the library with `make -C oracle` when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "plume-sph_gb300"))
+
+from plume_gpu.abi import PlumeGrid, PlumeOptions, PlumeSoA, ParticleSet  # noqa: E402
+
+_LIB = None
+
+
+class OracleTime(C.Structure):
+    _fields_ = [("time", C.c_double), ("dtime", C.c_double), ("ndtimeoutput", C.c_double),
+                ("step", C.c_int), ("ioutput", C.c_int)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.oracle_steps.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                   C.POINTER(PlumeSoA), C.POINTER(C.c_size_t),
+                                   C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int]
+        L.oracle_adaptive.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                      C.POINTER(PlumeSoA), C.c_size_t, C.c_int]
+        L.oracle_pairs.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                   C.POINTER(PlumeSoA), C.c_size_t, C.c_int,
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_size_t,
+                                   C.POINTER(C.c_size_t)]
+        L.oracle_sample_step_seconds.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                                 C.POINTER(PlumeSoA), C.c_size_t, C.c_size_t,
+                                                 C.c_int]
+        L.oracle_sample_step_seconds.restype = C.c_double
+        _LIB = L
+    return _LIB
+
+
+class OracleRun:
+    """Stateful wrapper: particles + time of one oracle run."""
+
+    def __init__(self, case, nthreads: int = 0):
+        self.case = case
+        self.ps = case.particles.copy()
+        self.opt = case.options.to_c()
+        self.grid = case.grid.to_c()
+        self.t = OracleTime(0.0, 0.0, case.options.timeoutput, case.step0, 0)
+        self.nthreads = nthreads
+
+    def adaptive(self):
+        s = self.ps.soa()
+        rc = lib().oracle_adaptive(C.byref(self.opt), C.byref(self.grid), C.byref(s),
+                                   self.ps.n, self.nthreads)
+        if rc:
+            raise RuntimeError(f"oracle_adaptive failed: {rc}")
+
+    def steps(self, nsteps: int):
+        s = self.ps.soa()
+        n = C.c_size_t(self.ps.n)
+        dts = (C.c_double * max(nsteps, 1))()
+        rc = lib().oracle_steps(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
+                                C.byref(self.t), nsteps, dts, self.nthreads)
+        if rc:
+            raise RuntimeError(f"oracle_steps failed: {rc}")
+        if n.value != self.ps.n:
+            self.ps = self.ps.take(np.arange(n.value))
+        return np.array(dts[:nsteps])
+
+    def pairs(self, mode: int = 0):
+        s = self.ps.soa()
+        cnt = C.c_size_t(0)
+        L = lib()
+        rc = L.oracle_pairs(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n, mode,
+                            None, None, 0, C.byref(cnt))
+        if rc:
+            raise RuntimeError(f"oracle_pairs failed: {rc}")
+        ki = np.zeros(cnt.value, dtype=np.uint64)
+        kj = np.zeros(cnt.value, dtype=np.uint64)
+        rc = L.oracle_pairs(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n, mode,
+                            ki.ctypes.data_as(C.POINTER(C.c_uint64)),
+                            kj.ctypes.data_as(C.POINTER(C.c_uint64)), cnt.value, C.byref(cnt))
+        if rc:
+            raise RuntimeError(f"oracle_pairs failed: {rc}")
+        return ki, kj
+
+
+def sample_step_seconds(case, ntarget: int, nthreads: int = 0) -> float:
+    ps = case.particles
+    s = ps.soa()
+    opt = case.options.to_c()
+    grid = case.grid.to_c()
+    return lib().oracle_sample_step_seconds(C.byref(opt), C.byref(grid), C.byref(s), ps.n,
+                                            ntarget, nthreads)

@@ -1,0 +1,86 @@
+"""Case / result files of the reference harness oracle/ref/driver.cc --
+TEST INFRASTRUCTURE (used by tests/golden/make_golden.py only)."""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+
+import numpy as np
+
+from .binding import ParticleSet  # noqa: F401  (sets sys.path)
+from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, ParticleSet as PS
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def build_ref(ref_root: str = "/root/reference"):
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
+
+
+def write_case(path, case, nsteps):
+    o, g, ps = case.options, case.grid, case.particles
+    with open(path, "wb") as fp:
+        fp.write(b"PLSPHIN1")
+        fp.write(struct.pack("<5i", o.dim, nsteps, ps.n, int(case.pre_adaptive), int(case.step0)))
+        fp.write(struct.pack("<5d", o.max_time, o.timeoutput, o.stat_erupt, o.end_erupt,
+                             o.sml_phase2))
+        if o.dim == 3:
+            fp.write(struct.pack("<3d", *g.mindom))
+            fp.write(struct.pack("<d", g.del_))
+            fp.write(struct.pack("<3i", *g.nb))
+            fp.write(np.ascontiguousarray(g.flags, dtype=np.uint8).tobytes())
+            fp.write(np.ascontiguousarray(g.face_index, dtype=np.int8).tobytes())
+            fp.write(struct.pack("<3d", *g.domain_lo))
+            fp.write(struct.pack("<3d", *g.domain_hi))
+        fp.write(ps.key.astype("<u8").tobytes())
+        for f in DOUBLE_FIELDS:
+            fp.write(getattr(ps, f).astype("<f8").tobytes())
+        for f in BYTE_FIELDS:
+            fp.write(getattr(ps, f).astype(np.uint8).tobytes())
+
+
+def read_result(path):
+    """Returns (steps, lists): steps = list of dict(dt, time, step, ioutput,
+    particles); lists = dict key_i -> np.ndarray of key_j in list order."""
+    data = open(path, "rb").read()
+    off = 0
+
+    def take(fmt):
+        nonlocal off
+        v = struct.unpack_from(fmt, data, off)
+        off += struct.calcsize(fmt)
+        return v
+
+    assert data[:8] == b"PLSPHOU1"
+    off = 8
+    dim, nsteps = take("<2i")
+    steps = []
+    for _ in range(nsteps):
+        dt, t = take("<2d")
+        st, io = take("<2i")
+        (n,) = take("<q")
+        ps = PS(n)
+        ps.key = np.frombuffer(data, "<u8", n, off).copy(); off += 8 * n
+        for f in DOUBLE_FIELDS:
+            setattr(ps, f, np.frombuffer(data, "<f8", n, off).copy()); off += 8 * n
+        for f in BYTE_FIELDS:
+            setattr(ps, f, np.frombuffer(data, np.uint8, n, off).copy()); off += n
+        steps.append({"dt": dt, "time": t, "step": st, "ioutput": io, "particles": ps})
+    (nl,) = take("<q")
+    lists = {}
+    for _ in range(nl):
+        (ki,) = take("<Q")
+        (ln,) = take("<q")
+        lists[ki] = np.frombuffer(data, "<u8", ln, off).copy(); off += 8 * ln
+    return steps, lists
+
+
+def run_ref(variant, case, nsteps, workdir):
+    os.makedirs(workdir, exist_ok=True)
+    cin = os.path.join(workdir, f"{case.name}.case")
+    cout = os.path.join(workdir, f"{case.name}.out")
+    write_case(cin, case, nsteps)
+    exe = os.path.join(HERE, "_ref", variant, "driver")
+    subprocess.run([exe, cin, cout], check=True)
+    return read_result(cout)

@@ -1,0 +1,982 @@
+/*
+ * sph_oracle.c -- CPU oracle of the Plume-SPH per-step particle path.
+ *
+ * TEST INFRASTRUCTURE (the checker, never the product).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm load
+ * it.  It restates the reference algorithm over structure-of-arrays
+ * particles; every function cites the reference lines it follows (paths
+ * inside the Plume-SPH source tree).  Operation order inside each formula is
+ * kept as the reference writes it, so that with the same libm the first
+ * step agrees with the reference build to the last bit.  Build with
+ * -ffp-contract=off (x86 compilers do not fuse by default; aarch64 ones do).
+ *
+ * Parity pin: golden vectors from the reference's own sources
+ * (tests/golden/make_golden.py, tests/test_oracle_golden.py).
+ */
+#include "sph_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* constants of src/plume/constant.h and sph_lib.cc */
+#define OR_T1        0.564189583547756   /* 1/sqrt(pi), sph_lib.cc:206     */
+#define OR_CUTOFF    3.0                 /* CUTOFF, constant.h:51          */
+#define OR_EPS_HALF  0.4                 /* EPSILON_HALF, constant.h:94    */
+#define OR_PRANDTL   0.85                /* PRANDTL_NUM, constant.h:95     */
+#define OR_E_SMOOTH  4.0                 /* E_SMOOTH_RATIO, constant.h:185 */
+#define OR_MSFRC_TH  1.0e-6              /* MSFRC_THRESH, constant.h:80    */
+#define OR_TINY      1.0e-8              /* TINY, constant.h:76            */
+/* cubic B-spline normalisations (1D: 2/3, 3D: 1/pi) */
+#define OR_M4_S1     0.66666666666666663
+#define OR_M4_S3     0.31830988618379069
+
+/* ------------------------------------------------------------------ */
+/* particle predicates, src/datstr/particle.h:555-615                   */
+/* ------------------------------------------------------------------ */
+static inline int need_neigh(uint8_t bc) { return bc == 100 || bc == 99; }
+static inline int is_real(uint8_t bc) { return bc == 100 || bc == 99; }
+static inline int contr_dens(uint8_t bc, int mode)
+{
+    /* particle.h:570-579 (PGHOST_CONTRIBUTE_DES) */
+    if (mode == 1) return bc == 100 || bc == 99 || bc == 1;
+    if (mode == 2) return bc == 100 || bc == 99 || bc == 1 || bc == 0;
+    return bc == 100 || bc == 99;
+}
+static inline int contr_vel_smooth(uint8_t bc)
+{
+    return bc == 100 || bc == 99 || bc == 2; /* particle.h:587-590 */
+}
+
+/* in_support, sph_header.h:49-60: every |dx_k| <= h */
+static inline int in_support(const double *dx, double h, int D)
+{
+    for (int i = 0; i < D; i++)
+        if (fabs(dx[i]) > h) return 0;
+    return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* kernels                                                              */
+/* ------------------------------------------------------------------ */
+/* weight, sph_lib.cc:210-230 */
+static double weight_gauss(const double *s, double h, int D)
+{
+    for (int i = 0; i < D; i++)
+        if (fabs(s[i]) > OR_CUTOFF) return 0;
+    double norm = 1, expt = 0;
+    for (int i = 0; i < D; i++) {
+        norm *= OR_T1 / h;
+        expt += s[i] * s[i];
+    }
+    return norm * exp(-expt);
+}
+/* d_weight, sph_lib.cc:240-253 */
+static double d_weight_gauss(const double *s, double h, int dir, int D)
+{
+    for (int i = 0; i < D; i++)
+        if (fabs(s[i]) > OR_CUTOFF) return 0;
+    double tmp = -2 * s[dir] / h;
+    return tmp * weight_gauss(s, h, D);
+}
+/* cubic B-spline with radial support 2h (the Sod / ensemble workloads) */
+static double weight_m4(const double *s, double h, int D)
+{
+    double r2 = 0;
+    for (int i = 0; i < D; i++) r2 += s[i] * s[i];
+    double q = sqrt(r2);
+    if (q >= 2.0) return 0;
+    double norm = (D == 1) ? OR_M4_S1 : OR_M4_S3;
+    for (int i = 0; i < D; i++) norm = norm / h;
+    double w;
+    if (q < 1.0) {
+        w = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
+    } else {
+        double t = 2.0 - q;
+        w = 0.25 * t * t * t;
+    }
+    return norm * w;
+}
+static double d_weight_m4(const double *s, double h, int dir, int D)
+{
+    double r2 = 0;
+    for (int i = 0; i < D; i++) r2 += s[i] * s[i];
+    double q = sqrt(r2);
+    if (q >= 2.0 || q == 0.0) return 0;
+    double norm = (D == 1) ? OR_M4_S1 : OR_M4_S3;
+    for (int i = 0; i < D; i++) norm = norm / h;
+    double dw;
+    if (q < 1.0) {
+        dw = -3.0 * q + 2.25 * q * q;
+    } else {
+        double t = 2.0 - q;
+        dw = -0.75 * t * t;
+    }
+    return norm * dw * s[dir] / (q * h);
+}
+static inline double kw(int kernel, const double *s, double h, int D)
+{
+    return kernel == PLUME_KERNEL_M4 ? weight_m4(s, h, D) : weight_gauss(s, h, D);
+}
+static inline double kdw(int kernel, const double *s, double h, int dir, int D)
+{
+    return kernel == PLUME_KERNEL_M4 ? d_weight_m4(s, h, dir, D)
+                                     : d_weight_gauss(s, h, dir, D);
+}
+
+/* compute_F, sph_lib.cc:257-281 */
+static double compute_F(const double *dwdx, const double *dx, int D)
+{
+    double r_sq = 0., W_r = 0.;
+    for (int i = 0; i < D; i++) W_r += dwdx[i] * dx[i];
+    if (W_r == 0) return 0.0;
+    for (int i = 0; i < D; i++) r_sq += dx[i] * dx[i];
+    return W_r / r_sq;
+}
+/* art_vis, sph_lib.cc:402-424 */
+static double art_vis(const PlumeOptions *o, double rhoab, double sndspdab,
+                      const double *rab, const double *vab, double rsqab,
+                      double h, int D)
+{
+    double vrab = 0., vis = 0.;
+    for (int k = 0; k < D; k++) vrab += rab[k] * vab[k];
+    double miuab = h * vrab / (rsqab + o->ata * h * h);
+    if (vrab > 0)
+        vis = 0.;
+    else if (vrab < 0)
+        vis = (o->beta * miuab - o->alpha * sndspdab) * miuab / rhoab;
+    return vis;
+}
+/* SPH_epsilon_mom, sph_lib.cc:1331-1338 */
+static double eps_mom(const double *vab, double Vb, int D)
+{
+    double dotv = 0.;
+    for (int i = 0; i < D; i++) dotv += vab[i] * vab[i];
+    return OR_EPS_HALF * dotv * Vb;
+}
+/* SPH_epsilon_heat_conductivity (6-argument form), sph_lib.cc:1399-1440 */
+static double eps_heat(double cp_ab, const double *ds, const double *vab,
+                       double hab, double cab, int D)
+{
+    double dotvv = 0., dotvr = 0., dotrr = 0., kab;
+    for (int i = 0; i < D; i++) dotvr += fabs(vab[i] * ds[i]);
+    if (dotvr == 0.) return 0.;
+    for (int i = 0; i < D; i++) dotrr += ds[i] * ds[i];
+    for (int i = 0; i < D; i++) dotvv += vab[i] * vab[i];
+    if (D == 3)
+        kab = 10.0 * OR_EPS_HALF * cp_ab * dotrr * dotvv / (OR_PRANDTL * dotvr);
+    else if (D == 2)
+        kab = 8.0 * OR_EPS_HALF * cp_ab * dotrr * dotvv / (OR_PRANDTL * dotvr);
+    else
+        kab = 0.0;
+    return kab / (hab * cab);
+}
+
+/* Particle::update_second_var, src/datstr/particle.cc:528-604 (ideal gas) */
+static void eos(const PlumeOptions *o, PlumeSoA *s, size_t i)
+{
+    double desm = s->rho[i];
+    double Y = s->Y[i];
+    double na = 1 - Y;
+    double engr = s->e[i];
+    double ng = o->ng0 * Y;
+    double ns = Y - ng;
+    double Cvm = ns * o->cvs + ng * o->cvg + na * o->cva;
+    double Rm = ng * o->rg + na * o->ra;
+    double Rmg = Rm / (ng + na);
+    double gamma = 1 + Rm / Cvm;
+    double desmg = desm * (na + ng);
+    double pressure = Rmg * desmg * engr / Cvm;
+    s->gamma[i] = gamma;
+    s->p[i] = pressure;
+    s->c[i] = pow(gamma * pressure / desmg, 0.5);
+    s->T[i] = engr / Cvm;
+    if (o->lans) s->cp[i] = Cvm;
+}
+
+/* ------------------------------------------------------------------ */
+/* bucket grid (preprocess.cc:167-177, bucket.h:238-245)                */
+/* ------------------------------------------------------------------ */
+static int bucket_axis(double x, double mind, double del, int nb)
+{
+    double f = floor((x - mind) / del);
+    if (!(f > -2.0) || !(f < (double)nb + 1.0)) return -1;
+    int b = (int)f;
+    if (b < 0) b = 0;
+    if (b > nb - 1) b = nb - 1;
+    while (b > 0 && x < mind + b * del) b--;
+    while (b < nb - 1 && x >= mind + (b + 1) * del) b++;
+    if (x < mind + b * del || x >= mind + (b + 1) * del) return -1;
+    return b;
+}
+static long bucket_of(const PlumeGrid *g, double x, double y, double z)
+{
+    int bx = bucket_axis(x, g->mindom[0], g->del, g->nb[0]);
+    int by = bucket_axis(y, g->mindom[1], g->del, g->nb[1]);
+    int bz = bucket_axis(z, g->mindom[2], g->del, g->nb[2]);
+    if (bx < 0 || by < 0 || bz < 0) return -1;
+    return ((long)bz * g->nb[1] + by) * g->nb[0] + bx;
+}
+static uint8_t bucket_flags(const PlumeGrid *g, long b)
+{
+    return g->flags ? g->flags[b] : 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* neighbour lists, search_neighs_consth (neighs.cc:37-211)             */
+/* ------------------------------------------------------------------ */
+typedef struct Lists {
+    size_t  *start;   /* n+1 */
+    int32_t *idx;
+    size_t   nidx;
+} Lists;
+
+static void lists_free(Lists *L)
+{
+    free(L->start);
+    free(L->idx);
+    memset(L, 0, sizeof(*L));
+}
+
+/* Builds, for each of the first `ntarget` need_neigh particles (all of them
+ * when ntarget == (size_t)-1), the list: every particle of its own bucket
+ * (neighs.cc:89-92), then, for the 26 adjacent buckets in x-major order
+ * (preprocess.cc:287-313), the particles inside the list_factor*h_i box
+ * (neighs.cc:84,117-131).  Particles of one bucket keep index order. */
+static int build_lists_3d(const PlumeOptions *o, const PlumeGrid *g,
+                          const PlumeSoA *s, size_t n, size_t ntarget,
+                          Lists *L, int nthreads)
+{
+    long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
+    long *bk = (long *)malloc(sizeof(long) * (n ? n : 1));
+    size_t *bstart = (size_t *)calloc((size_t)nbk + 1, sizeof(size_t));
+    int32_t *bidx = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    if (!bk || !bstart || !bidx) { free(bk); free(bstart); free(bidx); return PLUME_E_INVALID; }
+    for (size_t i = 0; i < n; i++) {
+        bk[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
+        if (bk[i] < 0) { free(bk); free(bstart); free(bidx); return PLUME_E_OUTSIDE_GRID; }
+        bstart[bk[i] + 1]++;
+    }
+    for (long b = 0; b < nbk; b++) bstart[b + 1] += bstart[b];
+    {
+        size_t *fill = (size_t *)malloc(sizeof(size_t) * (size_t)(nbk ? nbk : 1));
+        memcpy(fill, bstart, sizeof(size_t) * (size_t)nbk);
+        for (size_t i = 0; i < n; i++) bidx[fill[bk[i]]++] = (int32_t)i;
+        free(fill);
+    }
+    /* targets */
+    size_t nt = 0;
+    for (size_t i = 0; i < n; i++)
+        if (need_neigh(s->bc_type[i]) && nt < ntarget) nt++;
+    L->start = (size_t *)calloc(n + 1, sizeof(size_t));
+    size_t *cnt = (size_t *)calloc(n + 1, sizeof(size_t));
+    char *is_t = (char *)calloc(n ? n : 1, 1);
+    {
+        size_t c = 0;
+        for (size_t i = 0; i < n && c < nt; i++)
+            if (need_neigh(s->bc_type[i])) { is_t[i] = 1; c++; }
+    }
+    int nbx = g->nb[0], nby = g->nb[1], nbz = g->nb[2];
+    /* two passes: count, then fill */
+    for (int pass = 0; pass < 2; pass++) {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
+        for (long ii = 0; ii < (long)n; ii++) {
+            size_t i = (size_t)ii;
+            if (!is_t[i]) continue;
+            long b = bk[i];
+            int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long)nbx * nby));
+            double hi = o->list_factor * s->h[i];
+            double xi[3] = { s->x[i], s->y[i], s->z[i] };
+            size_t c = 0;
+            int32_t *out = pass ? L->idx + L->start[i] : NULL;
+            for (size_t q = bstart[b]; q < bstart[b + 1]; q++) {
+                if (out) out[c] = bidx[q];
+                c++;
+            }
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        if (!dx && !dy && !dz) continue;
+                        int cx = bx + dx, cy = by + dy, cz = bz + dz;
+                        if (cx < 0 || cx >= nbx || cy < 0 || cy >= nby || cz < 0 || cz >= nbz) continue;
+                        long nb_ = ((long)cz * nby + cy) * nbx + cx;
+                        for (size_t q = bstart[nb_]; q < bstart[nb_ + 1]; q++) {
+                            int32_t j = bidx[q];
+                            double ds[3] = { xi[0] - s->x[j], xi[1] - s->y[j], xi[2] - s->z[j] };
+                            if (in_support(ds, hi, 3)) {
+                                if (out) out[c] = j;
+                                c++;
+                            }
+                        }
+                    }
+            if (!pass) cnt[i] = c;
+        }
+        if (!pass) {
+            L->start[0] = 0;
+            for (size_t i = 0; i < n; i++) L->start[i + 1] = L->start[i] + cnt[i];
+            L->nidx = L->start[n];
+            L->idx = (int32_t *)malloc(sizeof(int32_t) * (L->nidx ? L->nidx : 1));
+        }
+    }
+    free(cnt);
+    free(is_t);
+    free(bk);
+    free(bstart);
+    free(bidx);
+    return PLUME_OK;
+}
+
+/* list access: 1D lists hold every particle in creation order
+ * (add_air.cc:470-479), 3D lists come from build_lists_3d */
+#define FOR_LIST(L, D, n, i, jv, ...)                                         \
+    do {                                                                       \
+        if ((D) == 1) {                                                        \
+            for (size_t q_ = 0; q_ < (n); q_++) { size_t jv = q_; __VA_ARGS__ }\
+        } else {                                                               \
+            for (size_t q_ = (L)->start[i]; q_ < (L)->start[(i) + 1]; q_++) {  \
+                size_t jv = (size_t)(L)->idx[q_]; __VA_ARGS__                  \
+            }                                                                  \
+        }                                                                      \
+    } while (0)
+
+static inline void coords(const PlumeSoA *s, size_t i, int D, double *x)
+{
+    x[0] = s->x[i];
+    if (D == 3) { x[1] = s->y[i]; x[2] = s->z[i]; }
+}
+static inline void vel(const PlumeSoA *s, size_t i, int D, int smoothed, double *v)
+{
+    if (smoothed) {
+        v[0] = s->vsx[i];
+        if (D == 3) { v[1] = s->vsy[i]; v[2] = s->vsz[i]; }
+    } else {
+        v[0] = s->vx[i];
+        if (D == 3) { v[1] = s->vy[i]; v[2] = s->vz[i]; }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* adaptive_sml, neighs.cc:479-693 (ADAPTIVE_SML == 1)                  */
+/* ------------------------------------------------------------------ */
+static int adaptive_pass(const PlumeOptions *o, PlumeSoA *s, size_t n,
+                         const Lists *L, int nthreads, size_t ntarget)
+{
+    const int D = o->dim;
+    int err = PLUME_OK;
+    size_t seen = 0;
+    (void)seen;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue; /* not a target */
+        double xi[3];
+        coords(s, i, D, xi);
+        for (int loop = 0; loop < o->num_loop; loop++) {
+            double H_old = s->h[i];
+            double H_star = H_old * o->c_smooth;
+            double supp = o->cutoff2 * H_star;
+            double rho_star = 0.;
+            FOR_LIST(L, D, n, i, j, {
+                if (contr_dens(s->bc_type[j], o->pghost_contrib)) {
+                    double xj[3], dx[3], si[3];
+                    coords(s, j, D, xj);
+                    for (int k = 0; k < D; k++) {
+                        dx[k] = xi[k] - xj[k];
+                        si[k] = dx[k] / H_star;
+                    }
+                    if (in_support(dx, supp, D)) {
+                        double mj = s->mass[j];
+                        double wght = kw(o->kernel, si, H_star, D);
+                        rho_star += wght * mj;
+                    }
+                }
+            });
+            double H_new;
+            if (D == 3)
+                H_new = o->eta_smooth * cbrt(s->mass[i] / rho_star);
+            else
+                H_new = o->eta_smooth * (s->mass[i] / rho_star);
+            s->h[i] = 1.0 * H_new; /* put_smlen: RATIO_SML_DX * h */
+            if (!(H_new > 0) || !isfinite(H_new)) {
+#pragma omp critical
+                err = PLUME_E_NONPOSITIVE;
+                break;
+            }
+            double errv = fabs((H_new - H_old) / H_old);
+            if (errv < o->thresh) break;
+        }
+    }
+    (void)ntarget;
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* mom_engr_update (USE_GSPH == 0), mom_engr_update.cc:29-439           */
+/* ------------------------------------------------------------------ */
+typedef struct Work {
+    double *nv[3], *ne, *nrho, *nY, *nE;
+} Work;
+
+static int momentum_pass(const PlumeOptions *o, PlumeSoA *s, size_t n,
+                         const Lists *L, double dt, Work *w, int nthreads)
+{
+    const int D = o->dim;
+    const double grav = -o->g; /* gravity[DIMENSION-1], mom_engr_update.cc:53-59 */
+    int err = PLUME_OK;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        double xi[3], veli[3], rhs_v[3] = { 0, 0, 0 }, rhs_e = 0;
+        coords(s, i, D, xi);
+        double hi = s->h[i];
+        double supp = o->cutoff2 * hi;
+        double pressi = s->p[i];
+        double tempi = s->T[i];
+        double Cp_i = s->cp[i];
+        if (!(s->rho[i] > 0)) {
+#pragma omp critical
+            err = PLUME_E_NONPOSITIVE;
+            continue;
+        }
+        double Vi = 1.0 / s->rho[i];
+        double pvsqi = pressi * Vi * Vi;
+        vel(s, i, D, o->lans, veli);
+        FOR_LIST(L, D, n, i, j, {
+            if (j != i) {
+                double xj[3], dx[3], si[3], dist_sq = 0;
+                coords(s, j, D, xj);
+                double h = 0.5 * (hi + s->h[j]);
+                for (int k = 0; k < D; k++) {
+                    dx[k] = xi[k] - xj[k];
+                    si[k] = dx[k] / h;
+                    dist_sq += dx[k] * dx[k];
+                }
+                if (in_support(dx, supp, D)) {
+                    double mj = s->mass[j];
+                    double pressj = s->p[j];
+                    double Vj = 1.0 / s->rho[j];
+                    double velj[3], velij[3], dwdxi[3];
+                    vel(s, j, D, o->lans, velj);
+                    for (int k = 0; k < D; k++) velij[k] = veli[k] - velj[k];
+                    double rhoab = 0.5 * (s->rho[i] + s->rho[j]);
+                    double sndspdab = 0.5 * (s->c[i] + s->c[j]);
+                    double vis = art_vis(o, rhoab, sndspdab, dx, velij, dist_sq, h, D);
+                    if (o->lans) vis -= eps_mom(velij, Vj, D);
+                    double mpvsqij = mj * (pressj * Vj * Vj + pvsqi + vis);
+                    for (int k = 0; k < D; k++) dwdxi[k] = kdw(o->kernel, si, h, k, D);
+                    double heat_tran = 0.;
+                    if (o->lans) {
+                        double Cp_ij = 0.5 * (s->cp[j] + Cp_i);
+                        double hab = 0.5 * (hi + s->h[j]);
+                        double kij = eps_heat(Cp_ij, dx, velij, hab, sndspdab, D);
+                        double Fij = compute_F(dwdxi, dx, D);
+                        heat_tran = mj * Vj * Vi * kij * (tempi - s->T[j]) * Fij;
+                    }
+                    for (int k = 0; k < D; k++) rhs_v[k] -= mpvsqij * dwdxi[k];
+                    double deltae = 0.;
+                    for (int k = 0; k < D; k++) deltae += 0.5 * (mpvsqij * dwdxi[k]) * velij[k];
+                    rhs_e += (deltae + heat_tran);
+                }
+            }
+        });
+        double vi[3];
+        vel(s, i, D, 0, vi);
+        double unew[3];
+        for (int k = 0; k < D; k++) unew[k] = vi[k] + dt * (rhs_v[k]);
+        unew[D - 1] += dt * grav;
+        for (int k = 0; k < D; k++) w->nv[k][i] = unew[k];
+        w->ne[i] = s->e[i] + dt * (rhs_e + veli[D - 1] * grav);
+    }
+    if (err) return err;
+    /* commit loop, mom_engr_update.cc:412-432 */
+    for (size_t i = 0; i < n; i++) {
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        s->vx[i] = w->nv[0][i];
+        if (D == 3) { s->vy[i] = w->nv[1][i]; s->vz[i] = w->nv[2][i]; }
+        s->e[i] = w->ne[i];
+        eos(o, s, i);
+    }
+    return PLUME_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* smooth_density, density_massfrac.cc:25-359                           */
+/* (DENSITY_UPDATE_SML 11, DENSITY_UPDATE_SPH 11, HAVE_ENERGY_SMOOTH)   */
+/* ------------------------------------------------------------------ */
+static int density_pass(const PlumeOptions *o, PlumeSoA *s, size_t n,
+                        const Lists *L, Work *w, int nthreads)
+{
+    const int D = o->dim;
+    int err = PLUME_OK;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        double xi[3];
+        coords(s, i, D, xi);
+        double hi0 = s->h[i];
+        double supp = o->cutoff2 * hi0;
+        double tmprho[2] = { 0., 0. };
+        double wnorm_e = 0.0, engr = 0.0;
+        FOR_LIST(L, D, n, i, j, {
+            if (contr_dens(s->bc_type[j], o->pghost_contrib)) {
+                double mj = s->mass[j];
+                double rhoj = s->rho[j];
+                int ph = s->phase[j];
+                if (ph == 1 || ph == 2) {
+                    double xj[3], ds[3], sv[3];
+                    coords(s, j, D, xj);
+                    for (int k = 0; k < D; k++) ds[k] = xi[k] - xj[k];
+                    if (in_support(ds, supp, D)) {
+                        double hh = 0.5 * (s->h[i] + s->h[j]);
+                        for (int k = 0; k < D; k++) sv[k] = ds[k] / hh;
+                        if (o->energy_smooth) {
+                            double s_e[3];
+                            for (int k = 0; k < D; k++) s_e[k] = OR_E_SMOOTH * ds[k] / hh;
+                            double wm_e = kw(o->kernel, s_e, hh / OR_E_SMOOTH, D) * mj;
+                            wnorm_e += wm_e / rhoj;
+                            engr += wm_e * s->e[j] / rhoj;
+                        }
+                        double wght = kw(o->kernel, sv, hh, D);
+                        double wm = wght * mj;
+                        tmprho[ph - 1] += wm;
+                    }
+                }
+            }
+        });
+        double density = 0.0;
+        if (o->energy_smooth) {
+            if (!(wnorm_e > 0)) {
+#pragma omp critical
+                err = PLUME_E_NONPOSITIVE;
+                continue;
+            }
+            engr = engr / wnorm_e;
+            w->nE[i] = engr;
+        }
+        density += tmprho[0];
+        density += tmprho[1];
+        double mssfrc = tmprho[1] / density;
+        if (!(density > 0)) {
+#pragma omp critical
+            err = PLUME_E_NONPOSITIVE;
+            continue;
+        }
+        w->nrho[i] = density;
+        w->nY[i] = mssfrc;
+    }
+    if (err) return err;
+    /* commit loop, density_massfrac.cc:337-352 */
+    for (size_t i = 0; i < n; i++) {
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        s->Y[i] = w->nY[i];
+        if (s->Y[i] >= OR_MSFRC_TH && s->involved[i] != 2) s->involved[i] = 2;
+        s->rho[i] = w->nrho[i];
+        if (o->energy_smooth) s->e[i] = w->nE[i];
+        eos(o, s, i);
+    }
+    return PLUME_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* smooth_velocity, smooth_velocity.cc:25-165 (HAVE_TURBULENCE_LANS 1)   */
+/* ------------------------------------------------------------------ */
+static int velocity_pass(const PlumeOptions *o, PlumeSoA *s, size_t n,
+                         const Lists *L, int nthreads)
+{
+    const int D = o->dim;
+    int err = PLUME_OK;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        double xi[3], vi[3], temp_dv[3] = { 0, 0, 0 }, wnorm = 0.;
+        coords(s, i, D, xi);
+        vel(s, i, D, 0, vi);
+        double hi = s->h[i];
+        double supp = o->cutoff2 * hi;
+        FOR_LIST(L, D, n, i, j, {
+            if (contr_vel_smooth(s->bc_type[j])) {
+                double xj[3], ds[3], sv[3], vj[3];
+                coords(s, j, D, xj);
+                for (int k = 0; k < D; k++) ds[k] = xi[k] - xj[k];
+                if (in_support(ds, supp, D)) {
+                    double rhoj = s->rho[j];
+                    double mj = s->mass[j];
+                    for (int k = 0; k < D; k++) sv[k] = ds[k] / hi;
+                    double wght = kw(o->kernel, sv, hi, D);
+                    double mvw = wght * mj / rhoj;
+                    vel(s, j, D, 0, vj);
+                    for (int k = 0; k < D; k++) temp_dv[k] += mvw * (vj[k] - vi[k]);
+                    wnorm += mvw;
+                }
+            }
+        });
+        if (!(wnorm > 0)) {
+#pragma omp critical
+            err = PLUME_E_NONPOSITIVE;
+            continue;
+        }
+        for (int k = 0; k < D; k++) temp_dv[k] /= wnorm;
+        s->vsx[i] = vi[0] + temp_dv[0];
+        if (D == 3) {
+            s->vsy[i] = vi[1] + temp_dv[1];
+            s->vsz[i] = vi[2] + temp_dv[2];
+        }
+    }
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* timestep, timestep.cc:94-135 (3D) and :139-183 (1D)                  */
+/* ------------------------------------------------------------------ */
+static int timestep(const PlumeOptions *o, const PlumeSoA *s, size_t n, double *out)
+{
+    double dt = 1.0E+10;
+    for (size_t i = 0; i < n; i++) {
+        if (!need_neigh(s->bc_type[i])) continue;
+        double c = s->c[i];
+        if (!(c > 0)) return PLUME_E_NONPOSITIVE;
+        double temp = s->h[i] / c;
+        if (temp < dt) dt = temp;
+    }
+    *out = o->cfl * dt;
+    return PLUME_OK;
+}
+
+/* TimeProps::incrtime, properties.h:71-83 */
+static void incrtime(const PlumeOptions *o, OracleTime *t, double *dt)
+{
+    if ((t->time + (*dt)) > t->ndtimeoutput) (*dt) = t->ndtimeoutput - t->time;
+    if ((t->time + (*dt)) > o->max_time) (*dt) = o->max_time - t->time;
+    t->time += (*dt);
+    t->dtime = (*dt);
+    t->step++;
+}
+/* TimeProps::ifoutput, properties.h:100-118 */
+static void ifoutput(const PlumeOptions *o, OracleTime *t)
+{
+    if (t->time >= t->ndtimeoutput || t->time == o->max_time) {
+        t->ioutput++;
+        t->ndtimeoutput = ((t->ioutput + 1) * o->timeoutput) / 1.0;
+    }
+}
+/* TimeProps::iferupt, properties.h:123-131 */
+static int iferupt(const PlumeOptions *o, const OracleTime *t)
+{
+    if ((t->time * 1.0) < o->stat_erupt) return 0;
+    if ((t->time * 1.0) > o->end_erupt) return 0;
+    return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* update_pos, update_pos.cc:34-168                                     */
+/* ------------------------------------------------------------------ */
+static void update_pos(const PlumeOptions *o, PlumeSoA *s, size_t n,
+                       const OracleTime *t)
+{
+    const int D = o->dim;
+    double dt = t->dtime;
+    int erupt = iferupt(o, t);
+    for (size_t i = 0; i < n; i++) {
+        uint8_t bc = s->bc_type[i];
+        if (is_real(bc)) {
+            double v[3];
+            vel(s, i, D, o->lans, v);
+            s->x[i] = s->x[i] + dt * v[0];
+            if (D == 3) {
+                s->y[i] = s->y[i] + dt * v[1];
+                s->z[i] = s->z[i] + dt * v[2];
+            }
+        } else if (bc == 0 && erupt) {
+            double v[3];
+            vel(s, i, D, 0, v);
+            s->x[i] = s->x[i] + dt * v[0];
+            if (D == 3) {
+                s->y[i] = s->y[i] + dt * v[1];
+                s->z[i] = s->z[i] + dt * v[2];
+                if (s->z[i] >= o->vent_z) {
+                    s->bc_type[i] = 100;       /* erupt_turn_real         */
+                    s->h[i] = 1.0 * o->sml_phase2; /* put_smlen           */
+                    s->involved[i] = 2;        /* set_involved_flag       */
+                }
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* update_particles_in_bucket, update_pos.cc:171-463 (serial case)      */
+/* Returns the number of deleted particles in *lost_out.                */
+/* ------------------------------------------------------------------ */
+static void compact(PlumeSoA *s, size_t *n, const char *del);
+
+static int rebucket(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                    size_t *n, const long *old_bucket, size_t *lost_out)
+{
+    size_t nn = *n, lost = 0;
+    char *del = (char *)calloc(nn ? nn : 1, 1);
+    int err = PLUME_OK;
+    for (size_t i = 0; i < nn; i++) {
+        uint8_t bc = s->bc_type[i];
+        if (!(is_real(bc) || bc == 0)) continue;
+        long ob = old_bucket[i];
+        uint8_t of = bucket_flags(g, ob);
+        if (of & PLUME_BUCKET_INACTIVE) continue;
+        double pos[3] = { s->x[i], s->y[i], s->z[i] };
+        if (is_real(bc) && (of & PLUME_BUCKET_MIXED) && g->face_index) {
+            /* Bucket::determine_escape, bucket.cc:435-452 */
+            const int8_t *fi = g->face_index + 6 * ob;
+            int los = 0;
+            for (int a = 0; a < 3; a++) {
+                if (fi[2 * a] == -1) {
+                    if ((pos[a] - g->domain_lo[a]) < -OR_TINY) los = 1;
+                } else if (fi[2 * a + 1] == 1) {
+                    if ((pos[a] - g->domain_hi[a]) > OR_TINY) los = 1;
+                }
+            }
+            if (los) { del[i] = 1; lost++; continue; }
+        }
+        long nb_ = bucket_of(g, pos[0], pos[1], pos[2]);
+        if (nb_ < 0) { err = PLUME_E_OUTSIDE_GRID; break; }
+        if (nb_ != ob && (bucket_flags(g, nb_) & PLUME_BUCKET_ABSORBING)) {
+            del[i] = 1;
+            lost++;
+        }
+    }
+    if (!err) compact(s, n, del);
+    free(del);
+    *lost_out = lost;
+    return err;
+}
+
+#define SOA_D(f) if (s->f) s->f[w] = s->f[r];
+static void compact(PlumeSoA *s, size_t *n, const char *del)
+{
+    size_t w = 0;
+    for (size_t r = 0; r < *n; r++) {
+        if (del[r]) continue;
+        if (w != r) {
+            SOA_D(key) SOA_D(x) SOA_D(y) SOA_D(z) SOA_D(vx) SOA_D(vy) SOA_D(vz)
+            SOA_D(vsx) SOA_D(vsy) SOA_D(vsz) SOA_D(mass) SOA_D(h) SOA_D(rho)
+            SOA_D(e) SOA_D(p) SOA_D(Y) SOA_D(gamma) SOA_D(c) SOA_D(T) SOA_D(cp)
+            SOA_D(phase) SOA_D(bc_type) SOA_D(involved)
+        }
+        w++;
+    }
+    *n = w;
+}
+#undef SOA_D
+
+static int alloc_work(Work *w, size_t n)
+{
+    size_t m = n ? n : 1;
+    w->nv[0] = (double *)malloc(sizeof(double) * m);
+    w->nv[1] = (double *)malloc(sizeof(double) * m);
+    w->nv[2] = (double *)malloc(sizeof(double) * m);
+    w->ne = (double *)malloc(sizeof(double) * m);
+    w->nrho = (double *)malloc(sizeof(double) * m);
+    w->nY = (double *)malloc(sizeof(double) * m);
+    w->nE = (double *)malloc(sizeof(double) * m);
+    return (w->nv[0] && w->nv[1] && w->nv[2] && w->ne && w->nrho && w->nY && w->nE)
+               ? PLUME_OK : PLUME_E_INVALID;
+}
+static void free_work(Work *w)
+{
+    free(w->nv[0]); free(w->nv[1]); free(w->nv[2]);
+    free(w->ne); free(w->nrho); free(w->nY); free(w->nE);
+}
+
+static int check_opts(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s)
+{
+    if (!o || !s) return PLUME_E_INVALID;
+    if (o->dim != 1 && o->dim != 3) return PLUME_E_INVALID;
+    if (o->dim == 3 && (!g || !s->y || !s->z || !s->vy || !s->vz)) return PLUME_E_INVALID;
+    return PLUME_OK;
+}
+
+static int nthreads_of(int nthreads)
+{
+#ifdef _OPENMP
+    return nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+    (void)nthreads;
+    return 1;
+#endif
+}
+
+int oracle_adaptive(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                    size_t n, int nthreads)
+{
+    int rc = check_opts(o, g, s);
+    if (rc) return rc;
+    nthreads = nthreads_of(nthreads);
+    Lists L = { 0 };
+    if (o->dim == 3) {
+        rc = build_lists_3d(o, g, s, n, (size_t)-1, &L, nthreads);
+        if (rc) return rc;
+    }
+    rc = adaptive_pass(o, s, n, &L, nthreads, (size_t)-1);
+    lists_free(&L);
+    return rc;
+}
+
+/* One step of the hot loop: 3D main.cc:217-471, 1D main.cc:676-750. */
+int oracle_steps(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                 size_t *n, OracleTime *t, int nsteps, double *dt_log,
+                 int nthreads)
+{
+    int rc = check_opts(o, g, s);
+    if (rc) return rc;
+    nthreads = nthreads_of(nthreads);
+    const int D = o->dim;
+    for (int st = 0; st < nsteps; st++) {
+        size_t nn = *n;
+        double dt;
+        rc = timestep(o, s, nn, &dt);
+        if (rc) return rc;
+        incrtime(o, t, &dt);
+        if (dt_log) dt_log[st] = dt;
+        Lists L = { 0 };
+        long *oldb = NULL;
+        if (D == 3) {
+            rc = build_lists_3d(o, g, s, nn, (size_t)-1, &L, nthreads);
+            if (rc) return rc;
+            oldb = (long *)malloc(sizeof(long) * (nn ? nn : 1));
+            for (size_t i = 0; i < nn; i++) oldb[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
+        }
+        Work w;
+        if (alloc_work(&w, nn)) { lists_free(&L); free(oldb); return PLUME_E_INVALID; }
+        int interval = o->sml_interval > 0 ? o->sml_interval : 1;
+        if (o->adaptive_sml && (t->step % interval) == 0)
+            rc = adaptive_pass(o, s, nn, &L, nthreads, (size_t)-1);
+        if (!rc) rc = momentum_pass(o, s, nn, &L, t->dtime, &w, nthreads);
+        if (!rc) rc = density_pass(o, s, nn, &L, &w, nthreads);
+        if (!rc && o->lans) rc = velocity_pass(o, s, nn, &L, nthreads);
+        free_work(&w);
+        lists_free(&L);
+        if (rc) { free(oldb); return rc; }
+        update_pos(o, s, nn, t);
+        if (D == 3) {
+            size_t lost = 0;
+            rc = rebucket(o, g, s, n, oldb, &lost);
+            free(oldb);
+            if (rc) return rc;
+        }
+        ifoutput(o, t);
+    }
+    return PLUME_OK;
+}
+
+int oracle_pairs(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
+                 size_t n, int mode, uint64_t *key_i, uint64_t *key_j,
+                 size_t cap, size_t *npairs)
+{
+    int rc = check_opts(o, g, s);
+    if (rc) return rc;
+    const int D = o->dim;
+    Lists L = { 0 };
+    if (D == 3) {
+        rc = build_lists_3d(o, g, s, n, (size_t)-1, &L, nthreads_of(0));
+        if (rc) return rc;
+    }
+    size_t c = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (!need_neigh(s->bc_type[i])) continue;
+        double xi[3];
+        coords(s, i, D, xi);
+        double hi = s->h[i];
+        FOR_LIST((&L), D, n, i, j, {
+            int take = 1;
+            if (mode == 1) {
+                double xj[3], dx[3], si[3];
+                coords(s, j, D, xj);
+                double h = 0.5 * (hi + s->h[j]);
+                for (int k = 0; k < D; k++) { dx[k] = xi[k] - xj[k]; si[k] = dx[k] / h; }
+                take = (j != i) && in_support(dx, o->cutoff2 * hi, D) &&
+                       kw(o->kernel, si, h, D) != 0.0;
+            }
+            if (take) {
+                if (c < cap && key_i && key_j) { key_i[c] = s->key[i]; key_j[c] = s->key[j]; }
+                c++;
+            }
+        });
+    }
+    lists_free(&L);
+    *npairs = c;
+    return PLUME_OK;
+}
+
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+double oracle_sample_step_seconds(const PlumeOptions *o, const PlumeGrid *g,
+                                  const PlumeSoA *s0, size_t n, size_t ntarget,
+                                  int nthreads)
+{
+    if (check_opts(o, g, s0) || o->dim != 3) return -1.0;
+    nthreads = nthreads_of(nthreads);
+    /* private copy of the state so the caller's arrays stay untouched */
+    PlumeSoA s = { 0 };
+    double *dbuf = (double *)malloc(sizeof(double) * 20 * (n ? n : 1));
+    uint8_t *bbuf = (uint8_t *)malloc(3 * (n ? n : 1));
+    uint64_t *kbuf = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
+    if (!dbuf || !bbuf || !kbuf) { free(dbuf); free(bbuf); free(kbuf); return -1.0; }
+    double *const src[20] = { s0->x, s0->y, s0->z, s0->vx, s0->vy, s0->vz, s0->vsx,
+                              s0->vsy, s0->vsz, s0->mass, s0->h, s0->rho, s0->e, s0->p,
+                              s0->Y, s0->gamma, s0->c, s0->T, s0->cp, NULL };
+    double **dst[19] = { &s.x, &s.y, &s.z, &s.vx, &s.vy, &s.vz, &s.vsx, &s.vsy, &s.vsz,
+                         &s.mass, &s.h, &s.rho, &s.e, &s.p, &s.Y, &s.gamma, &s.c, &s.T, &s.cp };
+    for (int f = 0; f < 19; f++) {
+        *dst[f] = dbuf + (size_t)f * n;
+        memcpy(*dst[f], src[f], sizeof(double) * n);
+    }
+    s.phase = bbuf; s.bc_type = bbuf + n; s.involved = bbuf + 2 * n;
+    memcpy(s.phase, s0->phase, n);
+    memcpy(s.bc_type, s0->bc_type, n);
+    memcpy(s.involved, s0->involved, n);
+    s.key = kbuf;
+    memcpy(s.key, s0->key, sizeof(uint64_t) * n);
+
+    double t0 = now_s();
+    double dt;
+    int rc = timestep(o, &s, n, &dt);
+    Lists L = { 0 };
+    if (!rc) rc = build_lists_3d(o, g, &s, n, ntarget, &L, nthreads);
+    Work w;
+    if (!rc) rc = alloc_work(&w, n);
+    if (!rc) {
+        if (o->adaptive_sml) {
+            /* adaptive_sml runs every sml_interval steps: charge its share */
+            double ta = now_s();
+            adaptive_pass(o, &s, n, &L, nthreads, ntarget);
+            double share = (now_s() - ta) * (1.0 - 1.0 / (o->sml_interval > 0 ? o->sml_interval : 1));
+            t0 += share;
+        }
+        momentum_pass(o, &s, n, &L, dt, &w, nthreads);
+        density_pass(o, &s, n, &L, &w, nthreads);
+        if (o->lans) velocity_pass(o, &s, n, &L, nthreads);
+        OracleTime tt = { 0, dt, 1e30, 1, 0 };
+        update_pos(o, &s, n, &tt);
+        free_work(&w);
+    }
+    double t1 = now_s();
+    lists_free(&L);
+    free(dbuf); free(bbuf); free(kbuf);
+    return rc ? -1.0 : (t1 - t0);
+}

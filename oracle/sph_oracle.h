@@ -1,0 +1,64 @@
+/*
+ * sph_oracle.h -- CPU oracle of the Plume-SPH particle step.
+ *
+ * TEST INFRASTRUCTURE.  This is the checker, not the product: only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm may
+ * load it.  It restates, in plain C over structure-of-arrays particles, the
+ * per-step algorithm of the reference solver (file:line citations in
+ * sph_oracle.c) with the reference's operation order, so that it agrees with
+ * the reference build (oracle/_ref, see oracle/Makefile) to the last bit on
+ * the first step and to rounding afterwards.
+ *
+ * Parity pin: tests/test_oracle_golden.py checks this oracle against golden
+ * vectors produced by running the reference's own source files
+ * (tests/golden/make_golden.py).
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "../include/plume_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* TimeProps (src/datstr/properties.h:17-69) with TIME_SCALE = 1. */
+typedef struct OracleTime {
+    double time;          /* current time                                   */
+    double dtime;         /* dt of the last step                            */
+    double ndtimeoutput;  /* next output time                               */
+    int    step;
+    int    ioutput;
+} OracleTime;
+
+/* One adaptive_sml pass (neighs.cc:479-693) with the current lists. */
+int oracle_adaptive(const PlumeOptions *opt, const PlumeGrid *grid,
+                    PlumeSoA *s, size_t n, int nthreads);
+
+/* nsteps steps of the hot loop.  *n is updated when particles are deleted
+ * (arrays are compacted in order).  dt_log (may be NULL) receives the
+ * clipped dt of each step.  Returns PLUME_OK or a PLUME_E_* code. */
+int oracle_steps(const PlumeOptions *opt, const PlumeGrid *grid,
+                 PlumeSoA *s, size_t *n, OracleTime *t, int nsteps,
+                 double *dt_log, int nthreads);
+
+/* Neighbour pairs, same modes as plume_neighbor_pairs(). */
+int oracle_pairs(const PlumeOptions *opt, const PlumeGrid *grid,
+                 const PlumeSoA *s, size_t n, int mode,
+                 uint64_t *key_i, uint64_t *key_j, size_t cap, size_t *npairs);
+
+/* Bounded CPU sample of one step: the neighbour search and the pair sweeps
+ * of a step run for the first `ntarget` need_neigh particles only (all
+ * other work of the step is per-particle streaming and is included for all
+ * particles).  Returns the wall seconds, or a negative value on error.
+ * The particle state is not modified. */
+double oracle_sample_step_seconds(const PlumeOptions *opt,
+                                  const PlumeGrid *grid, const PlumeSoA *s,
+                                  size_t n, size_t ntarget, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

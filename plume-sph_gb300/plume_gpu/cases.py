@@ -1,0 +1,381 @@
+"""Workload builders: particles, bucket grid and options of each workload.
+
+The host-side set-up keeps the reference's conventions (its set-up code is
+not part of the accelerated path):
+
+* 1D shock tubes follow set_up_shock_tube (src/plume/add_air.cc:37-485):
+  creation order (left no-save reals, left ghosts, left reals, right reals,
+  right no-save reals, right ghosts), equal mass (EQUAL_PART_MASS) or equal
+  spacing, ghost h = 1.1 dx (ADAPTIVE_SML_GHOST 11), initial gamma 1.4 and
+  sound speed 340 from the Particle constructor (particle.cc:422-520).
+* The 3D plume follows the bucket geometry of the preprocessor
+  (src/preproc/preprocess.cc:100-177: bucket edge PARTICLE_DENSITY*h0, domain
+  padded by 1.5 buckets, bucket types of determine_bucket_type :404-439), a
+  cubic air lattice in the original domain, pressure ghosts (bc 1) on the
+  sides and top, wall ghosts (bc 2) under the ground and an eruption duct of
+  erupt ghosts (bc 0) under the vent like setup_erupt (setup_erupt.cc:44-387:
+  a lattice centred on the vent axis, depth 1.5*8*h0, pressure-balanced
+  mixture density rhov = pv0/(Rg*Tv0)/ng0, energy ev0).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .abi import (BC_ERUPT, BC_NOSAVE_REAL, BC_PRESSURE, BC_REAL, BC_WALL,
+                  BUCKET_ABSORBING, BUCKET_MIXED, KERNEL_GAUSS, KERNEL_M4,
+                  PREC_FP64, Grid, Options, ParticleSet)
+
+
+@dataclass
+class Case:
+    name: str
+    options: Options
+    grid: Grid
+    particles: ParticleSet
+    pre_adaptive: bool = False   # 1D main calls adaptive_sml once before the loop
+    step0: int = 0               # TimeProps::step at the start
+    info: dict | None = None
+
+
+def _f32(v: float) -> float:
+    return float(np.float32(v))
+
+
+# ----------------------------------------------------------------------------
+# 1D shock tubes
+# ----------------------------------------------------------------------------
+def _shock_tube(rho_l, p_l, u_l, rho_r, p_r, u_r, middle, lo, hi, s0, nb, nnsrp_l,
+                nnsrp_r, equal_mass):
+    """Particle placement of set_up_shock_tube (add_air.cc:37-485).
+
+    When the no-save-real count on the left is 0 the first left ghost sits
+    at lo - dx/2 (the reference leaves that start position unset)."""
+    dx_l = s0
+    dx_r = dx_l * rho_l / rho_r if equal_mass else s0
+    smlen = max(dx_r, dx_l)
+    dx2_l = 0.5 * dx_l
+    gmm, sndspd = 1.4, 340.0
+    rows = []  # (x, m, h, rho, u, p, bc, involved)
+
+    def rho_at(x):
+        return rho_r if x > middle else rho_l
+
+    def p_at(x):
+        return p_r if x > middle else p_l
+
+    def u_at(x):
+        return u_r if x > middle else u_l
+
+    x = lo - dx2_l
+    for k in range(nnsrp_l):
+        x = lo - (dx2_l + k * dx_l)
+        d = rho_at(x)
+        rows.append((x, d * dx_l, smlen, d, u_l, p_l, BC_NOSAVE_REAL, 0))
+    if nnsrp_l == 0:
+        x = lo - dx2_l + dx_l
+    for k in range(nb):
+        x -= dx_l
+        d = rho_at(x)
+        rows.append((x, d * dx_l, dx_l * 1.1, d, u_l, p_l, BC_ERUPT, 0))
+    x = lo + dx2_l
+    while x <= middle:
+        d = rho_at(x)
+        rows.append((x, d * dx_l, smlen, d, u_at(x), p_at(x), BC_REAL, 2))
+        x += dx_l
+    x = x - dx_l + dx_r
+    while x <= hi:
+        d = rho_at(x)
+        rows.append((x, d * dx_r, smlen, d, u_at(x), p_at(x), BC_REAL, 2))
+        x += dx_r
+    for k in range(nnsrp_r):
+        d = rho_at(x)
+        rows.append((x, d * dx_r, smlen, d, u_r, p_r, BC_NOSAVE_REAL, 2))
+        x += dx_r
+    for k in range(nb):
+        d = rho_at(x)
+        rows.append((x, d * dx_r, dx_r * 1.1, d, u_r, p_r, BC_ERUPT, 2))
+        x += dx_r
+    n = len(rows)
+    ps = ParticleSet(n)
+    arr = np.array([r[:6] for r in rows], dtype=np.float64)
+    ps.key[:] = np.arange(n, dtype=np.uint64)
+    ps.x[:] = arr[:, 0]
+    ps.mass[:] = arr[:, 1]
+    ps.h[:] = arr[:, 2]
+    ps.rho[:] = arr[:, 3]
+    ps.vx[:] = arr[:, 4]
+    ps.p[:] = arr[:, 5]
+    ps.e[:] = ps.p / ((gmm - 1) * ps.rho)
+    ps.gamma[:] = gmm
+    ps.c[:] = sndspd
+    ps.Y[:] = 0.0
+    ps.phase[:] = 1
+    ps.bc_type[:] = np.array([r[6] for r in rows], dtype=np.uint8)
+    ps.involved[:] = np.array([r[7] for r in rows], dtype=np.uint8)
+    return ps
+
+
+def options_1d(kernel=KERNEL_GAUSS, eta=1.0, cfl=0.1, cva=717.0, precision=PREC_FP64,
+               max_time=0.2, timeoutput=0.1) -> Options:
+    """1D switches of src/plume/options.h:16-410 with USE_GSPH=0 and the 1D
+    constants of parameters.h:1225-1448."""
+    return Options(dim=1, precision=precision, kernel=kernel, lans=0, energy_smooth=0,
+                   pghost_contrib=2, adaptive_sml=1, sml_interval=1, num_loop=5,
+                   thresh=1e-5, c_smooth=2.0, eta_smooth=eta, alpha=1.0, beta=2.0,
+                   ata=0.01, cfl=cfl, cutoff2=12.0, list_factor=4.25, g=0.0, ng0=0.05,
+                   cvs=1100.0, cvg=1348.0, cva=cva, rg=462.0, ra=287.0, vent_z=0.0,
+                   sml_phase2=0.0, max_time=_f32(max_time), timeoutput=_f32(timeoutput),
+                   stat_erupt=0.0, end_erupt=7200.0)
+
+
+def _grid_1d(ps: ParticleSet, opt: Options, cells_per_h: float = 0.5) -> Grid:
+    """A 1D cell grid over the particle span (tiling of the GPU sweeps only;
+    1D neighbour lists are every particle, add_air.cc:470-479)."""
+    span_lo = float(ps.x.min())
+    span_hi = float(ps.x.max())
+    hmax = float(ps.h.max())
+    pad = 8.0 * max(hmax, (span_hi - span_lo) * 1e-3)
+    lo = span_lo - pad
+    hi = span_hi + pad
+    cell = max(hmax * cells_per_h, (hi - lo) / 2.0e6)
+    nb = int(math.ceil((hi - lo) / cell))
+    return Grid(mindom=(lo, 0.0, 0.0), del_=cell, nb=(nb, 1, 1), subcells=1,
+                domain_lo=(lo, 0.0, 0.0), domain_hi=(hi, 0.0, 0.0))
+
+
+def sod_1d(n_real: int = 2000, ghosts: int = 10, kernel: int = KERNEL_M4,
+           precision: int = PREC_FP64, t_end: float = 0.2,
+           states=((1.0, 1.0, 0.0), (0.125, 0.1, 0.0))) -> Case:
+    """The 1D Sod workload: [0,1] split at 0.5, equal-mass particles, ideal
+    gas gamma = 1.4 (R = 287, Cv = 717.5), h = 1.3 m/rho, alpha=1, beta=2,
+    CFL 0.3, `ghosts` ghosts per end, cubic-spline kernel."""
+    (rl, pl, ul), (rr, pr, ur) = states
+    # input smoothing length (simulation.data, read with stof) giving n_real
+    target = 0.5 / n_real * (1 + rr / rl)
+    best = None
+    for k in range(-400, 401):
+        s0 = _f32(target * (1 + k * 2e-5))
+        ps = _shock_tube(rl, pl, ul, rr, pr, ur, 0.5, 0.0, 1.0, s0, ghosts, 0, 0, True)
+        nr = int(ps.need_neigh().sum())
+        if nr == n_real:
+            best = (abs(k), s0, ps)
+            if k >= 0:
+                break
+    if best is None:
+        raise ValueError(f"no spacing gives {n_real} particles")
+    s0, ps = best[1], best[2]
+    opt = options_1d(kernel=kernel, eta=1.3, cfl=0.3, cva=717.5, precision=precision,
+                     max_time=t_end, timeoutput=t_end / 2)
+    opt.capacity = ps.n
+    return Case("sod_1d", opt, _grid_1d(ps, opt), ps, pre_adaptive=True,
+                info={"s0": s0, "n_real": n_real, "ghosts_per_end": ghosts})
+
+
+def shock_tube_1d(test: int = 1, s0: float = 0.003, kernel: int = KERNEL_GAUSS,
+                  precision: int = PREC_FP64) -> Case:
+    """The reference's shipped 1D shock-tube deck (SHOCK_TUBE_TESTS 1,
+    bin/simulation_1D_shocktube_Sod.data): [-0.4,0.4] split at 0, rho 1/0.25,
+    p 1/0.1795, 35 ghosts and 40/20 no-save reals per side, equal spacing,
+    Gaussian kernel, eta 1.0, CFL 0.1, t_end 0.17."""
+    if test != 1:
+        raise ValueError("only SHOCK_TUBE_TESTS 1 is provided")
+    s0 = _f32(s0)
+    ps = _shock_tube(1.0, 1.0, 0.0, 0.25, 0.1795, 0.0, 0.0, -0.4, 0.4, s0, 35, 40, 20, False)
+    opt = options_1d(kernel=kernel, eta=1.0, cfl=0.1, cva=717.0, precision=precision,
+                     max_time=0.17, timeoutput=0.1)
+    opt.capacity = ps.n
+    return Case("shock_tube_1d", opt, _grid_1d(ps, opt), ps, pre_adaptive=True,
+                info={"s0": s0})
+
+
+# ----------------------------------------------------------------------------
+# 3D plume
+# ----------------------------------------------------------------------------
+def atmosphere(z, T0=288.0, lapse=6.5e-3, z_trop=11000.0, p0=101325.0, R=287.0,
+               g=9.80665):
+    """Hydrostatic atmosphere: T = T0 - lapse*z to z_trop, isothermal above."""
+    z = np.asarray(z, dtype=np.float64)
+    zt = np.minimum(z, z_trop)
+    T = T0 - lapse * zt
+    p = p0 * (T / T0) ** (g / (R * lapse))
+    Tt = T0 - lapse * z_trop
+    pt = p0 * (Tt / T0) ** (g / (R * lapse))
+    above = z > z_trop
+    p = np.where(above, pt * np.exp(-g * (z - z_trop) / (R * Tt)), p)
+    T = np.where(above, Tt, T)
+    rho = p / (R * T)
+    return T, p, rho
+
+
+def _face(crd, lo, hi):
+    # determine_face_index, bucket.cc:459-470
+    return -1 if crd < lo else (1 if crd > hi else 0)
+
+
+def plume_grid(lo, hi, h0, subcells=4) -> Grid:
+    """Bucket grid of the preprocessor (preprocess.cc:100-177, :404-439)."""
+    del_ = 8.0 * h0                     # PARTICLE_DENSITY * smoothing length
+    mind = [lo[a] - 1.5 * del_ for a in range(3)]
+    maxd = [hi[a] + 1.5 * del_ for a in range(3)]
+    nb = [int(math.ceil((maxd[a] - mind[a]) / del_)) for a in range(3)]
+    nbk = nb[0] * nb[1] * nb[2]
+    flags = np.zeros(nbk, dtype=np.uint8)
+    face = np.zeros(6 * nbk, dtype=np.int8)
+    for k in range(nb[2]):
+        for j in range(nb[1]):
+            for i in range(nb[0]):
+                b = (k * nb[1] + j) * nb[0] + i
+                c0 = [mind[0] + i * del_, mind[1] + j * del_, mind[2] + k * del_]
+                c1 = [mind[0] + (i + 1) * del_, mind[1] + (j + 1) * del_,
+                      mind[2] + (k + 1) * del_]
+                bt = []
+                for a in range(3):
+                    bt += [_face(c0[a], lo[a], hi[a]), _face(c1[a], lo[a], hi[a])]
+                flag = [abs(bt[2 * a] + bt[2 * a + 1]) for a in range(3)]
+                face[6 * b:6 * b + 6] = bt
+                if 2 in flag:
+                    flags[b] = BUCKET_ABSORBING          # underground or pressure bc
+                elif 1 in flag:
+                    flags[b] = BUCKET_MIXED
+    return Grid(mindom=tuple(mind), del_=del_, nb=tuple(nb), subcells=subcells,
+                flags=flags, face_index=face, domain_lo=tuple(lo), domain_hi=tuple(hi))
+
+
+def options_3d(precision=PREC_FP64, h0=150.0, cva=711.0) -> Options:
+    """3D plume switches (options.h:416-837 with ATMOSPHERE_TYPE 1, USE_GSPH 0)
+    and constants (parameters.h:862-1041 with cp = 998, ash 0.95)."""
+    return Options(dim=3, precision=precision, kernel=KERNEL_GAUSS, lans=1, energy_smooth=1,
+                   pghost_contrib=1, adaptive_sml=1, sml_interval=50, num_loop=2,
+                   thresh=1e-5, c_smooth=2.0, eta_smooth=1.5, alpha=0.3, beta=0.6,
+                   ata=0.01, cfl=0.8, cutoff2=8.0, list_factor=4.25, g=9.80665,
+                   ng0=0.05, cvs=1100.0, cvg=1348.0, cva=cva, rg=462.0, ra=287.0,
+                   vent_z=0.0, sml_phase2=h0, max_time=_f32(1.0e5), timeoutput=_f32(1.0e5),
+                   stat_erupt=0.0, end_erupt=_f32(72000.0), max_per_bucket=1 << 30)
+
+
+def _eos(opt: Options, ps: ParticleSet, sel=slice(None)):
+    """Particle::update_second_var (particle.cc:528-604), vectorised."""
+    Y = ps.Y[sel]
+    na = 1 - Y
+    ng = opt.ng0 * Y
+    ns = Y - ng
+    Cvm = ns * opt.cvs + ng * opt.cvg + na * opt.cva
+    Rm = ng * opt.rg + na * opt.ra
+    Rmg = Rm / (ng + na)
+    gam = 1 + Rm / Cvm
+    desmg = ps.rho[sel] * (na + ng)
+    p = Rmg * desmg * ps.e[sel] / Cvm
+    ps.gamma[sel] = gam
+    ps.p[sel] = p
+    ps.c[sel] = np.sqrt(gam * p / desmg)
+    ps.T[sel] = ps.e[sel] / Cvm
+    if opt.lans:
+        ps.cp[sel] = Cvm
+
+
+def plume_3d(half_width=1.0e4, height=2.0e4, dx=150.0, vent_radius=100.0,
+             vent_velocity=150.0, vent_T=1053.0, ash=0.95, ghost_layers=6,
+             vent_dx=None, duct_depth=None, jitter=0.01, seed=0, precision=PREC_FP64,
+             T0=288.0, lapse=6.5e-3, p0=101325.0, subcells=4, name="plume_3d") -> Case:
+    """The 3D dusty-gas plume workload (20 x 20 x 20 km, 150 m lattice,
+    hydrostatic 288 K atmosphere with 6.5 K/km lapse to 11 km, air cp = 998 and
+    R = 287, vent of radius 100 m at ground centre injecting at 150 m/s and
+    1053 K with ash mass fraction 0.95, outflow ghosts on sides and top,
+    +-1% lattice jitter from `seed`), and smaller copies of it for tests."""
+    opt = options_3d(precision=precision, h0=dx)
+    lo = (-half_width, -half_width, 0.0)
+    hi = (half_width, half_width, height)
+    grid = plume_grid(lo, hi, dx, subcells=subcells)
+    rng = np.random.default_rng(seed)
+    g = opt.g
+    # lattice centred on the vent axis: x = (i + 1/2) dx
+    nxh = int(math.ceil(half_width / dx)) + ghost_layers
+    xs = (np.arange(-nxh, nxh) + 0.5) * dx
+    nz = int(math.ceil(height / dx)) + ghost_layers
+    zs = (np.arange(-ghost_layers, nz) + 0.5) * dx
+    X, Yc, Z = np.meshgrid(xs, xs, zs, indexing="ij")
+    X = X.ravel(); Yc = Yc.ravel(); Z = Z.ravel()
+    inside = (np.abs(X) < half_width) & (np.abs(Yc) < half_width) & (Z > 0) & (Z < height)
+    pad = ghost_layers * dx
+    near = (np.abs(X) < half_width + pad) & (np.abs(Yc) < half_width + pad) & \
+           (Z < height + pad) & (Z > -pad)
+    rv = vent_radius
+    vdx = vent_dx if vent_dx is not None else min(dx, rv / 2.0)
+    duct = duct_depth if duct_depth is not None else 1.5 * 8.0 * dx
+    in_duct_col = (X ** 2 + Yc ** 2) <= (rv + 0.5 * dx) ** 2
+    press = near & ~inside & (Z > 0)
+    wall = near & (Z < 0) & ~(in_duct_col & (Z > -duct))
+    parts = []
+
+    def lattice_set(mask, bc, jit):
+        n = int(mask.sum())
+        ps = ParticleSet(n)
+        x, y, z = X[mask].copy(), Yc[mask].copy(), Z[mask].copy()
+        if jit:
+            x += rng.uniform(-jitter, jitter, n) * dx
+            y += rng.uniform(-jitter, jitter, n) * dx
+            z += rng.uniform(-jitter, jitter, n) * dx
+        ps.x[:], ps.y[:], ps.z[:] = x, y, z
+        zz = np.abs(z) if bc == BC_WALL else z
+        T, p, rho = atmosphere(zz, T0=T0, lapse=lapse, p0=p0, R=opt.ra, g=g)
+        ps.rho[:] = rho
+        ps.e[:] = opt.cva * T
+        ps.mass[:] = rho * dx ** 3
+        ps.h[:] = dx
+        ps.Y[:] = 0.0
+        ps.phase[:] = 1
+        ps.bc_type[:] = bc
+        ps.involved[:] = 0
+        return ps
+
+    parts.append(lattice_set(inside, BC_REAL, jitter > 0))
+    parts.append(lattice_set(press, BC_PRESSURE, jitter > 0))
+    parts.append(lattice_set(wall, BC_WALL, jitter > 0))
+    # eruption duct (setup_erupt.cc:44-387): lattice of spacing vdx centred on
+    # the vent axis, from z = -vdx/2 down to -duct
+    nv = int(math.ceil(rv / vdx))
+    vx = (np.arange(-nv, nv) + 0.5) * vdx
+    vz = -(np.arange(int(duct // vdx)) + 0.5) * vdx
+    VX, VY, VZ = np.meshgrid(vx, vx, vz, indexing="ij")
+    VX = VX.ravel(); VY = VY.ravel(); VZ = VZ.ravel()
+    m = (VX ** 2 + VY ** 2) <= rv * rv
+    ne = int(m.sum())
+    ev = ParticleSet(ne)
+    ev.x[:], ev.y[:], ev.z[:] = VX[m], VY[m], VZ[m]
+    ng0 = 1.0 - ash
+    Tv = vent_T
+    pv = p0
+    rhov = pv / (opt.rg * Tv) / ng0          # rhov_P = pv0/(Rg Tv0)/ng0
+    ev.rho[:] = rhov
+    ev.e[:] = (ng0 * opt.cvg + (1 - ng0) * opt.cvs) * Tv   # ev0_P
+    ev.vz[:] = vent_velocity
+    ev.mass[:] = rhov * vdx ** 3
+    ev.h[:] = vdx
+    ev.Y[:] = 1.0
+    ev.phase[:] = 2
+    ev.bc_type[:] = BC_ERUPT
+    ev.involved[:] = 0
+    parts.append(ev)
+    ps = ParticleSet.concat(parts)
+    ps.key[:] = np.arange(ps.n, dtype=np.uint64)
+    opt.ng0 = ng0
+    _eos(opt, ps)
+    opt.capacity = int(ps.n * 1.25) + 1024
+    info = {"dx": dx, "vent_dx": vdx, "duct_depth": duct, "n_air": int(inside.sum()),
+            "n_vent": ne, "rhov": rhov, "half_width": half_width, "height": height}
+    return Case(name, opt, grid, ps, info=info)
+
+
+def plume_small(seed=0, precision=PREC_FP64, subcells=4) -> Case:
+    """A 800 m cube of the 3D plume at 50 m spacing (test size)."""
+    return plume_3d(half_width=400.0, height=800.0, dx=50.0, vent_radius=50.0,
+                    vent_velocity=150.0, vent_dx=25.0, duct_depth=300.0, seed=seed,
+                    precision=precision, subcells=subcells, name="plume_small")
+
+
+def plume_config2(seed=0, precision=PREC_FP64, subcells=4) -> Case:
+    """The full 3D plume workload: 20 x 20 x 20 km at 150 m (134^3 air)."""
+    return plume_3d(seed=seed, precision=precision, subcells=subcells, name="plume_3d_config2")

@@ -1,0 +1,70 @@
+"""Shared helpers of the test suite."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from plume_gpu import cases
+from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, ParticleSet
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MASK = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def mix64(k):
+    z = (np.asarray(k, dtype=np.uint64) + np.uint64(0x9E3779B97F4A7C15)) & MASK
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & MASK
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & MASK
+    return z ^ (z >> np.uint64(31))
+
+
+def set_summary(ki, kj):
+    """per-i count and xor-hash of the j set, for i in sorted unique order"""
+    order = np.lexsort((kj, ki))
+    ki, kj = ki[order], kj[order]
+    keys, start = np.unique(ki, return_index=True)
+    cnt = np.diff(np.append(start, len(ki)))
+    with np.errstate(over="ignore"):
+        h = np.bitwise_xor.reduceat(mix64(kj), start) if len(ki) else np.zeros(0, np.uint64)
+    return keys, cnt, h
+
+
+def unpack(d, prefix) -> ParticleSet:
+    ps = ParticleSet(0)
+    ps.key = np.array(d[prefix + "key"], dtype=np.uint64)
+    for f in DOUBLE_FIELDS + BYTE_FIELDS:
+        setattr(ps, f, np.array(d[prefix + f]))
+    return ps
+
+
+def golden_case(name):
+    """(case with the fixture's input particles, fixture dict)"""
+    d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    if name == "sod_1d_200":
+        c = cases.sod_1d(n_real=200)
+    elif name == "shock_tube_1d":
+        c = cases.shock_tube_1d()
+    elif name == "plume_3d_small":
+        c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                           vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")
+    else:
+        raise KeyError(name)
+    c.particles = unpack(d, "in_")
+    c.step0 = int(d["step0"])
+    c.pre_adaptive = bool(int(d["pre_adaptive"]))
+    return c, d
+
+
+def field_errors(a: ParticleSet, b: ParticleSet, fields=DOUBLE_FIELDS):
+    """max |a-b| / max|b| per field, after matching by key"""
+    a = a.sorted_by_key()
+    b = b.sorted_by_key()
+    assert a.n == b.n, (a.n, b.n)
+    assert np.array_equal(a.key, b.key)
+    out = {}
+    for f in fields:
+        x, y = getattr(a, f), getattr(b, f)
+        scale = max(float(np.abs(y).max()) if y.size else 0.0, 1e-300)
+        out[f] = float(np.abs(x - y).max() / scale) if y.size else 0.0
+    return out

@@ -1,0 +1,109 @@
+"""Generate the golden vectors that pin the CPU oracle.
+
+Runs the reference solver's own hot-path sources (compiled by
+`make -C oracle ref` from the Plume-SPH tree, driven by oracle/ref/driver.cc)
+on three small workloads and stores inputs, per-step dt, the final particle
+state and a summary of the reference's neighbour lists:
+
+  sod_1d_200.npz       1D Sod, 200 equal-mass reals, cubic-spline kernel
+                       (kernel-swap build), h = 1.3 m/rho, CFL 0.3, 20 steps
+  shock_tube_1d.npz    the reference's shipped 1D deck (Gaussian kernel,
+                       SHOCK_TUBE_TESTS 1, h0 = 0.003, 397 particles), 20 steps
+  plume_3d_small.npz   3D plume, 600 m cube at 50 m spacing with pressure,
+                       wall and erupt ghosts, LANS + energy smoothing, steps
+                       49..51 (step 50 runs adaptive_sml)
+
+Usage (in a container that has the reference tree):
+  python tests/golden/make_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "plume-sph_gb300"))
+
+from plume_gpu import cases  # noqa: E402
+from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS  # noqa: E402
+from oracle import refio  # noqa: E402
+
+MASK = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def mix64(k):
+    """splitmix64 finaliser (order-independent list hashing)."""
+    z = (np.asarray(k, dtype=np.uint64) + np.uint64(0x9E3779B97F4A7C15)) & MASK
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & MASK
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & MASK
+    return z ^ (z >> np.uint64(31))
+
+
+def list_summary(keys_i, lists_by_i):
+    """count and order-independent hash of each particle's neighbour set"""
+    cnt = np.zeros(len(keys_i), dtype=np.int64)
+    hsh = np.zeros(len(keys_i), dtype=np.uint64)
+    for r, k in enumerate(keys_i):
+        lj = lists_by_i[int(k)]
+        cnt[r] = len(lj)
+        with np.errstate(over="ignore"):
+            hsh[r] = np.bitwise_xor.reduce(mix64(lj)) if len(lj) else np.uint64(0)
+    return cnt, hsh
+
+
+def pack(prefix, ps):
+    out = {f"{prefix}key": ps.key}
+    for f in DOUBLE_FIELDS + BYTE_FIELDS:
+        out[f"{prefix}{f}"] = getattr(ps, f)
+    return out
+
+
+def make(case, variant, nsteps, path, sample_lists=64):
+    steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden")
+    o = case.options
+    d = {
+        "dim": o.dim, "nsteps": nsteps, "pre_adaptive": int(case.pre_adaptive),
+        "step0": case.step0, "dt": np.array([s["dt"] for s in steps]),
+        "time": np.array([s["time"] for s in steps]),
+        "step": np.array([s["step"] for s in steps]),
+    }
+    d.update(pack("in_", case.particles))
+    d.update(pack("out_", steps[-1]["particles"].sorted_by_key()))
+    ki = np.array(sorted(lists.keys()), dtype=np.uint64)
+    cnt, hsh = list_summary(ki, lists)
+    d.update({"list_key": ki, "list_count": cnt, "list_hash": hsh})
+    rng = np.random.default_rng(7)
+    pick = rng.choice(len(ki), size=min(sample_lists, len(ki)), replace=False)
+    flat, offs = [], [0]
+    for r in sorted(pick):
+        flat.append(np.asarray(lists[int(ki[r])], dtype=np.uint64))
+        offs.append(offs[-1] + len(flat[-1]))
+    d.update({"sample_key": ki[sorted(pick)], "sample_offs": np.array(offs, dtype=np.int64),
+              "sample_flat": np.concatenate(flat) if flat else np.zeros(0, np.uint64)})
+    if o.dim == 3:
+        # the lists of the last step were built from the state before it
+        d.update(pack("pre_", steps[-2]["particles"].sorted_by_key()))
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    refio.build_ref(a.ref)
+    make(cases.sod_1d(n_real=200), "ref1d_sod", 20, os.path.join(HERE, "sod_1d_200.npz"))
+    make(cases.shock_tube_1d(), "ref1d_gauss", 20, os.path.join(HERE, "shock_tube_1d.npz"))
+    c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                       vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")
+    c.step0 = 48
+    make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_small.npz"))
+
+
+if __name__ == "__main__":
+    main()
