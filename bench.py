@@ -1,0 +1,382 @@
+"""Benchmark of the Plume-SPH particle step on GB300.
+
+Workload: the 3D dusty-gas plume (20 x 20 x 20 km, 150 m lattice = 134^3
+air particles, hydrostatic 288 K atmosphere, 100 m vent at 150 m/s / 1053 K
+with ash mass fraction 0.95, outflow ghosts, +-1% jitter, seed 0), synthetic
+inputs built by plume_gpu.cases.plume_config2.  A step is one pass of the
+hot loop (dt, neighbour search, adaptive h every 50 steps, momentum/energy,
+density, LANS filter, position update).  The metric is particle-steps/s:
+need_neigh particles x steps / seconds.
+
+  value     mixed-precision path, particles resident in HBM, CUDA events
+            on the library stream over exactly K steps
+  e2e       the same steps through the C ABI with host buffers: every step
+            uploads the particle table from pinned host memory, steps, and
+            downloads it (the drop-in use by a host that keeps its own
+            particle table)
+  fp64      the FP64 path on the same workload (for the FP64 / mixed ratio)
+  roofline  the momentum/energy sweep (dominant kernel)
+  cpu_baseline  the CPU oracle (restatement of the reference path) on a
+            bounded sample of the same workload, all host threads
+
+`--impl reference` times the reference's CPU path (the oracle port: the
+reference's own build is x86-only and does not travel) on the host cores.
+Multi-GPU: replicas only (independent copies per rank).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "plume-sph_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s"
+WORKLOAD = "plume3d_20km_150m_134cube"
+
+# algorithmic bytes per particle of the momentum/energy sweep kernel:
+# i-side and j-side fields read once from HBM (neighbour reuse on chip),
+# outputs written once.  Fields read: x,y,z, vx,vy,vz, vsx,vsy,vsz, h, mass,
+# rho, p, c, T, cp, e, hlist (18 x 8 B) + xr,yr,zr (3 x 4 B, mixed) + bc,
+# bkt (1 + 4 B); written: new v (3 x 8 B) + new e (8 B).
+MOM_BYTES_READ = 18 * 8 + 3 * 4 + 1 + 4
+MOM_BYTES_WRITE = 4 * 8
+# algorithmic FLOPs of one in-support pair of the momentum sweep (3D with
+# LANS and heat terms): 80 FLOP + 2 SFU
+MOM_FLOP_PER_PAIR = 80
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        return dist, dist.get_rank(), ws
+    return None, 0, 1
+
+
+def reduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def pinned_particles(ps):
+    """copy of a ParticleSet whose arrays live in pinned host memory"""
+    import torch
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, ParticleSet
+    out = ParticleSet(0)
+    keep = []
+
+    def pin(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)) if a.dtype != np.uint64
+                        else torch.int64, pin_memory=True)
+        v = t.numpy().view(a.dtype)
+        v[...] = a
+        keep.append(t)
+        return v
+    out.key = pin(ps.key)
+    for f in DOUBLE_FIELDS + BYTE_FIELDS:
+        setattr(out, f, pin(getattr(ps, f)))
+    out._pinned = keep
+    return out
+
+
+def cpu_sample(case, budget_s: float = 12.0, nthreads: int = 0):
+    """oracle on a bounded sample: the first `ntarget` air particles get the
+    full per-step work (list build + sweeps)"""
+    from oracle.binding import sample_step_seconds
+    nt = 4000
+    t = sample_step_seconds(case, nt, nthreads)
+    if t <= 0:
+        raise RuntimeError("oracle sample failed")
+    per = t / nt
+    nt2 = int(min(max(budget_s / per, nt), case.particles.need_neigh().sum()))
+    t2 = sample_step_seconds(case, nt2, nthreads)
+    return nt2, t2
+
+
+def run_reference(args, dist, rank, ws):
+    """--impl reference: the reference CPU path (oracle port) on host cores"""
+    if rank != 0:
+        return 0
+    from plume_gpu import cases
+    case = cases.plume_config2(seed=0)
+    ncores = os.cpu_count() or 1
+    vals = []
+    nt = None
+    for k in range(args.warmup + args.steps):
+        if nt is None:
+            nt, t = cpu_sample(case, budget_s=max(2.0, 60.0 / (args.warmup + args.steps)))
+        else:
+            from oracle.binding import sample_step_seconds
+            t = sample_step_seconds(case, nt, 0)
+        if k >= args.warmup:
+            vals.append(nt / t)
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * case.particles.need_neigh().sum() / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "n_air": int(case.particles.need_neigh().sum()),
+                                         "inputs": "host memory"},
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": ncores, "kind": "port",
+                         "sample": f"{nt} air particles per step (neighbour lists + all sweeps), "
+                                   f"remaining per-particle work for all {case.particles.n} particles"},
+        "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true", help="test-size workload")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist, rank, ws = dist_init()
+    if args.impl == "reference":
+        rc = run_reference(args, dist, rank, ws)
+        if dist is not None:
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+    import plume_gpu
+    from plume_gpu import PREC_FP64, PREC_MIXED, Solver, cases
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    plume_gpu.build()
+
+    def make(prec):
+        if args.small:
+            return cases.plume_3d(half_width=2000.0, height=4000.0, dx=50.0, vent_radius=50.0,
+                                  vent_dx=25.0, duct_depth=600.0, seed=0, precision=prec,
+                                  name="plume_small_bench")
+        return cases.plume_config2(seed=0, precision=prec)
+
+    case = make(PREC_MIXED)
+    n_air0 = int(case.particles.need_neigh().sum())
+    sol = Solver(case)
+    # warm-up (not timed)
+    sol.steps(args.warmup)
+    barrier(dist)
+    torch.cuda.synchronize()
+    _, n_real_before = sol.count()
+    with ClockSampler(local) as clk:
+        log = sol.steps(args.steps, log=False)
+        phases = sol.phase_times()
+    torch.cuda.synchronize()
+    launches = sol.launches()
+    _, n_real_after = sol.count()
+    t_dev = phases["total"] / 1000.0
+    t_max = reduce_max(dist, t_dev)
+    # particle-steps: need_neigh particles of each step (count at the start
+    # and end of the timed region; the inlet changes it by < 0.1 %)
+    n_real = 0.5 * (n_real_before + n_real_after)
+    value = ws * n_real * args.steps / t_max
+    ms_per_step = 1000.0 * t_max / args.steps
+
+    # dominant kernel: momentum sweep
+    peak_hbm, peak_kind = load_peaks()
+    nt, _ = sol.count()
+    mom_ms = phases["momentum"] / args.steps
+    alg_bytes = nt * MOM_BYTES_READ + n_real * MOM_BYTES_WRITE
+    achieved_gbs = alg_bytes / (mom_ms / 1000.0) / 1e9
+    npairs = None
+    try:
+        # in-support pairs of the momentum sweep (count only)
+        import ctypes as C
+        n = C.c_size_t()
+        rc = sol.L.plume_neighbor_pairs(sol.ctx, 1, None, None, 0, C.byref(n))
+        npairs = int(n.value) if rc == 0 else None
+    except Exception:
+        npairs = None
+    fp32_tflops = (npairs * MOM_FLOP_PER_PAIR / (mom_ms / 1000.0) / 1e12) if npairs else None
+    sm_max = 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FFMA lanes x 2 FLOP x clock
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "momentum_traffic.json")
+    if os.path.exists(tfile):
+        tj = json.load(open(tfile))
+        # DRAM bytes per particle of a captured small case, scaled by particles
+        traffic = tj.get("dram_bytes_per_particle", 0) * nt if tj.get("dram_bytes_per_particle") else None
+
+    # e2e: through the C ABI with pinned host buffers, every step
+    # upload -> step -> download
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    host = pinned_particles(sol.download())
+    host.key = host.key  # pinned copy of the whole particle table
+    bytes_per = 8 + 8 * len(DOUBLE_FIELDS) + len(BYTE_FIELDS)
+    e2e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nrs, h2d, d2h = 0, 0, 0
+    n_host = host.n
+    for _ in range(e2e_steps):
+        view = host.take(slice(0, n_host)) if n_host != host.n else host
+        sol.upload(view)
+        h2d += n_host * bytes_per
+        sol.steps(1)
+        n_host = sol.download_into(host)
+        d2h += n_host * bytes_per
+        nrs += int(host.need_neigh()[:n_host].sum())
+    torch.cuda.synchronize()
+    t_e2e = reduce_max(dist, time.perf_counter() - t0)
+    e2e_value = ws * nrs / t_e2e
+    h2d //= e2e_steps
+    d2h //= e2e_steps
+    sol.close()
+
+    # FP64 path on the same workload (shorter)
+    fp64 = None
+    if not args.no_fp64:
+        c64 = make(PREC_FP64)
+        s64 = Solver(c64)
+        s64.steps(3)
+        k64 = max(2, min(args.steps, 3))
+        _, nr0 = s64.count()
+        s64.steps(k64)
+        ph64 = s64.phase_times()
+        _, nr1 = s64.count()
+        t64 = reduce_max(dist, ph64["total"] / 1000.0)
+        fp64 = {"value": ws * 0.5 * (nr0 + nr1) * k64 / t64, "unit": METRIC, "steps": k64,
+                "ms_per_step": 1000.0 * t64 / k64,
+                "momentum_ms": ph64["momentum"] / k64}
+        s64.close()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            ncpu = os.cpu_count() or 1
+            ntg, tc = cpu_sample(make(PREC_FP64), budget_s=12.0)
+            cpu = {"value": ntg / tc, "unit": METRIC, "cores": ncpu, "kind": "port",
+                   "sample": f"one step for {ntg} of {n_air0} air particles (lists + sweeps), "
+                             f"all particles for the per-particle work"}
+        except Exception as e:  # the oracle is optional on the box
+            cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-mixed", "data": "synthetic",
+            "config": {"workload": WORKLOAD if not args.small else "plume3d_small",
+                       "n_air": n_air0, "n_particles": int(case.particles.n),
+                       "precision": "fp32 pair arithmetic, fp64 positions and updates",
+                       "parallelism": f"replicas{ws}", "l2": "working set > L2 (state ~0.6 GB)"},
+            "gpu_launches": launches,
+            "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "fp64": fp64,
+            "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_hbm,
+                         "unit": "GB/s", "frac": achieved_gbs / peak_hbm, "traffic": traffic,
+                         "kernel": "k_momentum<3,float>", "peak_kind": peak_kind,
+                         "pipe": {"bound": "fp32", "achieved_tflops": fp32_tflops,
+                                  "peak_tflops": fp32_peak,
+                                  "frac": (fp32_tflops / fp32_peak) if fp32_tflops else None,
+                                  "pairs_per_launch": npairs,
+                                  "flop_per_pair": MOM_FLOP_PER_PAIR}},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -209,6 +209,11 @@ int plume_step(plume_ctx *ctx, double *dt_out);
  * or point to nsteps entries. */
 int plume_steps(plume_ctx *ctx, int nsteps, PlumeStepLog *log);
 
+/* One adaptive_sml pass at the current state, with neighbour candidates
+ * taken at the current positions (the 1D solver calls adaptive_sml once
+ * before its time loop, src/plume/main.cc:643-649). */
+int plume_adapt_sml(plume_ctx *ctx);
+
 /* Particle count (total and need_neigh). */
 int plume_count(plume_ctx *ctx, size_t *n_total, size_t *n_real);
 /* Copy all particles to host arrays of capacity cap; *n receives the count. */
@@ -230,9 +235,12 @@ int plume_set_time(plume_ctx *ctx, double time, int step, int ioutput,
 int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
                          uint64_t *key_j, size_t cap, size_t *n);
 
-/* Per-phase device time of the last plume_step/plume_steps call, in ms:
- * [0] sort+cells, [1] adaptive h, [2] momentum/energy, [3] density,
- * [4] velocity filter, [5] position/rebucket, [6] dt reduction, [7] total. */
+/* Per-phase device time of the last plume_step/plume_steps call, summed over
+ * its steps, in ms (CUDA events on the context's stream):
+ * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket
+ * max h, [3] momentum/energy sweep, [4] its commit + EOS, [5] density sweep,
+ * [6] its commit + EOS, [7] velocity filter, [8] position update and
+ * re-bucketing, [9] dt reduction, [10] total.  n <= 11 entries. */
 int plume_phase_times(plume_ctx *ctx, float *ms, int n);
 
 /* Device kernel launches issued by the last plume_step/plume_steps call. */

@@ -13,7 +13,8 @@
 //   update_pos, update_particles_in_bucket (3D), TimeProps::ifoutput.
 //
 // Case file (little endian):
-//   char[8] "PLSPHIN1"; int32 dim, nsteps, n, pre_adaptive, step0;
+//   char[8] "PLSPHIN1"; int32 dim, nsteps, n, pre_adaptive, step0, dump_last;
+//   (nsteps < 0: run until TimeProps::ifend(); dump_last: dump only the last step)
 //   double max_time, timeoutput, stat_erupt, end_erupt, sml_phase2;
 //   3D only: double mindom[3], del; int32 nb[3]; uint8 flags[nbk];
 //            int8 face_index[6*nbk]; double lo[3], hi[3];
@@ -48,7 +49,7 @@
 static const int NF = 19;
 
 struct Case {
-  int dim, nsteps, n, pre_adaptive, step0;
+  int dim, nsteps, n, pre_adaptive, step0, dump_last;
   double max_time, timeoutput, stat_erupt, end_erupt, sml_phase2;
   double mindom[3], del;
   int nb[3];
@@ -73,9 +74,10 @@ static void read_case(const char *path, Case &c) {
   char magic[8];
   rd(fp, magic, 1, 8);
   if (memcmp(magic, "PLSPHIN1", 8)) { fprintf(stderr, "bad magic\n"); exit(2); }
-  int32_t hdr[5];
-  rd(fp, hdr, 4, 5);
+  int32_t hdr[6];
+  rd(fp, hdr, 4, 6);
   c.dim = hdr[0]; c.nsteps = hdr[1]; c.n = hdr[2]; c.pre_adaptive = hdr[3]; c.step0 = hdr[4];
+  c.dump_last = hdr[5];
   double t[5];
   rd(fp, t, 8, 5);
   c.max_time = t[0]; c.timeoutput = t[1]; c.stat_erupt = t[2]; c.end_erupt = t[3];
@@ -374,14 +376,16 @@ int main(int argc, char **argv) {
   FILE *fo = fopen(argv[2], "wb");
   if (!fo) { perror(argv[2]); return 2; }
   fwrite("PLSPHOU1", 1, 8, fo);
-  int32_t hdr[2] = { c.dim, c.nsteps };
+  // the step count is patched in after the run when nsteps < 0 or dump_last
+  int32_t hdr[2] = { c.dim, 0 };
   fwrite(hdr, 4, 2, fo);
 
 #if CODE_DIMENSION == 1
   if (c.pre_adaptive) adaptive_sml(0, P);  // main.cc:643-649
 #endif
   int lost = 0;
-  for (int st = 0; st < c.nsteps; st++) {
+  int ndumped = 0;
+  for (int st = 0; c.nsteps < 0 ? !tp->ifend() : st < c.nsteps; st++) {
 #if CODE_DIMENSION == 1
     double dt = timestep(P, tp);
     tp->incrtime(&dt);
@@ -403,9 +407,16 @@ int main(int argc, char **argv) {
     update_particles_in_bucket(0, P, BG, &lost);
 #endif
     tp->ifoutput();
-    dump_state(fo, P, c, *tp, dt);
+    bool last = (c.nsteps < 0) ? tp->ifend() : (st == c.nsteps - 1);
+    if (!c.dump_last || last) {
+      dump_state(fo, P, c, *tp, dt);
+      ndumped++;
+    }
   }
   dump_lists(fo, P, c);
+  fseek(fo, 12, SEEK_SET);
+  int32_t nd = ndumped;
+  fwrite(&nd, 4, 1, fo);
   fclose(fo);
   (void)lost;
   (void)BG;

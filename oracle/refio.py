@@ -18,11 +18,12 @@ def build_ref(ref_root: str = "/root/reference"):
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
 
 
-def write_case(path, case, nsteps):
+def write_case(path, case, nsteps, dump_last=False):
     o, g, ps = case.options, case.grid, case.particles
     with open(path, "wb") as fp:
         fp.write(b"PLSPHIN1")
-        fp.write(struct.pack("<5i", o.dim, nsteps, ps.n, int(case.pre_adaptive), int(case.step0)))
+        fp.write(struct.pack("<6i", o.dim, nsteps, ps.n, int(case.pre_adaptive), int(case.step0),
+                             int(dump_last)))
         fp.write(struct.pack("<5d", o.max_time, o.timeoutput, o.stat_erupt, o.end_erupt,
                              o.sml_phase2))
         if o.dim == 3:
@@ -76,11 +77,11 @@ def read_result(path):
     return steps, lists
 
 
-def run_ref(variant, case, nsteps, workdir):
+def run_ref(variant, case, nsteps, workdir, dump_last=False):
     os.makedirs(workdir, exist_ok=True)
     cin = os.path.join(workdir, f"{case.name}.case")
     cout = os.path.join(workdir, f"{case.name}.out")
-    write_case(cin, case, nsteps)
+    write_case(cin, case, nsteps, dump_last)
     exe = os.path.join(HERE, "_ref", variant, "driver")
     subprocess.run([exe, cin, cout], check=True)
     return read_result(cout)

@@ -1,0 +1,1022 @@
+// plume_gpu.cu -- context, step orchestration and the C ABI of
+// include/plume_gpu.h.
+//
+// One step (src/plume/main.cc:217-471 in 3D, :676-750 in 1D):
+//   k_dt_reduce + k_incrtime      timestep (timestep.cc:94-183) and
+//                                 TimeProps::incrtime (properties.h:71-83)
+//   search                        cell keys, radix sort, gather, cell_start
+//                                 (replaces search_neighs_consth and the
+//                                 bucket lists of update_particles_in_bucket)
+//   k_adaptive                    adaptive_sml every sml_interval steps
+//   k_momentum + k_commit_mom     mom_engr_update
+//   k_density + k_commit_dens     smooth_density
+//   k_velocity                    smooth_velocity (LANS)
+//   k_update_pos                  update_pos + deletions of the re-bucketing
+//   k_end_step                    TimeProps::ifoutput (properties.h:100-118)
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/plume_gpu.h"
+#include "radix_sort.cuh"
+#include "sph_kernels.cuh"
+
+using namespace plume;
+
+namespace {
+
+constexpr int NTHREADS = 128;
+// phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax, 3 momentum,
+// 4 commit_mom, 5 density, 6 commit_dens, 7 velocity, 8 position, 9 dt,
+// 10 total
+constexpr int NPHASE = 11;
+constexpr int NEV = 11;
+
+inline int nblocks(size_t n, int t = NTHREADS) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+// ---- dt: min over need_neigh of h/c (timestep.cc:94-135) -----------------
+__global__ void k_dt_reduce(Dev A, const int* __restrict__ d_count, TimeState* ts) {
+  __shared__ double red[NTHREADS];
+  __shared__ unsigned int nr[NTHREADS];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 1.0e10;
+  unsigned int real = 0;
+  if (i < *d_count && need_neigh(A.bc[i])) {
+    double c = A.c[i];
+    if (!(c > 0)) set_status(ts, 4);
+    double t = A.h[i] / c;
+    if (t < v) v = t;
+    real = 1;
+  }
+  red[threadIdx.x] = v;
+  nr[threadIdx.x] = real;
+  __syncthreads();
+  for (int s = NTHREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x] = fmin(red[threadIdx.x], red[threadIdx.x + s]);
+      nr[threadIdx.x] += nr[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    if (m > 0 && m == m) atomicMin(&ts->dtmin_bits, dbits(m));
+    if (nr[0]) atomicAdd(&ts->n_real, (unsigned long long)nr[0]);
+  }
+}
+
+// TimeProps::incrtime and iferupt
+__global__ void k_incrtime(Opt o, TimeState* ts) {
+  double dt = o.cfl * __longlong_as_double((long long)ts->dtmin_bits);
+  if ((ts->time + dt) > ts->ndtimeoutput) dt = ts->ndtimeoutput - ts->time;
+  if ((ts->time + dt) > o.max_time) dt = o.max_time - ts->time;
+  ts->time += dt;
+  ts->dtime = dt;
+  ts->step++;
+  ts->erupt = !((ts->time * 1.0) < o.stat_erupt) && !((ts->time * 1.0) > o.end_erupt);
+}
+
+// TimeProps::ifoutput; resets the per-step reductions
+__global__ void k_end_step(Opt o, TimeState* ts) {
+  if (ts->time >= ts->ndtimeoutput || ts->time == o.max_time) {
+    ts->ioutput++;
+    ts->ndtimeoutput = ((ts->ioutput + 1) * o.timeoutput) / 1.0;
+  }
+}
+__global__ void k_begin_step(TimeState* ts) {
+  ts->dtmin_bits = dbits(1.0e10);
+  ts->n_real = 0;
+}
+
+// ---- search --------------------------------------------------------------
+__global__ void k_keys(Geo g, Dev A, int n, uint32_t* __restrict__ keys, uint32_t ncells, TimeState* ts) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (A.bc[i] == BC_DEAD) {
+    keys[i] = ncells;
+    return;
+  }
+  bool o1 = false, o2 = false, o3 = false;
+  int b0, b1 = 0, b2 = 0;
+  int c0 = cell_axis(g, 0, A.x[i], &b0, &o1);
+  int c1 = 0, c2 = 0;
+  if (g.dim == 3) {
+    c1 = cell_axis(g, 1, A.y[i], &b1, &o2);
+    c2 = cell_axis(g, 2, A.z[i], &b2, &o3);
+  }
+  if (o1 || o2 || o3) {
+    set_status(ts, 6);
+    keys[i] = ncells;
+    A.bc[i] = BC_DEAD;
+    return;
+  }
+  keys[i] = (uint32_t)(((size_t)c2 * g.G[1] + c1) * g.G[0] + c0);
+  A.bkt[i] = (g.dim == 3) ? (b2 * g.nb[1] + b1) * g.nb[0] + b0 : b0;
+}
+
+__global__ void k_gather(Geo g, Dev A, Dev B, Work W, const uint32_t* __restrict__ perm, int n, int mixed) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int q = perm[p];
+  B.key[p] = A.key[q];
+  B.x[p] = A.x[q];
+  B.vx[p] = A.vx[q];
+  B.vsx[p] = A.vsx[q];
+  if (g.dim == 3) {
+    B.y[p] = A.y[q]; B.z[p] = A.z[q];
+    B.vy[p] = A.vy[q]; B.vz[p] = A.vz[q];
+    B.vsy[p] = A.vsy[q]; B.vsz[p] = A.vsz[q];
+  }
+  B.mass[p] = A.mass[q];
+  double h = A.h[q];
+  B.h[p] = h;
+  W.hlist[p] = h;
+  B.rho[p] = A.rho[q];
+  B.e[p] = A.e[q];
+  B.p[p] = A.p[q];
+  B.Y[p] = A.Y[q];
+  B.gam[p] = A.gam[q];
+  B.c[p] = A.c[q];
+  B.T[p] = A.T[q];
+  B.cp[p] = A.cp[q];
+  B.phase[p] = A.phase[q];
+  B.bc[p] = A.bc[q];
+  B.inv[p] = A.inv[q];
+  int b = A.bkt[q];
+  B.bkt[p] = b;
+  if (mixed) {
+    int bi[3];
+    if (g.dim == 3) {
+      bi[0] = b % g.nb[0];
+      bi[1] = (b / g.nb[0]) % g.nb[1];
+      bi[2] = b / (g.nb[0] * g.nb[1]);
+      W.xr[p] = (float)(A.x[q] - (g.mind[0] + bi[0] * g.del));
+      W.yr[p] = (float)(A.y[q] - (g.mind[1] + bi[1] * g.del));
+      W.zr[p] = (float)(A.z[q] - (g.mind[2] + bi[2] * g.del));
+    } else {
+      W.xr[p] = (float)(A.x[q] - (g.mind[0] + b * g.del));
+    }
+  }
+}
+
+// cell_start[c] = first sorted index with key >= c, c in [0, ncells + 1]
+__global__ void k_cell_start(const uint32_t* __restrict__ skeys, int n, uint32_t ncells,
+                             uint32_t* __restrict__ cs, int* d_count) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > n) return;
+  long long kp = (p < n) ? (long long)skeys[p] : (long long)ncells + 1;
+  long long kprev = (p == 0) ? -1 : (long long)skeys[p - 1];
+  if (kp > (long long)ncells + 1) kp = ncells + 1;
+  for (long long c = kprev + 1; c <= kp; c++) {
+    cs[c] = (uint32_t)p;
+    if (c == (long long)ncells) *d_count = p;
+  }
+}
+
+__global__ void k_fill_cs(uint32_t* cs, uint32_t ncells, int* d_count) {
+  size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c <= ncells + 1) cs[c] = 0;
+  if (c == 0) *d_count = 0;
+}
+
+// ---- per-bucket maximum h (search radius of the h_ij sweeps) ------------
+__global__ void k_hmax_reset(unsigned long long* hb, int nbk) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nbk) hb[b] = 0ull;
+}
+__global__ void k_hmax(Dev A, const int* __restrict__ d_count, unsigned long long* hb, int dim) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count) return;
+  if (A.bc[i] == BC_DEAD) return;
+  double h = A.h[i];
+  atomicMax(&hb[dim == 3 ? A.bkt[i] : 0], dbits(h));
+}
+__global__ void k_hmax27(Geo g, const unsigned long long* __restrict__ hb, double* __restrict__ h27) {
+  int nbk = g.nb[0] * g.nb[1] * g.nb[2];
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g.dim != 3) {
+    if (b == 0) h27[0] = __longlong_as_double((long long)hb[0]);
+    return;
+  }
+  if (b >= nbk) return;
+  int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
+  double m = 0;
+  for (int dz = -1; dz <= 1; dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        int x = bx + dx, y = by + dy, z = bz + dz;
+        if (x < 0 || y < 0 || z < 0 || x >= g.nb[0] || y >= g.nb[1] || z >= g.nb[2]) continue;
+        m = fmax(m, __longlong_as_double((long long)hb[(z * g.nb[1] + y) * g.nb[0] + x]));
+      }
+  h27[b] = m;
+}
+
+// ---- neighbour pairs (plume_neighbor_pairs) -------------------------------
+template <int D>
+__global__ void k_pairs(int mode, Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
+                        const int* __restrict__ d_count, const unsigned long long* __restrict__ offs,
+                        unsigned int* __restrict__ cnt, uint64_t* __restrict__ ki, uint64_t* __restrict__ kj) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = *d_count;
+  if (i >= n) return;
+  if (!need_neigh(A.bc[i])) {
+    if (!offs) cnt[i] = 0;
+    return;
+  }
+  double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
+  int bi[3];
+  bucket_coords<D>(g, A.bkt[i], bi);
+  const double hi = A.h[i];
+  const double Lb = o.list_factor * W.hlist[i];
+  unsigned long long base = offs ? offs[i] : 0ull;
+  unsigned int c = 0;
+  auto take = [&](uint32_t j) {
+    if (offs) {
+      ki[base + c] = A.key[i];
+      kj[base + c] = A.key[j];
+    }
+    c++;
+  };
+  if (mode == 0 && D == 1) {
+    for (int j = 0; j < n; j++)
+      if (A.bc[j] != BC_DEAD) take(j);
+  } else {
+    double R = (mode == 0) ? fmax(Lb, g.del) * (1.0 + 1e-10) : o.cutoff2 * hi * (1.0 + 1e-10);
+    for_segments<D, double>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+      for (uint32_t j = j0; j < j1; j++) {
+        double xj[3] = {A.x[j], D == 3 ? A.y[j] : 0.0, D == 3 ? A.z[j] : 0.0};
+        double dx[3];
+        for (int k = 0; k < D; k++) dx[k] = xi[k] - xj[k];
+        bool inlist = own || in_box<D, double>(dx, Lb);
+        if (!inlist) continue;
+        if (mode == 1) {
+          if (j == (uint32_t)i) continue;
+          if (!in_box<D, double>(dx, o.cutoff2 * hi)) continue;
+          double h = 0.5 * (hi + A.h[j]);
+          double si[3];
+          for (int k = 0; k < D; k++) si[k] = dx[k] / h;
+          if (kw<D, double>(o.kernel, si, h) == 0.0) continue;
+        }
+        take(j);
+      }
+    });
+  }
+  if (!offs) cnt[i] = c;
+}
+
+// exclusive scan of uint32 counts into uint64 offsets (three kernels)
+__global__ void k_scan_blocks(const unsigned int* __restrict__ cnt, int n, unsigned long long* __restrict__ out,
+                              unsigned long long* __restrict__ sums) {
+  __shared__ unsigned long long s[1024];
+  int t = threadIdx.x;
+  int i = blockIdx.x * 1024 + t;
+  s[t] = (i < n) ? cnt[i] : 0ull;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    unsigned long long v = (t >= off) ? s[t - off] : 0ull;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  if (i < n) out[i] = s[t] - cnt[i];
+  if (t == 1023) sums[blockIdx.x] = s[t];
+}
+__global__ void k_scan_sums(unsigned long long* sums, int m, unsigned long long* total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    unsigned long long run = 0;
+    for (int b = 0; b < m; b++) {
+      unsigned long long v = sums[b];
+      sums[b] = run;
+      run += v;
+    }
+    *total = run;
+  }
+}
+__global__ void k_scan_add(unsigned long long* out, int n, const unsigned long long* __restrict__ sums) {
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// ---- ghost state (plume_set_ghost_state) -----------------------------------
+__global__ void k_set_ghost(Opt o, Dev A, const int* __restrict__ d_count, const uint64_t* __restrict__ keys,
+                            const double* __restrict__ state, const double* __restrict__ Yin, int m, int dim) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count) return;
+  uint64_t k = A.key[i];
+  int lo = 0, hi = m;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (keys[mid] < k) lo = mid + 1; else hi = mid;
+  }
+  if (lo >= m || keys[lo] != k) return;
+  const int w = dim + 2;
+  const double* s = state + (size_t)lo * w;
+  A.rho[i] = s[0];
+  A.vx[i] = s[1];
+  if (dim == 3) { A.vy[i] = s[2]; A.vz[i] = s[3]; }
+  A.e[i] = s[w - 1];
+  if (Yin) A.Y[i] = Yin[lo];
+  double gam, p, c, T, cp = A.cp[i];
+  eos(o, A.rho[i], A.Y[i], A.e[i], gam, p, c, T, cp, o.lans != 0);
+  A.gam[i] = gam; A.p[i] = p; A.c[i] = c; A.T[i] = T; A.cp[i] = cp;
+}
+
+}  // namespace
+
+// ============================================================================
+// context
+// ============================================================================
+static thread_local std::string g_create_error;
+
+struct plume_ctx {
+  PlumeOptions opt{};
+  Opt o{};
+  Geo g{};
+  cudaStream_t st = nullptr;
+  size_t cap = 0;
+  size_t n_alloc = 0;  // rows in use (upper bound of live particles)
+  Dev A{}, B{};
+  Work W{};
+  uint32_t *keys = nullptr, *perm = nullptr, *cs = nullptr;
+  uint32_t ncells = 0;
+  int keybits = 1;
+  int* d_count = nullptr;
+  TimeState* ts = nullptr;
+  TimeState* h_ts = nullptr;  // pinned mirror
+  unsigned long long* hb = nullptr;
+  double* h27 = nullptr;
+  int nbk = 1;
+  uint8_t* bflags = nullptr;
+  int8_t* bface = nullptr;
+  RadixSorter sorter;
+  std::vector<void*> allocs;
+  int host_step = 0;
+  bool pending_dead = false;
+  std::string err;
+  // per-step event sets (NEV events each) for the phase times of a call
+  std::vector<cudaEvent_t> evs;
+  cudaEvent_t* ev = nullptr;  // event set of the step being issued
+  float phase_ms[NPHASE] = {};
+  unsigned long long launches = 0;
+};
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess) {                                                          \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+      return PLUME_E_CUDA;                                                            \
+    }                                                                                 \
+  } while (0)
+
+static int dev_alloc(plume_ctx* ctx, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return PLUME_E_CUDA;
+  }
+  ctx->allocs.push_back(*p);
+  return PLUME_OK;
+}
+#define DALLOC(ptr, bytes)                                                   \
+  do {                                                                       \
+    int rc_ = dev_alloc(ctx, (void**)&(ptr), (bytes));                       \
+    if (rc_) return rc_;                                                     \
+  } while (0)
+
+static int alloc_dev(plume_ctx* ctx, Dev& D, size_t cap) {
+  DALLOC(D.key, 8 * cap);
+  double** f[] = {&D.x, &D.y, &D.z, &D.vx, &D.vy, &D.vz, &D.vsx, &D.vsy, &D.vsz, &D.mass,
+                  &D.h, &D.rho, &D.e, &D.p, &D.Y, &D.gam, &D.c, &D.T, &D.cp};
+  for (auto p : f) DALLOC(*p, 8 * cap);
+  DALLOC(D.phase, cap);
+  DALLOC(D.bc, cap);
+  DALLOC(D.inv, cap);
+  DALLOC(D.bkt, 4 * cap);
+  return PLUME_OK;
+}
+
+static Opt make_opt(const PlumeOptions& p) {
+  Opt o;
+  o.dim = p.dim; o.prec = p.precision; o.kernel = p.kernel; o.lans = p.lans; o.esmooth = p.energy_smooth;
+  o.pgc = p.pghost_contrib; o.adaptive = p.adaptive_sml; o.interval = p.sml_interval > 0 ? p.sml_interval : 1;
+  o.num_loop = p.num_loop; o.thresh = p.thresh; o.c_smooth = p.c_smooth; o.eta = p.eta_smooth;
+  o.alpha = p.alpha; o.beta = p.beta; o.ata = p.ata; o.cfl = p.cfl; o.cutoff2 = p.cutoff2;
+  o.list_factor = p.list_factor; o.g = p.g; o.ng0 = p.ng0; o.cvs = p.cvs; o.cvg = p.cvg; o.cva = p.cva;
+  o.rg = p.rg; o.ra = p.ra; o.vent_z = p.vent_z; o.sml2 = p.sml_phase2; o.max_time = p.max_time;
+  o.timeoutput = p.timeoutput; o.stat_erupt = p.stat_erupt; o.end_erupt = p.end_erupt;
+  o.ksupport = (p.kernel == PLUME_KERNEL_M4) ? 2.0 : 3.0;
+  return o;
+}
+
+static int ctx_sync_status(plume_ctx* ctx) {
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
+  int s = ctx->h_ts->status;
+  if (s) {
+    ctx->err = std::string("device status ") + std::to_string(s);
+    TimeState clr = *ctx->h_ts;
+    clr.status = 0;
+    CK(cudaMemcpy(ctx->ts, &clr, sizeof(TimeState), cudaMemcpyHostToDevice));
+  }
+  return s;
+}
+
+// search: keys, radix sort, gather into B, swap, cell_start
+static int search(plume_ctx* ctx) {
+  const int n = (int)ctx->n_alloc;
+  cudaStream_t st = ctx->st;
+  if (n == 0) {
+    k_fill_cs<<<nblocks((size_t)ctx->ncells + 2, 256), 256, 0, st>>>(ctx->cs, ctx->ncells, ctx->d_count);
+    ctx->launches++;
+    return PLUME_OK;
+  }
+  k_keys<<<nblocks(n), NTHREADS, 0, st>>>(ctx->g, ctx->A, n, ctx->keys, ctx->ncells, ctx->ts);
+  ctx->launches++;
+  ctx->launches += ctx->sorter.sort(ctx->keys, ctx->perm, n, ctx->keybits, st);
+  k_gather<<<nblocks(n), NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->B, ctx->W, ctx->perm, n,
+                                            ctx->opt.precision == PLUME_PREC_MIXED);
+  std::swap(ctx->A, ctx->B);
+  k_cell_start<<<nblocks((size_t)n + 1), NTHREADS, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
+  ctx->launches += 2;
+  ctx->pending_dead = false;
+  CK(cudaGetLastError());
+  return PLUME_OK;
+}
+
+template <int D, typename T>
+static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
+  cudaStream_t st = ctx->st;
+  const int n = (int)ctx->n_alloc;
+  const int nb = nblocks(n);
+  if (adaptive_now) {
+    k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    ctx->launches++;
+  }
+  cudaEventRecord(ctx->ev[3], st);
+  k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
+  k_hmax<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->hb, D);
+  k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->g, ctx->hb, ctx->h27);
+  cudaEventRecord(ctx->ev[4], st);
+  k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  cudaEventRecord(ctx->ev[5], st);
+  k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
+  ctx->launches += 5;
+  cudaEventRecord(ctx->ev[6], st);
+  k_density<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  cudaEventRecord(ctx->ev[7], st);
+  k_commit_dens<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
+  ctx->launches += 2;
+  cudaEventRecord(ctx->ev[8], st);
+  if (ctx->o.lans) {
+    k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    ctx->launches++;
+  }
+  cudaEventRecord(ctx->ev[9], st);
+}
+
+// one step, no host synchronisation
+static int step_async(plume_ctx* ctx) {
+  cudaStream_t st = ctx->st;
+  const int n = (int)ctx->n_alloc;
+  cudaEventRecord(ctx->ev[0], st);
+  k_begin_step<<<1, 1, 0, st>>>(ctx->ts);
+  k_dt_reduce<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->ts);
+  k_incrtime<<<1, 1, 0, st>>>(ctx->o, ctx->ts);
+  ctx->launches += 3;
+  cudaEventRecord(ctx->ev[1], st);
+  int rc = search(ctx);
+  if (rc) return rc;
+  cudaEventRecord(ctx->ev[2], st);
+  ctx->host_step++;
+  bool adaptive_now = ctx->o.adaptive && (ctx->host_step % ctx->o.interval) == 0;
+  const bool mixed = ctx->opt.precision == PLUME_PREC_MIXED;
+  if (ctx->o.dim == 3) {
+    if (mixed) launch_sweeps<3, float>(ctx, adaptive_now); else launch_sweeps<3, double>(ctx, adaptive_now);
+    k_update_pos<3><<<nblocks(n), NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
+  } else {
+    if (mixed) launch_sweeps<1, float>(ctx, adaptive_now); else launch_sweeps<1, double>(ctx, adaptive_now);
+    k_update_pos<1><<<nblocks(n), NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
+  }
+  k_end_step<<<1, 1, 0, st>>>(ctx->o, ctx->ts);
+  ctx->launches += 2;
+  ctx->pending_dead = true;
+  cudaEventRecord(ctx->ev[10], st);
+  CK(cudaGetLastError());
+  return PLUME_OK;
+}
+
+// events of a step: 0 start, 1 after dt, 2 after search, 3 after adaptive,
+// 4 after hmax, 5 after momentum, 6 after commit, 7 after density, 8 after
+// commit, 9 after velocity, 10 end
+static void accumulate_phases(plume_ctx* ctx, const cudaEvent_t* e) {
+  float t[NPHASE];
+  cudaEventElapsedTime(&t[9], e[0], e[1]);
+  cudaEventElapsedTime(&t[0], e[1], e[2]);
+  cudaEventElapsedTime(&t[1], e[2], e[3]);
+  cudaEventElapsedTime(&t[2], e[3], e[4]);
+  cudaEventElapsedTime(&t[3], e[4], e[5]);
+  cudaEventElapsedTime(&t[4], e[5], e[6]);
+  cudaEventElapsedTime(&t[5], e[6], e[7]);
+  cudaEventElapsedTime(&t[6], e[7], e[8]);
+  cudaEventElapsedTime(&t[7], e[8], e[9]);
+  cudaEventElapsedTime(&t[8], e[9], e[10]);
+  cudaEventElapsedTime(&t[10], e[0], e[10]);
+  for (int k = 0; k < NPHASE; k++) ctx->phase_ms[k] += t[k];
+}
+
+static int ensure_events(plume_ctx* ctx, int nsteps) {
+  size_t need = (size_t)NEV * (size_t)(nsteps > 0 ? nsteps : 1);
+  while (ctx->evs.size() < need) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    ctx->evs.push_back(e);
+  }
+  return PLUME_OK;
+}
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char* plume_version(void) { return "0.1.0"; }
+
+int plume_last_error(plume_ctx* ctx, char* buf, size_t len) {
+  if (!buf || !len) return PLUME_E_INVALID;
+  const std::string& s = ctx ? ctx->err : g_create_error;
+  snprintf(buf, len, "%s", s.c_str());
+  return PLUME_OK;
+}
+
+int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out) {
+  if (!opt || !grid || !out) {
+    g_create_error = "null argument";
+    return PLUME_E_INVALID;
+  }
+  if (opt->dim != 1 && opt->dim != 3) {
+    g_create_error = "dim must be 1 or 3";
+    return PLUME_E_INVALID;
+  }
+  if (opt->capacity == 0 || opt->capacity > (size_t)0x7fffffff) {
+    g_create_error = "capacity must be in [1, 2^31)";
+    return PLUME_E_INVALID;
+  }
+  if (grid->del <= 0 || grid->nb[0] < 1 || grid->nb[1] < 1 || grid->nb[2] < 1 ||
+      (opt->dim == 1 && (grid->nb[1] != 1 || grid->nb[2] != 1))) {
+    g_create_error = "invalid bucket grid";
+    return PLUME_E_INVALID;
+  }
+  int s = grid->subcells > 0 ? grid->subcells : 1;
+  double ncell_d = (double)grid->nb[0] * s * (opt->dim == 3 ? (double)grid->nb[1] * s * grid->nb[2] * s : 1.0);
+  if (ncell_d > 2.0e9) {
+    g_create_error = "too many fine cells";
+    return PLUME_E_INVALID;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    g_create_error = "no CUDA device";
+    return PLUME_E_CUDA;
+  }
+  plume_ctx* ctx = new plume_ctx();
+  ctx->opt = *opt;
+  ctx->o = make_opt(*opt);
+  Geo& g = ctx->g;
+  for (int a = 0; a < 3; a++) {
+    g.mind[a] = grid->mindom[a];
+    g.nb[a] = grid->nb[a];
+    g.lo[a] = grid->domain_lo[a];
+    g.hi[a] = grid->domain_hi[a];
+  }
+  g.del = grid->del;
+  g.s = s;
+  g.cw = grid->del / s;
+  g.dim = opt->dim;
+  for (int a = 0; a < 3; a++) g.G[a] = (opt->dim == 3 || a == 0) ? g.nb[a] * s : 1;
+  ctx->ncells = (uint32_t)((size_t)g.G[0] * g.G[1] * g.G[2]);
+  ctx->keybits = 1;
+  while ((1ull << ctx->keybits) <= (unsigned long long)ctx->ncells) ctx->keybits++;
+  ctx->nbk = (opt->dim == 3) ? g.nb[0] * g.nb[1] * g.nb[2] : 1;
+  ctx->cap = opt->capacity;
+  int rc = PLUME_OK;
+  auto fail = [&](int code) {
+    g_create_error = ctx->err;
+    plume_destroy(ctx);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+    ctx->err = "cudaStreamCreate failed";
+    return fail(PLUME_E_CUDA);
+  }
+  if ((rc = ensure_events(ctx, 1))) return fail(rc);
+  ctx->ev = ctx->evs.data();
+  if ((rc = alloc_dev(ctx, ctx->A, ctx->cap)) || (rc = alloc_dev(ctx, ctx->B, ctx->cap))) return fail(rc);
+  {
+    size_t c = ctx->cap;
+    double** w[] = {&ctx->W.hlist, &ctx->W.nv0, &ctx->W.nv1, &ctx->W.nv2, &ctx->W.ne, &ctx->W.nrho,
+                    &ctx->W.nY, &ctx->W.nE};
+    for (auto p : w)
+      if ((rc = dev_alloc(ctx, (void**)p, 8 * c))) return fail(rc);
+    if ((rc = dev_alloc(ctx, (void**)&ctx->W.xr, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->W.yr, 4 * c)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->W.zr, 4 * c)))
+      return fail(rc);
+    if ((rc = dev_alloc(ctx, (void**)&ctx->keys, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->perm, 4 * c)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->cs, 4 * ((size_t)ctx->ncells + 2))) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->d_count, sizeof(int))) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->ts, sizeof(TimeState))) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->hb, 8 * (size_t)ctx->nbk)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->h27, 8 * (size_t)ctx->nbk)))
+      return fail(rc);
+    if (ctx->sorter.reserve((int)c) != cudaSuccess) {
+      ctx->err = "radix sort buffers";
+      return fail(PLUME_E_CUDA);
+    }
+  }
+  if (opt->dim == 3 && grid->flags) {
+    if ((rc = dev_alloc(ctx, (void**)&ctx->bflags, ctx->nbk))) return fail(rc);
+    cudaMemcpy(ctx->bflags, grid->flags, ctx->nbk, cudaMemcpyHostToDevice);
+  }
+  if (opt->dim == 3 && grid->face_index) {
+    if ((rc = dev_alloc(ctx, (void**)&ctx->bface, 6 * (size_t)ctx->nbk))) return fail(rc);
+    cudaMemcpy(ctx->bface, grid->face_index, 6 * (size_t)ctx->nbk, cudaMemcpyHostToDevice);
+  }
+  if (cudaMallocHost(&ctx->h_ts, sizeof(TimeState)) != cudaSuccess) {
+    ctx->err = "cudaMallocHost";
+    return fail(PLUME_E_CUDA);
+  }
+  TimeState t{};
+  t.time = 0;
+  t.ndtimeoutput = opt->timeoutput;
+  t.dtmin_bits = 0;
+  *ctx->h_ts = t;
+  if (cudaMemcpy(ctx->ts, &t, sizeof(TimeState), cudaMemcpyHostToDevice) != cudaSuccess) {
+    ctx->err = "init time state";
+    return fail(PLUME_E_CUDA);
+  }
+  int zero = 0;
+  cudaMemcpy(ctx->d_count, &zero, sizeof(int), cudaMemcpyHostToDevice);
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    ctx->err = "device init";
+    return fail(PLUME_E_CUDA);
+  }
+  *out = ctx;
+  return PLUME_OK;
+}
+
+int plume_destroy(plume_ctx* ctx) {
+  if (!ctx) return PLUME_OK;
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  for (void* p : ctx->allocs) cudaFree(p);
+  ctx->sorter.release();
+  if (ctx->h_ts) cudaFreeHost(ctx->h_ts);
+  for (auto& e : ctx->evs)
+    if (e) cudaEventDestroy(e);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+  return PLUME_OK;
+}
+
+static int check_soa(plume_ctx* ctx, const PlumeSoA* s) {
+  if (!s || !s->key || !s->x || !s->vx || !s->mass || !s->h || !s->rho || !s->e || !s->p || !s->Y ||
+      !s->gamma || !s->c || !s->T || !s->cp || !s->phase || !s->bc_type || !s->involved) {
+    ctx->err = "missing particle array";
+    return PLUME_E_INVALID;
+  }
+  if (ctx->o.dim == 3 && (!s->y || !s->z || !s->vy || !s->vz)) {
+    ctx->err = "3D particles need y, z, vy, vz";
+    return PLUME_E_INVALID;
+  }
+  return PLUME_OK;
+}
+
+static int copy_soa(plume_ctx* ctx, const PlumeSoA* s, size_t off, size_t n, cudaMemcpyKind kind) {
+  int rc = check_soa(ctx, s);
+  if (rc) return rc;
+  const bool d3 = ctx->o.dim == 3;
+  cudaStream_t st = ctx->st;
+  Dev& A = ctx->A;
+  CK(cudaMemcpyAsync(A.key + off, s->key, 8 * n, kind, st));
+  struct F { double* d; const double* h; } f[] = {
+      {A.x, s->x}, {A.vx, s->vx}, {A.mass, s->mass}, {A.h, s->h}, {A.rho, s->rho}, {A.e, s->e},
+      {A.p, s->p}, {A.Y, s->Y}, {A.gam, s->gamma}, {A.c, s->c}, {A.T, s->T}, {A.cp, s->cp}};
+  for (auto& q : f) CK(cudaMemcpyAsync(q.d + off, q.h, 8 * n, kind, st));
+  if (d3) {
+    CK(cudaMemcpyAsync(A.y + off, s->y, 8 * n, kind, st));
+    CK(cudaMemcpyAsync(A.z + off, s->z, 8 * n, kind, st));
+    CK(cudaMemcpyAsync(A.vy + off, s->vy, 8 * n, kind, st));
+    CK(cudaMemcpyAsync(A.vz + off, s->vz, 8 * n, kind, st));
+  }
+  // smoothed velocity: optional on upload (zero when absent)
+  double* vs[3] = {A.vsx, A.vsy, A.vsz};
+  const double* hv[3] = {s->vsx, s->vsy, s->vsz};
+  for (int a = 0; a < (d3 ? 3 : 1); a++) {
+    if (hv[a])
+      CK(cudaMemcpyAsync(vs[a] + off, hv[a], 8 * n, kind, st));
+    else
+      CK(cudaMemsetAsync(vs[a] + off, 0, 8 * n, st));
+  }
+  CK(cudaMemcpyAsync(A.phase + off, s->phase, n, kind, st));
+  CK(cudaMemcpyAsync(A.bc + off, s->bc_type, n, kind, st));
+  CK(cudaMemcpyAsync(A.inv + off, s->involved, n, kind, st));
+  return PLUME_OK;
+}
+
+static int set_count(plume_ctx* ctx, size_t n) {
+  ctx->n_alloc = n;
+  int v = (int)n;
+  CK(cudaMemcpyAsync(ctx->d_count, &v, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return PLUME_OK;
+}
+
+int plume_upload(plume_ctx* ctx, const PlumeSoA* host, size_t n) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (n > ctx->cap) {
+    ctx->err = "particle count exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  int rc = copy_soa(ctx, host, 0, n, cudaMemcpyHostToDevice);
+  if (rc) return rc;
+  rc = set_count(ctx, n);
+  if (rc) return rc;
+  ctx->pending_dead = true;  // order unknown: search before any pair query
+  return PLUME_OK;
+}
+
+int plume_upload_device(plume_ctx* ctx, const PlumeSoA* dev, size_t n) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (n > ctx->cap) {
+    ctx->err = "particle count exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  int rc = copy_soa(ctx, dev, 0, n, cudaMemcpyDeviceToDevice);
+  if (rc) return rc;
+  rc = set_count(ctx, n);
+  if (rc) return rc;
+  ctx->pending_dead = true;
+  return PLUME_OK;
+}
+
+int plume_append(plume_ctx* ctx, const PlumeSoA* host, size_t n) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (ctx->n_alloc + n > ctx->cap) {
+    ctx->err = "append exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  int rc = copy_soa(ctx, host, ctx->n_alloc, n, cudaMemcpyHostToDevice);
+  if (rc) return rc;
+  rc = set_count(ctx, ctx->n_alloc + n);
+  ctx->pending_dead = true;
+  return rc;
+}
+
+int plume_set_ghost_state(plume_ctx* ctx, const uint64_t* keys, const double* state, const double* Y, size_t n) {
+  if (!ctx || (n && (!keys || !state))) return PLUME_E_INVALID;
+  if (n == 0) return PLUME_OK;
+  const int w = ctx->o.dim + 2;
+  std::vector<size_t> ord(n);
+  for (size_t i = 0; i < n; i++) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return keys[a] < keys[b]; });
+  std::vector<uint64_t> k(n);
+  std::vector<double> s(n * w), y(Y ? n : 0);
+  for (size_t r = 0; r < n; r++) {
+    k[r] = keys[ord[r]];
+    for (int c = 0; c < w; c++) s[r * w + c] = state[ord[r] * w + c];
+    if (Y) y[r] = Y[ord[r]];
+  }
+  uint64_t* dk = nullptr;
+  double *ds = nullptr, *dy = nullptr;
+  CK(cudaMalloc(&dk, 8 * n));
+  CK(cudaMalloc(&ds, 8 * n * w));
+  if (Y) CK(cudaMalloc(&dy, 8 * n));
+  CK(cudaMemcpy(dk, k.data(), 8 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ds, s.data(), 8 * n * w, cudaMemcpyHostToDevice));
+  if (Y) CK(cudaMemcpy(dy, y.data(), 8 * n, cudaMemcpyHostToDevice));
+  k_set_ghost<<<nblocks(ctx->n_alloc ? ctx->n_alloc : 1), NTHREADS, 0, ctx->st>>>(
+      ctx->o, ctx->A, ctx->d_count, dk, ds, dy, (int)n, ctx->o.dim);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->st));
+  cudaFree(dk);
+  cudaFree(ds);
+  if (dy) cudaFree(dy);
+  return PLUME_OK;
+}
+
+static int finish_steps(plume_ctx* ctx) {
+  int s = ctx_sync_status(ctx);
+  int n = 0;
+  CK(cudaMemcpy(&n, ctx->d_count, sizeof(int), cudaMemcpyDeviceToHost));
+  ctx->n_alloc = (size_t)n;
+  return s;
+}
+
+int plume_steps(plume_ctx* ctx, int nsteps, PlumeStepLog* log) {
+  if (!ctx || nsteps < 0) return PLUME_E_INVALID;
+  for (auto& v : ctx->phase_ms) v = 0;
+  ctx->launches = 0;
+  int rc0 = ensure_events(ctx, nsteps);
+  if (rc0) return rc0;
+  for (int k = 0; k < nsteps; k++) {
+    ctx->ev = ctx->evs.data() + (size_t)NEV * k;
+    int rc = step_async(ctx);
+    if (rc) return rc;
+    if (log) {
+      int s = finish_steps(ctx);
+      accumulate_phases(ctx, ctx->ev);
+      // the particle count shrinks only at the next search
+      PlumeStepLog& L = log[k];
+      L.dt = ctx->h_ts->dtime;
+      L.time = ctx->h_ts->time;
+      L.step = ctx->h_ts->step;
+      L.status = s;
+      L.n_total = ctx->n_alloc;
+      L.n_real = ctx->h_ts->n_real;
+      L.n_lost = ctx->h_ts->n_lost;
+      if (s) return s;
+    }
+  }
+  int s = finish_steps(ctx);
+  if (!log)
+    for (int k = 0; k < nsteps; k++) accumulate_phases(ctx, ctx->evs.data() + (size_t)NEV * k);
+  return s;
+}
+
+int plume_step(plume_ctx* ctx, double* dt_out) {
+  int rc = plume_steps(ctx, 1, nullptr);
+  if (dt_out && ctx) *dt_out = ctx->h_ts->dtime;
+  return rc;
+}
+
+int plume_adapt_sml(plume_ctx* ctx) {
+  if (!ctx) return PLUME_E_INVALID;
+  int rc = search(ctx);
+  if (rc) return rc;
+  const int nb = nblocks(ctx->n_alloc ? ctx->n_alloc : 1);
+  const bool mixed = ctx->opt.precision == PLUME_PREC_MIXED;
+  if (ctx->o.dim == 3) {
+    if (mixed) k_adaptive<3, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    else k_adaptive<3, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+  } else {
+    if (mixed) k_adaptive<1, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    else k_adaptive<1, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+  }
+  CK(cudaGetLastError());
+  return ctx_sync_status(ctx);
+}
+
+int plume_count(plume_ctx* ctx, size_t* n_total, size_t* n_real) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (ctx->pending_dead) {
+    int rc = search(ctx);
+    if (rc) return rc;
+    int s = ctx_sync_status(ctx);
+    if (s) return s;
+    int n = 0;
+    CK(cudaMemcpy(&n, ctx->d_count, sizeof(int), cudaMemcpyDeviceToHost));
+    ctx->n_alloc = (size_t)n;
+  }
+  if (n_total) *n_total = ctx->n_alloc;
+  if (n_real) {
+    std::vector<uint8_t> bc(ctx->n_alloc);
+    CK(cudaMemcpy(bc.data(), ctx->A.bc, ctx->n_alloc, cudaMemcpyDeviceToHost));
+    size_t r = 0;
+    for (uint8_t b : bc) r += (b == 100 || b == 99);
+    *n_real = r;
+  }
+  return PLUME_OK;
+}
+
+int plume_download(plume_ctx* ctx, PlumeSoA* host, size_t cap, size_t* n) {
+  if (!ctx || !host || !n) return PLUME_E_INVALID;
+  size_t nt = 0;
+  int rc = plume_count(ctx, &nt, nullptr);
+  if (rc) return rc;
+  *n = nt;
+  if (nt > cap) {
+    ctx->err = "download capacity too small";
+    return PLUME_E_CAPACITY;
+  }
+  rc = check_soa(ctx, host);
+  if (rc) return rc;
+  Dev& A = ctx->A;
+  cudaStream_t st = ctx->st;
+  auto d2h = [&](void* h, const void* d, size_t bytes) -> cudaError_t {
+    return h ? cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+  };
+  CK(d2h(host->key, A.key, 8 * nt));
+  const double* src[] = {A.x, A.y, A.z, A.vx, A.vy, A.vz, A.vsx, A.vsy, A.vsz, A.mass, A.h, A.rho, A.e,
+                         A.p, A.Y, A.gam, A.c, A.T, A.cp};
+  double* dst[] = {host->x, host->y, host->z, host->vx, host->vy, host->vz, host->vsx, host->vsy,
+                   host->vsz, host->mass, host->h, host->rho, host->e, host->p, host->Y, host->gamma,
+                   host->c, host->T, host->cp};
+  const bool d3 = ctx->o.dim == 3;
+  for (int f = 0; f < 19; f++) {
+    bool axis = (f == 1 || f == 2 || f == 4 || f == 5 || f == 7 || f == 8);
+    if (axis && !d3) {
+      if (dst[f]) memset(dst[f], 0, 8 * nt);
+      continue;
+    }
+    CK(d2h(dst[f], src[f], 8 * nt));
+  }
+  CK(d2h(host->phase, A.phase, nt));
+  CK(d2h(host->bc_type, A.bc, nt));
+  CK(d2h(host->involved, A.inv, nt));
+  CK(cudaStreamSynchronize(st));
+  return PLUME_OK;
+}
+
+int plume_get_time(plume_ctx* ctx, double* time, int* step, int* ioutput) {
+  if (!ctx) return PLUME_E_INVALID;
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
+  if (time) *time = ctx->h_ts->time;
+  if (step) *step = ctx->h_ts->step;
+  if (ioutput) *ioutput = ctx->h_ts->ioutput;
+  return PLUME_OK;
+}
+
+int plume_set_time(plume_ctx* ctx, double time, int step, int ioutput, double next_output) {
+  if (!ctx) return PLUME_E_INVALID;
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
+  ctx->h_ts->time = time;
+  ctx->h_ts->step = step;
+  ctx->h_ts->ioutput = ioutput;
+  ctx->h_ts->ndtimeoutput = next_output;
+  CK(cudaMemcpy(ctx->ts, ctx->h_ts, sizeof(TimeState), cudaMemcpyHostToDevice));
+  ctx->host_step = step;
+  return PLUME_OK;
+}
+
+int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* key_j, size_t cap, size_t* n) {
+  if (!ctx || !n || (mode != 0 && mode != 1)) return PLUME_E_INVALID;
+  int rc = search(ctx);
+  if (rc) return rc;
+  int s = ctx_sync_status(ctx);
+  if (s) return s;
+  int cnt_h = 0;
+  CK(cudaMemcpy(&cnt_h, ctx->d_count, sizeof(int), cudaMemcpyDeviceToHost));
+  ctx->n_alloc = (size_t)cnt_h;
+  const int np = cnt_h;
+  unsigned int* cnt = nullptr;
+  unsigned long long *offs = nullptr, *sums = nullptr, *tot = nullptr;
+  int nbk = (np + 1023) / 1024;
+  CK(cudaMalloc(&cnt, 4 * (size_t)(np ? np : 1)));
+  CK(cudaMalloc(&offs, 8 * (size_t)(np ? np : 1)));
+  CK(cudaMalloc(&sums, 8 * (size_t)(nbk ? nbk : 1)));
+  CK(cudaMalloc(&tot, 8));
+  cudaStream_t st = ctx->st;
+  const int nb = nblocks(np ? np : 1);
+  if (ctx->o.dim == 3)
+    k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+  else
+    k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+  unsigned long long total = 0;
+  if (np) {
+    k_scan_blocks<<<nbk, 1024, 0, st>>>(cnt, np, offs, sums);
+    k_scan_sums<<<1, 1, 0, st>>>(sums, nbk, tot);
+    k_scan_add<<<nbk, 1024, 0, st>>>(offs, np, sums);
+    CK(cudaMemcpyAsync(&total, tot, 8, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  *n = (size_t)total;
+  if (total <= cap && key_i && key_j && total) {
+    uint64_t *dki = nullptr, *dkj = nullptr;
+    CK(cudaMalloc(&dki, 8 * total));
+    CK(cudaMalloc(&dkj, 8 * total));
+    if (ctx->o.dim == 3)
+      k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+    else
+      k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+    CK(cudaMemcpyAsync(key_i, dki, 8 * total, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(key_j, dkj, 8 * total, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    cudaFree(dki);
+    cudaFree(dkj);
+  }
+  cudaFree(cnt);
+  cudaFree(offs);
+  cudaFree(sums);
+  cudaFree(tot);
+  CK(cudaGetLastError());
+  return PLUME_OK;
+}
+
+int plume_phase_times(plume_ctx* ctx, float* ms, int n) {
+  if (!ctx || !ms) return PLUME_E_INVALID;
+  for (int k = 0; k < n && k < NPHASE; k++) ms[k] = ctx->phase_ms[k];
+  return PLUME_OK;
+}
+
+int plume_launch_count(plume_ctx* ctx, uint64_t* n) {
+  if (!ctx || !n) return PLUME_E_INVALID;
+  *n = ctx->launches;
+  return PLUME_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,158 @@
+"""Host-side mirror of the reference's per-step interface over the C ABI.
+
+`Solver` owns one plume_ctx (one CUDA stream on the current device).  Its
+methods follow the reference free functions the library replaces
+(src/plume/particler.h): `step()` is one pass of the hot loop of
+src/plume/main.cc:217-471 (3D) / :676-750 (1D); `adaptive_sml()` is the
+pre-loop call of the 1D solver (main.cc:643-649); errors are raised as
+`PlumeError` carrying the PLUME_E_* status, where the reference asserts.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .abi import (DOUBLE_FIELDS, STATUS_NAMES, ParticleSet, PlumeSoA, PlumeStepLog)
+
+
+class PlumeError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} {detail}".strip())
+
+
+class Solver:
+    def __init__(self, case):
+        self.case = case
+        self.L = _lib.lib()
+        self._opt = case.options.to_c()
+        if self._opt.capacity == 0:
+            self._opt.capacity = max(case.particles.n, 1)
+        self._grid = case.grid.to_c()
+        self.ctx = C.c_void_p()
+        rc = self.L.plume_create(C.byref(self._opt), C.byref(self._grid), C.byref(self.ctx))
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.L.plume_last_error(None, buf, 512)
+            raise PlumeError(rc, "plume_create", buf.value.decode())
+        if case.particles.n:
+            self.upload(case.particles)
+        if case.step0:
+            self.set_time(0.0, case.step0, 0, case.options.timeoutput)
+
+    # -- helpers ------------------------------------------------------------
+    def _check(self, rc, where):
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.L.plume_last_error(self.ctx, buf, 512)
+            raise PlumeError(rc, where, buf.value.decode())
+
+    def close(self):
+        if self.ctx:
+            self.L.plume_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- particles ----------------------------------------------------------
+    def upload(self, ps: ParticleSet):
+        s = ps.soa()
+        self._check(self.L.plume_upload(self.ctx, C.byref(s), ps.n), "plume_upload")
+
+    def upload_device(self, soa: PlumeSoA, n: int):
+        self._check(self.L.plume_upload_device(self.ctx, C.byref(soa), n), "plume_upload_device")
+
+    def append(self, ps: ParticleSet):
+        s = ps.soa()
+        self._check(self.L.plume_append(self.ctx, C.byref(s), ps.n), "plume_append")
+
+    def set_ghost_state(self, keys, state, Y=None):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        yp = None
+        if Y is not None:
+            Y = np.ascontiguousarray(Y, dtype=np.float64)
+            yp = Y.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self.L.plume_set_ghost_state(
+            self.ctx, keys.ctypes.data_as(C.POINTER(C.c_uint64)),
+            state.ctypes.data_as(C.POINTER(C.c_double)), yp, len(keys)), "plume_set_ghost_state")
+
+    def count(self):
+        nt, nr = C.c_size_t(), C.c_size_t()
+        self._check(self.L.plume_count(self.ctx, C.byref(nt), C.byref(nr)), "plume_count")
+        return nt.value, nr.value
+
+    def download_into(self, ps: ParticleSet) -> int:
+        """download into existing arrays (e.g. pinned host buffers); returns
+        the particle count"""
+        s = ps.soa()
+        n = C.c_size_t()
+        self._check(self.L.plume_download(self.ctx, C.byref(s), ps.n, C.byref(n)), "plume_download")
+        return n.value
+
+    def download(self) -> ParticleSet:
+        nt, _ = self.count()
+        ps = ParticleSet(nt)
+        s = ps.soa()
+        n = C.c_size_t()
+        self._check(self.L.plume_download(self.ctx, C.byref(s), nt, C.byref(n)), "plume_download")
+        if n.value != nt:
+            ps = ps.take(np.arange(n.value))
+        return ps
+
+    # -- time stepping ------------------------------------------------------
+    def adaptive_sml(self):
+        self._check(self.L.plume_adapt_sml(self.ctx), "plume_adapt_sml")
+
+    def step(self) -> float:
+        dt = C.c_double()
+        self._check(self.L.plume_step(self.ctx, C.byref(dt)), "plume_step")
+        return dt.value
+
+    def steps(self, n: int, log: bool = False):
+        if log:
+            arr = (PlumeStepLog * max(n, 1))()
+            self._check(self.L.plume_steps(self.ctx, n, arr), "plume_steps")
+            return [{"dt": a.dt, "time": a.time, "step": a.step, "n_total": a.n_total,
+                     "n_real": a.n_real, "n_lost": a.n_lost} for a in arr[:n]]
+        self._check(self.L.plume_steps(self.ctx, n, None), "plume_steps")
+        return None
+
+    def time(self):
+        t, s, o = C.c_double(), C.c_int(), C.c_int()
+        self._check(self.L.plume_get_time(self.ctx, C.byref(t), C.byref(s), C.byref(o)),
+                    "plume_get_time")
+        return t.value, s.value, o.value
+
+    def set_time(self, time: float, step: int, ioutput: int, next_output: float):
+        self._check(self.L.plume_set_time(self.ctx, time, step, ioutput, next_output),
+                    "plume_set_time")
+
+    def pairs(self, mode: int = 0):
+        n = C.c_size_t()
+        self._check(self.L.plume_neighbor_pairs(self.ctx, mode, None, None, 0, C.byref(n)),
+                    "plume_neighbor_pairs")
+        ki = np.zeros(n.value, dtype=np.uint64)
+        kj = np.zeros(n.value, dtype=np.uint64)
+        self._check(self.L.plume_neighbor_pairs(
+            self.ctx, mode, ki.ctypes.data_as(C.POINTER(C.c_uint64)),
+            kj.ctypes.data_as(C.POINTER(C.c_uint64)), n.value, C.byref(n)), "plume_neighbor_pairs")
+        return ki, kj
+
+    def phase_times(self):
+        ms = (C.c_float * 11)()
+        self._check(self.L.plume_phase_times(self.ctx, ms, 11), "plume_phase_times")
+        names = ["search", "adaptive", "hmax", "momentum", "commit_mom", "density", "commit_dens",
+                 "velocity", "position", "dt", "total"]
+        return dict(zip(names, list(ms)))
+
+    def launches(self) -> int:
+        n = C.c_uint64()
+        self._check(self.L.plume_launch_count(self.ctx, C.byref(n)), "plume_launch_count")
+        return int(n.value)

@@ -42,7 +42,9 @@ def golden_case(name):
     """(case with the fixture's input particles, fixture dict)"""
     d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
     if name == "sod_1d_200":
-        c = cases.sod_1d(n_real=200)
+        c = cases.sod_1d(n_real=200, kernel=cases.KERNEL_M4)
+    elif name == "sod_1d_2000_end":
+        c = cases.sod_1d(n_real=2000)
     elif name == "shock_tube_1d":
         c = cases.shock_tube_1d()
     elif name == "plume_3d_small":

@@ -7,6 +7,8 @@ state and a summary of the reference's neighbour lists:
 
   sod_1d_200.npz       1D Sod, 200 equal-mass reals, cubic-spline kernel
                        (kernel-swap build), h = 1.3 m/rho, CFL 0.3, 20 steps
+  sod_1d_2000_end.npz  the 1D Sod workload: 2,000 equal-mass reals, Gaussian
+                       kernel, run to t = 0.2 (final state only)
   shock_tube_1d.npz    the reference's shipped 1D deck (Gaussian kernel,
                        SHOCK_TUBE_TESTS 1, h0 = 0.003, 397 particles), 20 steps
   plume_3d_small.npz   3D plume, 600 m cube at 50 m spacing with pressure,
@@ -63,8 +65,10 @@ def pack(prefix, ps):
     return out
 
 
-def make(case, variant, nsteps, path, sample_lists=64):
-    steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden")
+def make(case, variant, nsteps, path, sample_lists=64, dump_last=False):
+    steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden", dump_last)
+    if dump_last:
+        nsteps = steps[-1]["step"] - case.step0
     o = case.options
     d = {
         "dim": o.dim, "nsteps": nsteps, "pre_adaptive": int(case.pre_adaptive),
@@ -97,7 +101,10 @@ def main():
     ap.add_argument("--ref", default="/root/reference")
     a = ap.parse_args()
     refio.build_ref(a.ref)
-    make(cases.sod_1d(n_real=200), "ref1d_sod", 20, os.path.join(HERE, "sod_1d_200.npz"))
+    make(cases.sod_1d(n_real=200, kernel=cases.KERNEL_M4), "ref1d_sod", 20,
+         os.path.join(HERE, "sod_1d_200.npz"))
+    make(cases.sod_1d(n_real=2000), "ref1d_sodg", -1, os.path.join(HERE, "sod_1d_2000_end.npz"),
+         sample_lists=4, dump_last=True)
     make(cases.shock_tube_1d(), "ref1d_gauss", 20, os.path.join(HERE, "shock_tube_1d.npz"))
     c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
                        vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")

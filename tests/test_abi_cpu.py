@@ -1,0 +1,110 @@
+"""Host-side checks that need no GPU: the C-ABI library builds and exports
+every entry point declared in include/plume_gpu.h, the ctypes structs match
+the header's layout, and the input reader and workload builders follow the
+reference's conventions."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import plume_gpu
+from plume_gpu import abi, cases, inputs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "plume_gpu.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*\*?\s*(plume_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    plume_gpu.build()
+    lib = C.CDLL(plume_gpu._lib.LIBPATH)
+    names = header_functions()
+    assert len(names) >= 18
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.plume_version and C.c_char_p(lib.plume_version.restype and None) is not None
+
+
+def test_ctypes_struct_layout_matches_header():
+    # compile a probe with the header and compare offsets/sizes
+    import subprocess
+    import tempfile
+    probe = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "plume_gpu.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(PlumeOptions), sizeof(PlumeGrid), sizeof(PlumeSoA), sizeof(PlumeStepLog));
+  printf("%zu %zu %zu\n", offsetof(PlumeOptions, capacity), offsetof(PlumeGrid, domain_hi), offsetof(PlumeSoA, involved));
+  return 0;
+}'''
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "p.c")
+        open(src, "w").write(probe)
+        exe = os.path.join(d, "p")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    sizes = [int(v) for v in out]
+    assert sizes[0] == C.sizeof(abi.PlumeOptions)
+    assert sizes[1] == C.sizeof(abi.PlumeGrid)
+    assert sizes[2] == C.sizeof(abi.PlumeSoA)
+    assert sizes[3] == C.sizeof(abi.PlumeStepLog)
+    assert sizes[4] == abi.PlumeOptions.capacity.offset
+    assert sizes[5] == abi.PlumeGrid.domain_hi.offset
+    assert sizes[6] == abi.PlumeSoA.involved.offset
+
+
+def test_read_data_uses_single_precision(tmp_path):
+    # the shipped Sod deck of the reference (values after the last ':')
+    sim = inputs.SimulationData(max_time=0.17, max_steps=100000000, timeoutput=0.1, stat_erupt=0.0,
+                                end_erupt=7200.0, format=1, p_constant=2587463, gamma=1.4,
+                                smoothing_length=0.003, idom=(-0.4, 0.4, 0, 0, 0, 0))
+    inputs.write_data(str(tmp_path), sim)
+    got = inputs.read_data(str(tmp_path))
+    assert got.smoothing_length == float(np.float32(0.003))
+    assert got.max_time == float(np.float32(0.17))
+    assert got.max_steps == 100000000
+    assert got.idom[0] == float(np.float32(-0.4))
+
+
+def test_sod_builder_counts_and_equal_mass():
+    c = cases.sod_1d(n_real=2000)
+    ps = c.particles
+    real = ps.need_neigh()
+    assert int(real.sum()) == 2000
+    assert int((ps.bc_type == 0).sum()) == 20
+    assert np.allclose(ps.mass[real], ps.mass[real][0], rtol=1e-12)
+    assert ps.x[real].min() > 0 and ps.x[real].max() < 1
+    assert c.options.eta_smooth == 1.3 and c.options.cfl == 0.3
+    assert abs(1 + c.options.ra / c.options.cva - 1.4) < 1e-15
+
+
+def test_plume_builder_geometry():
+    c = cases.plume_small()
+    g, ps = c.grid, c.particles
+    assert g.del_ == 8 * 50.0
+    # every particle inside the bucket grid
+    for a, f in enumerate("xyz"):
+        v = getattr(ps, f)
+        assert v.min() >= g.mindom[a] and v.max() < g.mindom[a] + g.nb[a] * g.del_
+    # vent particles are pressure balanced with the air at the ground
+    vent = ps.bc_type == abi.BC_ERUPT
+    air = ps.bc_type == abi.BC_REAL
+    assert vent.sum() > 0
+    assert np.allclose(ps.p[vent], 101325.0, rtol=1e-9)
+    assert np.all(ps.Y[vent] == 1.0) and np.all(ps.Y[air] == 0.0)
+    # bucket types: mixed buckets straddle the domain faces
+    assert (g.flags & abi.BUCKET_MIXED).any() and (g.flags & abi.BUCKET_ABSORBING).any()
+
+
+def test_config2_size():
+    c = cases.plume_config2()
+    air = int(c.particles.need_neigh().sum())
+    assert 2.3e6 < air < 2.5e6

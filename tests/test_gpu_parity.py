@@ -1,0 +1,172 @@
+"""GPU particle step against the CPU oracle (parity tests proper).
+
+Every test runs the CUDA library through the C ABI (plume_gpu.Solver) and
+compares with the oracle on the same inputs.  Tolerances:
+  * neighbour sets: bit-exact (same pairs, FP64 box tests on identical
+    positions);
+  * FP64 path fields: max |gpu - oracle| / max |oracle| per field <= 1e-10
+    (the GPU sums neighbours in cell order, the oracle in list order; CUDA's
+    exp may differ from libm's in the last bit);
+  * mixed path: relative L1 density error vs the FP64 path <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+from oracle.binding import OracleRun
+from plume_gpu import PREC_MIXED, Solver, cases
+from plume_gpu.abi import BYTE_FIELDS
+from _util import field_errors, golden_case, set_summary, unpack
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+
+def _gpu_run(case, nsteps):
+    s = Solver(case)
+    if case.pre_adaptive:
+        s.adaptive_sml()
+    log = s.steps(nsteps, log=True)
+    return s, log
+
+
+def _check_fields(gps, ops, tol):
+    err = field_errors(gps, ops)
+    assert max(err.values()) <= tol, err
+    g, o = gps.sorted_by_key(), ops.sorted_by_key()
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(g, f), getattr(o, f), err_msg=f)
+    return err
+
+
+@pytest.mark.parametrize("name", ["sod_1d_200", "shock_tube_1d"])
+def test_1d_fp64_matches_oracle(name):
+    case, d = golden_case(name)
+    nsteps = int(d["nsteps"])
+    s, log = _gpu_run(case, nsteps)
+    o = OracleRun(case)
+    if case.pre_adaptive:
+        o.adaptive()
+    dts = o.steps(nsteps)
+    np.testing.assert_allclose([r["dt"] for r in log], dts, rtol=1e-12, atol=0)
+    t, step, io = s.time()
+    assert step == o.t.step and io == o.t.ioutput
+    _check_fields(s.download(), o.ps, FP64_TOL)
+    # and against the reference's own golden output
+    _check_fields(s.download(), unpack(d, "out_"), FP64_TOL)
+
+
+def test_3d_plume_fp64_matches_oracle_and_reference():
+    case, d = golden_case("plume_3d_small")
+    nsteps = int(d["nsteps"])
+    s, log = _gpu_run(case, nsteps)
+    o = OracleRun(case)
+    dts = o.steps(nsteps)
+    np.testing.assert_allclose([r["dt"] for r in log], dts, rtol=1e-12, atol=0)
+    _check_fields(s.download(), o.ps, FP64_TOL)
+    _check_fields(s.download(), unpack(d, "out_"), FP64_TOL)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_3d_neighbour_sets_bit_exact(mode):
+    case, d = golden_case("plume_3d_small")
+    case.particles = unpack(d, "pre_")
+    s = Solver(case)
+    gi, gj = s.pairs(mode)
+    oi, oj = OracleRun(case).pairs(mode)
+    gk, gc, gh = set_summary(gi, gj)
+    ok, oc, oh = set_summary(oi, oj)
+    np.testing.assert_array_equal(gk, ok)
+    np.testing.assert_array_equal(gc, oc)
+    np.testing.assert_array_equal(gh, oh)
+    if mode == 0:
+        # the reference's own lists (restricted to particles that were
+        # need_neigh when they were built)
+        pre = case.particles
+        live = np.isin(d["list_key"], pre.key[pre.need_neigh()])
+        np.testing.assert_array_equal(gk, d["list_key"][live])
+        np.testing.assert_array_equal(gc, d["list_count"][live])
+        np.testing.assert_array_equal(gh, d["list_hash"][live])
+
+
+def test_1d_neighbour_sets_bit_exact():
+    case, d = golden_case("sod_1d_200")
+    s = Solver(case)
+    for mode in (0, 1):
+        gk, gc, gh = set_summary(*s.pairs(mode))
+        ok, oc, oh = set_summary(*OracleRun(case).pairs(mode))
+        np.testing.assert_array_equal(gk, ok)
+        np.testing.assert_array_equal(gc, oc)
+        np.testing.assert_array_equal(gh, oh)
+
+
+def test_3d_adaptive_step_and_deletions():
+    """steps 49..53 of the small plume: adaptive_sml at step 50, erupt
+    ghosts turning real at the vent plane, outflow deletions."""
+    case = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                          vent_dx=25.0, duct_depth=300.0, seed=5, name="plume_small_b")
+    case.step0 = 48
+    s, log = _gpu_run(case, 5)
+    o = OracleRun(case)
+    o.steps(5)
+    _check_fields(s.download(), o.ps, FP64_TOL)
+
+
+def test_3d_mixed_precision_density_error():
+    case = cases.plume_small(seed=1)
+    fp64 = Solver(case)
+    fp64.steps(4)
+    mc = cases.plume_small(seed=1, precision=PREC_MIXED)
+    mixed = Solver(mc)
+    mixed.steps(4)
+    a = fp64.download().sorted_by_key()
+    b = mixed.download().sorted_by_key()
+    assert np.array_equal(a.key, b.key)
+    real = a.need_neigh()
+    l1 = np.abs(b.rho[real] - a.rho[real]).sum() / np.abs(a.rho[real]).sum()
+    assert l1 <= 1e-4, l1
+
+
+def test_1d_mixed_precision_density_error():
+    case = cases.sod_1d(n_real=400)
+    fp64 = Solver(case)
+    fp64.adaptive_sml()
+    fp64.steps(200)
+    mc = cases.sod_1d(n_real=400, precision=PREC_MIXED)
+    mixed = Solver(mc)
+    mixed.adaptive_sml()
+    mixed.steps(200)
+    a = fp64.download().sorted_by_key()
+    b = mixed.download().sorted_by_key()
+    real = a.need_neigh()
+    l1 = np.abs(b.rho[real] - a.rho[real]).sum() / np.abs(a.rho[real]).sum()
+    assert l1 <= 1e-4, l1
+
+
+def test_sod_2000_full_run_matches_reference():
+    """The 1D Sod workload (2,000 equal-mass particles, Gaussian kernel) to
+    t = 0.2 (2,549 steps) against the reference build's final state."""
+    case, d = golden_case("sod_1d_2000_end")
+    s = Solver(case)
+    s.adaptive_sml()
+    s.steps(int(d["nsteps"]))
+    t, step, _ = s.time()
+    assert step == int(d["step"][-1])
+    assert abs(t - float(d["time"][-1])) <= 1e-12
+    err = _check_fields(s.download(), unpack(d, "out_"), FP64_TOL)
+    print("sod 2000 t=0.2 max field error", max(err.values()))
+
+
+def test_status_on_nonpositive_sound_speed():
+    """timestep asserts c > 0 (timestep.cc:126); the library returns
+    PLUME_E_NONPOSITIVE and the context stays usable."""
+    from plume_gpu.solver import PlumeError
+    case = cases.sod_1d(n_real=200)
+    case.particles.c[50] = 0.0
+    s = Solver(case)
+    with pytest.raises(PlumeError) as ei:
+        s.step()
+    assert ei.value.status == 4
+    ok = cases.sod_1d(n_real=200)
+    s.upload(ok.particles)
+    s.step()

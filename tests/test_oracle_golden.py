@@ -32,6 +32,19 @@ def test_oracle_1d_bit_exact(name):
         np.testing.assert_array_equal(getattr(o.ps.sorted_by_key(), f), getattr(ref, f))
 
 
+def test_oracle_sod_2000_full_run_bit_exact():
+    """The 1D Sod workload (2,000 particles, Gaussian kernel) to t = 0.2:
+    2,549 steps, final state identical to the reference's."""
+    case, d = golden_case("sod_1d_2000_end")
+    o = OracleRun(case, nthreads=0)
+    o.adaptive()
+    o.steps(int(d["nsteps"]))
+    assert o.t.step == int(d["step"][-1])
+    assert o.t.time == float(d["time"][-1])
+    err = field_errors(o.ps, unpack(d, "out_"))
+    assert max(err.values()) == 0.0, err
+
+
 def test_oracle_1d_lists_are_all_particles():
     case, d = golden_case("sod_1d_200")
     o = OracleRun(case)
