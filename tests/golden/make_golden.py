@@ -8,7 +8,10 @@ state and a summary of the reference's neighbour lists:
   sod_1d_200.npz       1D Sod, 200 equal-mass reals, cubic-spline kernel
                        (kernel-swap build), h = 1.3 m/rho, CFL 0.3, 20 steps
   sod_1d_2000_end.npz  the 1D Sod workload: 2,000 equal-mass reals, Gaussian
-                       kernel, run to t = 0.2 (final state only)
+                       kernel, run to t = 0.2 (final state only), plus the
+                       final state of a second reference run whose input
+                       differs by one ulp in the x of the wall-adjacent
+                       particle (the scheme's own sensitivity floor)
   shock_tube_1d.npz    the reference's shipped 1D deck (Gaussian kernel,
                        SHOCK_TUBE_TESTS 1, h0 = 0.003, 397 particles), 20 steps
   plume_3d_small.npz   3D plume, 600 m cube at 50 m spacing with pressure,
@@ -65,8 +68,17 @@ def pack(prefix, ps):
     return out
 
 
-def make(case, variant, nsteps, path, sample_lists=64, dump_last=False):
+def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_key=None):
     steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden", dump_last)
+    extra = {}
+    if perturb_key is not None:
+        pc = case.__class__(**{**case.__dict__, "particles": case.particles.copy()})
+        k = int(np.nonzero(pc.particles.key == perturb_key)[0][0])
+        pc.particles.x[k] = np.nextafter(pc.particles.x[k], np.inf)
+        psteps, _ = refio.run_ref(variant, pc, nsteps, "/tmp/plume_golden_p", dump_last)
+        extra.update(pack("ulp_", psteps[-1]["particles"].sorted_by_key()))
+        extra["ulp_key"] = np.uint64(perturb_key)
+        extra["ulp_step"] = psteps[-1]["step"]
     if dump_last:
         nsteps = steps[-1]["step"] - case.step0
     o = case.options
@@ -92,6 +104,7 @@ def make(case, variant, nsteps, path, sample_lists=64, dump_last=False):
     if o.dim == 3:
         # the lists of the last step were built from the state before it
         d.update(pack("pre_", steps[-2]["particles"].sorted_by_key()))
+    d.update(extra)
     np.savez_compressed(path, **d)
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
@@ -103,8 +116,10 @@ def main():
     refio.build_ref(a.ref)
     make(cases.sod_1d(n_real=200, kernel=cases.KERNEL_M4), "ref1d_sod", 20,
          os.path.join(HERE, "sod_1d_200.npz"))
-    make(cases.sod_1d(n_real=2000), "ref1d_sodg", -1, os.path.join(HERE, "sod_1d_2000_end.npz"),
-         sample_lists=4, dump_last=True)
+    sod = cases.sod_1d(n_real=2000)
+    wall = int(sod.particles.key[sod.particles.need_neigh()][0])  # first real particle
+    make(sod, "ref1d_sodg", -1, os.path.join(HERE, "sod_1d_2000_end.npz"),
+         sample_lists=4, dump_last=True, perturb_key=wall)
     make(cases.shock_tube_1d(), "ref1d_gauss", 20, os.path.join(HERE, "shock_tube_1d.npz"))
     c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
                        vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")
