@@ -23,6 +23,7 @@
 #include "../../include/plume_gpu.h"
 #include "radix_sort.cuh"
 #include "sph_kernels.cuh"
+#include "sph_warp.cuh"
 
 using namespace plume;
 
@@ -342,6 +343,10 @@ struct plume_ctx {
   size_t n_alloc = 0;  // rows in use (upper bound of live particles)
   Dev A{}, B{};
   Work W{};
+  Packed K{};  // FP32 pair records of the mixed path
+  // 3D sweep walk: one warp per particle (true) or one thread per particle;
+  // default per precision, PLUME_SWEEP=warp|thread overrides
+  bool sweep_warp = false;
   uint32_t *keys = nullptr, *perm = nullptr, *cs = nullptr;
   uint32_t ncells = 0;
   int keybits = 1;
@@ -463,18 +468,50 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   k_hmax<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->hb, D);
   k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->g, ctx->hb, ctx->h27);
   cudaEventRecord(ctx->ev[4], st);
-  k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
+  const bool mixed = sizeof(T) == 4;
+  if constexpr (D == 3) {
+    if (mixed) {
+      k_pack_mom<<<nb, NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->K, ctx->W, ctx->o.lans, ctx->d_count);
+      ctx->launches++;
+    }
+    if (ctx->sweep_warp)
+      k_sweep3<T, WMom, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+    else
+      k_sweep3<T, WMom, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  } else
+    k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
   cudaEventRecord(ctx->ev[5], st);
   k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
   ctx->launches += 5;
   cudaEventRecord(ctx->ev[6], st);
-  k_density<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  if constexpr (D == 3) {
+    if (mixed) {
+      k_pack_dens<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->o.pgc, ctx->d_count);
+      ctx->launches++;
+    }
+    if (ctx->sweep_warp)
+      k_sweep3<T, WDens, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+    else
+      k_sweep3<T, WDens, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  } else
+    k_density<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
   cudaEventRecord(ctx->ev[7], st);
   k_commit_dens<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
   ctx->launches += 2;
   cudaEventRecord(ctx->ev[8], st);
   if (ctx->o.lans) {
-    k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    if constexpr (D == 3) {
+      if (mixed) {
+        k_pack_vel<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
+        ctx->launches++;
+      }
+      if (ctx->sweep_warp)
+        k_sweep3<T, WVel, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+      else
+        k_sweep3<T, WVel, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+    } else
+      k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
     ctx->launches++;
   }
   cudaEventRecord(ctx->ev[9], st);
@@ -603,6 +640,11 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
   while ((1ull << ctx->keybits) <= (unsigned long long)ctx->ncells) ctx->keybits++;
   ctx->nbk = (opt->dim == 3) ? g.nb[0] * g.nb[1] * g.nb[2] : 1;
   ctx->cap = opt->capacity;
+  ctx->sweep_warp = (opt->precision == PLUME_PREC_FP64);
+  if (const char* sw = getenv("PLUME_SWEEP")) {
+    if (!strcmp(sw, "warp")) ctx->sweep_warp = true;
+    if (!strcmp(sw, "thread")) ctx->sweep_warp = false;
+  }
   int rc = PLUME_OK;
   auto fail = [&](int code) {
     g_create_error = ctx->err;
@@ -625,6 +667,11 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
     if ((rc = dev_alloc(ctx, (void**)&ctx->W.xr, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->W.yr, 4 * c)) ||
         (rc = dev_alloc(ctx, (void**)&ctx->W.zr, 4 * c)))
       return fail(rc);
+    if (opt->precision == PLUME_PREC_MIXED && opt->dim == 3) {
+      if ((rc = dev_alloc(ctx, (void**)&ctx->K.P, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.Q, 16 * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->K.R, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.S, 16 * c)))
+        return fail(rc);
+    }
     if ((rc = dev_alloc(ctx, (void**)&ctx->keys, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->perm, 4 * c)) ||
         (rc = dev_alloc(ctx, (void**)&ctx->cs, 4 * ((size_t)ctx->ncells + 2))) ||
         (rc = dev_alloc(ctx, (void**)&ctx->d_count, sizeof(int))) ||

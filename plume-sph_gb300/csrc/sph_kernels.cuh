@@ -89,6 +89,22 @@ struct Pos<D, float> {
   }
 };
 
+// dx = x_i - x_j in the sweep's arithmetic.  3D mixed: bucket-relative FP32
+// coordinates plus the segment's bucket offset; 1D mixed (every cell is its
+// own bucket): the FP64 difference rounded to FP32; FP64: absolute.
+template <int D, typename T>
+__device__ __forceinline__ void pair_dx(const T* xsh, const double* xi, const Dev& A, const Work& W, uint32_t j,
+                                        T* dx) {
+  if constexpr (D == 1 && sizeof(T) == 4) {
+    dx[0] = (T)(xi[0] - A.x[j]);
+  } else {
+    T xj[3];
+    Pos<D, T>::load(A, W, j, xj);
+#pragma unroll
+    for (int k = 0; k < D; k++) dx[k] = xsh[k] - xj[k];
+  }
+}
+
 template <int D, typename T>
 __device__ __forceinline__ bool in_box(const T* dx, T r) {
 #pragma unroll
@@ -125,14 +141,10 @@ __global__ void k_adaptive(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
       T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
       for (uint32_t j = j0; j < j1; j++) {
         if (!contr_dens(A.bc[j], o.pgc)) continue;
-        T xj[3];
-        Pos<D, T>::load(A, W, j, xj);
         T dx[3], si[3];
+        pair_dx<D, T>(xsh, xi, A, W, j, dx);
 #pragma unroll
-        for (int k = 0; k < D; k++) {
-          dx[k] = xsh[k] - xj[k];
-          si[k] = dx[k] / H_star;
-        }
+        for (int k = 0; k < D; k++) si[k] = dx[k] / H_star;
         if (!own && !in_box<D, T>(dx, Lb)) continue;
         if (!in_box<D, T>(dx, supp)) continue;
         T mj = T(A.mass[j]);
@@ -199,11 +211,8 @@ __global__ void k_momentum(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
     T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
     for (uint32_t j = j0; j < j1; j++) {
       if (j == (uint32_t)i) continue;
-      T xj[3];
-      Pos<D, T>::load(A, W, j, xj);
       T dx[3];
-#pragma unroll
-      for (int k = 0; k < D; k++) dx[k] = xsh[k] - xj[k];
+      pair_dx<D, T>(xsh, xi, A, W, j, dx);
       if (!own && !in_box<D, T>(dx, Lb)) continue;
       if (!in_box<D, T>(dx, supp)) continue;
       const T hj = T(A.h[j]);
@@ -337,11 +346,8 @@ __global__ void k_density(Opt o, Geo g, Dev A, Work W, const uint32_t* __restric
       if (!contr_dens(bcj, o.pgc)) continue;
       const uint8_t ph = A.phase[j];
       if (ph != 1 && ph != 2) continue;
-      T xj[3];
-      Pos<D, T>::load(A, W, j, xj);
       T ds[3];
-#pragma unroll
-      for (int k = 0; k < D; k++) ds[k] = xsh[k] - xj[k];
+      pair_dx<D, T>(xsh, xi, A, W, j, ds);
       if (!own && !in_box<D, T>(ds, Lb)) continue;
       if (!in_box<D, T>(ds, supp)) continue;
       const T mj = T(A.mass[j]);
@@ -430,11 +436,8 @@ __global__ void k_velocity(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
     T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
     for (uint32_t j = j0; j < j1; j++) {
       if (!contr_vel_smooth(A.bc[j])) continue;
-      T xj[3];
-      Pos<D, T>::load(A, W, j, xj);
       T ds[3];
-#pragma unroll
-      for (int k = 0; k < D; k++) ds[k] = xsh[k] - xj[k];
+      pair_dx<D, T>(xsh, xi, A, W, j, ds);
       if (!own && !in_box<D, T>(ds, Lb)) continue;
       if (!in_box<D, T>(ds, supp)) continue;
       const T rhoj = T(A.rho[j]);

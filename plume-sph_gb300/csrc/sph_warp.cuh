@@ -1,0 +1,561 @@
+// sph_warp.cuh -- warp-per-particle 3D pair sweeps with ballot compaction.
+//
+// One warp owns one particle i at a time.  Its lanes walk i's candidate
+// rows (the search box clipped to the 27 buckets around i's bucket,
+// search_neighs_consth, neighs.cc:37-211) 32 candidates at a time and apply
+// a cheap, conservative filter: the reference's list rule (own bucket or
+// inside list_factor * h_i, neighs.cc:84-131), the sweep's particle
+// predicate and box, and the kernel support |dx_k| <= ksupport * h_ij.
+// Survivors are compacted (ballot + popc) into a per-warp buffer; every
+// time 32 have gathered, each lane evaluates one pair with the exact
+// arithmetic of the sweep (pairs beyond the kernel support contribute
+// exactly zero in the reference, so dropping them changes no sum).  The
+// lanes' partial sums are reduced in FP64 at the end of the particle.
+//
+// The FP64 path reads the particle arrays directly; the mixed path reads
+// per-sweep packed FP32 records (float4) written by k_pack_* with
+// bucket-relative coordinates.
+#pragma once
+#include "sph_kernels.cuh"
+
+namespace plume {
+
+constexpr unsigned WFULL = 0xffffffffu;
+constexpr int WP_WARPS = 4;  // warps per block (128 threads)
+
+// packed FP32 records of the mixed path (one set, rewritten per sweep)
+struct Packed {
+  float4* P;  // (xr, yr, zr, h or -h when the particle does not contribute)
+  float4* Q;
+  float4* R;
+  float4* S;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(WFULL, v, o);
+  return v;
+}
+
+// per-warp compaction buffer
+template <typename T>
+struct WBuf {
+  int j[64];
+  T dx[3][64];
+};
+
+// fast reciprocal for the mixed path, exact division for FP64
+template <typename T>
+__device__ __forceinline__ T rcp(T x) { return T(1) / x; }
+template <>
+__device__ __forceinline__ float rcp<float>(float x) { return __frcp_rn(x); }
+
+// Walks the candidates of particle i (warp-uniform arguments) and calls
+// s.math(j, dx) for every survivor of s.filter(j, own, ox, oy, oz, dx).
+template <typename T, class S>
+__device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict__ cs, const double* xi,
+                                        const int* bi, double R, WBuf<T>& B, S& s) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  int count = 0;
+  int lo[3], hi[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    int l = cell_axis(g, a, xi[a] - R, nullptr, nullptr);
+    int h = cell_axis(g, a, xi[a] + R, nullptr, nullptr);
+    lo[a] = max(l, max((bi[a] - 1) * g.s, 0));
+    hi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
+  }
+  constexpr bool REL = sizeof(T) == 4;
+  for (int cz = lo[2]; cz <= hi[2]; cz++) {
+    const int bz = cz / g.s;
+    const T oz = REL ? T((bi[2] - bz) * g.del) : T(0);
+    for (int cy = lo[1]; cy <= hi[1]; cy++) {
+      const int by = cy / g.s;
+      const T oy = REL ? T((bi[1] - by) * g.del) : T(0);
+      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      int cx = lo[0];
+      while (cx <= hi[0]) {
+        const int bx = cx / g.s;
+        const int e = min(hi[0], bx * g.s + g.s - 1);
+        const uint32_t j0 = cs[rowbase + cx];
+        const uint32_t j1 = cs[rowbase + e + 1];
+        const bool own = (bx == bi[0]) && (by == bi[1]) && (bz == bi[2]);
+        const T ox = REL ? T((bi[0] - bx) * g.del) : T(0);
+        for (uint32_t jb = j0; jb < j1; jb += 32) {
+          const uint32_t j = jb + lane;
+          T dx[3];
+          const bool take = (j < j1) && s.filter(j, own, ox, oy, oz, dx);
+          const unsigned m = __ballot_sync(WFULL, take);
+          if (take) {
+            const int slot = count + __popc(m & lt);
+            B.j[slot] = (int)j;
+            B.dx[0][slot] = dx[0];
+            B.dx[1][slot] = dx[1];
+            B.dx[2][slot] = dx[2];
+          }
+          count += __popc(m);
+          __syncwarp();
+          if (count >= 32) {
+            T d[3] = {B.dx[0][lane], B.dx[1][lane], B.dx[2][lane]};
+            s.math(B.j[lane], d);
+            __syncwarp();
+            const int rest = count - 32;
+            if (lane < rest) {
+              B.j[lane] = B.j[lane + 32];
+              B.dx[0][lane] = B.dx[0][lane + 32];
+              B.dx[1][lane] = B.dx[1][lane + 32];
+              B.dx[2][lane] = B.dx[2][lane + 32];
+            }
+            count = rest;
+            __syncwarp();
+          }
+        }
+        cx = e + 1;
+      }
+    }
+  }
+  if (lane < count) {
+    T d[3] = {B.dx[0][lane], B.dx[1][lane], B.dx[2][lane]};
+    s.math(B.j[lane], d);
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------ particle data
+// FP64 path: SoA loads; mixed path: packed records
+template <typename T>
+struct JPos;
+template <>
+struct JPos<double> {
+  __device__ __forceinline__ static void get(const Dev& A, const Packed&, uint32_t j, double* x, double& h) {
+    x[0] = A.x[j]; x[1] = A.y[j]; x[2] = A.z[j];
+    h = A.h[j];
+  }
+};
+template <>
+struct JPos<float> {
+  __device__ __forceinline__ static void get(const Dev&, const Packed& K, uint32_t j, float* x, float& h) {
+    const float4 p = K.P[j];
+    x[0] = p.x; x[1] = p.y; x[2] = p.z;
+    h = p.w;
+  }
+};
+
+// ------------------------------------------------------------ momentum
+template <typename T>
+struct WMom {
+  const Dev& A;
+  const Packed& K;
+  const Opt& o;
+  bool lans;
+  uint32_t i;
+  T xs[3], hi, supp, Lb, rhoi, Vi, pvsqi, ci, tempi, Cp_i, veli[3];
+  Acc<T> rv[3], re;
+  __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
+  // i-side set-up; returns false (with the status set) when i is skipped
+  __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState* ts,
+                                        double* xi, int* bi, double& R) {
+    const double rho_i = A.rho[ii];
+    if (!(rho_i > 0)) {
+      set_status(ts, 4);
+      return false;
+    }
+    lans = o.lans != 0;
+    i = (uint32_t)ii;
+    xi[0] = A.x[ii]; xi[1] = A.y[ii]; xi[2] = A.z[ii];
+    const int b = A.bkt[ii];
+    bucket_coords<3>(g, b, bi);
+    Pos<3, T>::load(A, W, ii, xs);
+    const double hi_d = A.h[ii];
+    hi = T(hi_d);
+    supp = T(o.cutoff2) * hi;
+    Lb = T(o.list_factor * W.hlist[ii]);
+    rhoi = T(rho_i);
+    Vi = T(1.0) / rhoi;
+    pvsqi = T(A.p[ii]) * Vi * Vi;
+    ci = T(A.c[ii]);
+    tempi = T(A.T[ii]);
+    Cp_i = T(A.cp[ii]);
+    if (lans) {
+      veli[0] = T(A.vsx[ii]); veli[1] = T(A.vsy[ii]); veli[2] = T(A.vsz[ii]);
+    } else {
+      veli[0] = T(A.vx[ii]); veli[1] = T(A.vy[ii]); veli[2] = T(A.vz[ii]);
+    }
+    R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hmax[b])) * (1.0 + 1e-10);
+    return true;
+  }
+  template <bool WARP>
+  __device__ __forceinline__ void finish(int ii, Work& W, TimeState* ts) {
+    double r0 = (double)rv[0].get(), r1 = (double)rv[1].get(), r2 = (double)rv[2].get();
+    double e = (double)re.get();
+    if (WARP) {
+      r0 = warp_sum(r0); r1 = warp_sum(r1); r2 = warp_sum(r2); e = warp_sum(e);
+      if ((threadIdx.x & 31) != 0) return;
+    }
+    const double dt = ts->dtime;
+    const double grav = -o.g;
+    double unew2 = A.vz[ii] + dt * r2;
+    unew2 += dt * grav;
+    W.nv0[ii] = A.vx[ii] + dt * r0;
+    W.nv1[ii] = A.vy[ii] + dt * r1;
+    W.nv2[ii] = unew2;
+    W.ne[ii] = A.e[ii] + dt * (e + (double)veli[2] * grav);
+  }
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
+    if (j == i) return false;
+    T xj[3], hj;
+    JPos<T>::get(A, K, j, xj, hj);
+    dx[0] = (xs[0] + ox) - xj[0];
+    dx[1] = (xs[1] + oy) - xj[1];
+    dx[2] = (xs[2] + oz) - xj[2];
+    if (!own && !in_box<3, T>(dx, Lb)) return false;
+    if (!in_box<3, T>(dx, supp)) return false;
+    const T ks = T(o.ksupport * 0.5 * (1.0 + 1e-6)) * (hi + fabs(hj));
+    return in_box<3, T>(dx, ks);
+  }
+  __device__ __forceinline__ void load_j(uint32_t j, T& hj, T& mj, T& rhoj, T& pj, T& cj, T& Tj, T& cpj,
+                                         T* vj) const;
+  __device__ __forceinline__ void math(uint32_t j, const T* dx) {
+    T hj, mj, rhoj, pressj, cj, Tj, cpj, vj[3];
+    load_j(j, hj, mj, rhoj, pressj, cj, Tj, cpj, vj);
+    const T h = T(0.5) * (hi + hj);
+    const T ih = rcp<T>(h);
+    T si[3], dist_sq = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      si[k] = (sizeof(T) == 8) ? dx[k] / h : dx[k] * ih;
+      dist_sq += dx[k] * dx[k];
+    }
+    const T Vj = rcp<T>(rhoj);
+    T velij[3] = {veli[0] - vj[0], veli[1] - vj[1], veli[2] - vj[2]};
+    const T rhoab = T(0.5) * (rhoi + rhoj);
+    const T sndspdab = T(0.5) * (ci + cj);
+    T vrab = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) vrab += dx[k] * velij[k];
+    const T miuab = (sizeof(T) == 8) ? h * vrab / (dist_sq + T(o.ata) * h * h)
+                                     : h * vrab * rcp<T>(dist_sq + T(o.ata) * h * h);
+    T vis = 0;
+    if (vrab < 0)
+      vis = (sizeof(T) == 8) ? (T(o.beta) * miuab - T(o.alpha) * sndspdab) * miuab / rhoab
+                             : (T(o.beta) * miuab - T(o.alpha) * sndspdab) * miuab * rcp<T>(rhoab);
+    T dotv = 0;
+    if (lans) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) dotv += velij[k] * velij[k];
+      vis -= T(EPS_HALF) * dotv * Vj;
+    }
+    const T mpvsqij = mj * (pressj * Vj * Vj + pvsqi + vis);
+    T dwdx[3];
+    if (sizeof(T) == 8 || o.kernel == 1) {
+      kdw<3, T>(o.kernel, si, h, dwdx);
+    } else {
+      // Gaussian, mixed: W = (T1/h)^3 exp(-s.s), dW/dx_k = -2 s_k / h W
+      const T w = (fabs(si[0]) > T(3) || fabs(si[1]) > T(3) || fabs(si[2]) > T(3))
+                      ? T(0)
+                      : (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) *
+                            __expf(-(si[0] * si[0] + si[1] * si[1] + si[2] * si[2]));
+      const T f = T(-2) * ih * w;
+#pragma unroll
+      for (int k = 0; k < 3; k++) dwdx[k] = f * si[k];
+    }
+    T heat_tran = 0;
+    if (lans) {
+      const T Cp_ij = T(0.5) * (cpj + Cp_i);
+      T dotvr = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) dotvr += fabs(velij[k] * dx[k]);
+      T kij = 0;
+      if (dotvr != T(0)) {
+        const T kab = (sizeof(T) == 8)
+                          ? T(10.0) * T(EPS_HALF) * Cp_ij * dist_sq * dotv / (T(PRANDTL) * dotvr)
+                          : T(10.0) * T(EPS_HALF) * Cp_ij * dist_sq * dotv * rcp<T>(T(PRANDTL) * dotvr);
+        kij = (sizeof(T) == 8) ? kab / (h * sndspdab) : kab * rcp<T>(h * sndspdab);
+      }
+      T W_r = 0, Fij = 0;
+#pragma unroll
+      for (int k = 0; k < 3; k++) W_r += dwdx[k] * dx[k];
+      if (W_r != T(0)) Fij = (sizeof(T) == 8) ? W_r / dist_sq : W_r * rcp<T>(dist_sq);
+      heat_tran = mj * Vj * Vi * kij * (tempi - Tj) * Fij;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) rv[k].sub(mpvsqij * dwdx[k]);
+    T deltae = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) deltae += T(0.5) * (mpvsqij * dwdx[k]) * velij[k];
+    re.add(deltae + heat_tran);
+  }
+};
+template <>
+__device__ __forceinline__ void WMom<double>::load_j(uint32_t j, double& hj, double& mj, double& rhoj,
+                                                     double& pj, double& cj, double& Tj, double& cpj,
+                                                     double* vj) const {
+  hj = A.h[j]; mj = A.mass[j]; rhoj = A.rho[j]; pj = A.p[j]; cj = A.c[j]; Tj = A.T[j]; cpj = A.cp[j];
+  if (lans) {
+    vj[0] = A.vsx[j]; vj[1] = A.vsy[j]; vj[2] = A.vsz[j];
+  } else {
+    vj[0] = A.vx[j]; vj[1] = A.vy[j]; vj[2] = A.vz[j];
+  }
+}
+template <>
+__device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& hj, float& mj, float& rhoj, float& pj,
+                                                    float& cj, float& Tj, float& cpj, float* vj) const {
+  const float4 p = K.P[j], q = K.Q[j], r = K.R[j], s = K.S[j];
+  hj = fabsf(p.w);
+  mj = q.x; rhoj = q.y; pj = q.z; cj = q.w;
+  Tj = r.x; cpj = r.y; vj[0] = r.z; vj[1] = r.w;
+  vj[2] = s.x;
+}
+
+// momentum record: P (xr,yr,zr,h), Q (m,rho,p,c), R (T,cp,vx,vy), S (vz)
+__global__ void k_pack_mom(Geo g, Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], (float)A.h[j]);
+  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.p[j], (float)A.c[j]);
+  if (lans) {
+    K.R[j] = make_float4((float)A.T[j], (float)A.cp[j], (float)A.vsx[j], (float)A.vsy[j]);
+    K.S[j] = make_float4((float)A.vsz[j], 0.f, 0.f, 0.f);
+  } else {
+    K.R[j] = make_float4((float)A.T[j], (float)A.cp[j], (float)A.vx[j], (float)A.vy[j]);
+    K.S[j] = make_float4((float)A.vz[j], 0.f, 0.f, 0.f);
+  }
+}
+
+// ------------------------------------------------------------ density
+template <typename T>
+struct WDens {
+  const Dev& A;
+  const Packed& K;
+  const Opt& o;
+  int pgc;
+  T xs[3], hi, supp, Lb;
+  Acc<T> rho1, rho2, wnorm_e, engr;
+  bool esm;
+  __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
+  __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
+                                        double* xi, int* bi, double& R) {
+    pgc = o.pgc;
+    esm = o.esmooth != 0;
+    xi[0] = A.x[ii]; xi[1] = A.y[ii]; xi[2] = A.z[ii];
+    const int b = A.bkt[ii];
+    bucket_coords<3>(g, b, bi);
+    Pos<3, T>::load(A, W, ii, xs);
+    const double hi_d = A.h[ii];
+    hi = T(hi_d);
+    supp = T(o.cutoff2) * hi;
+    Lb = T(o.list_factor * W.hlist[ii]);
+    R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hmax[b])) * (1.0 + 1e-10);
+    return true;
+  }
+  template <bool WARP>
+  __device__ __forceinline__ void finish(int ii, Work& W, TimeState* ts) {
+    double r1 = (double)rho1.get(), r2 = (double)rho2.get();
+    double wn = (double)wnorm_e.get(), en = (double)engr.get();
+    if (WARP) {
+      r1 = warp_sum(r1); r2 = warp_sum(r2); wn = warp_sum(wn); en = warp_sum(en);
+      if ((threadIdx.x & 31) != 0) return;
+    }
+    if (esm) {
+      if (!(wn > 0)) {
+        set_status(ts, 4);
+        return;
+      }
+      W.nE[ii] = en / wn;
+    }
+    double density = 0.0;
+    density += r1;
+    density += r2;
+    if (!(density > 0)) {
+      set_status(ts, (density != density) ? 3 : 4);
+      return;
+    }
+    W.nrho[ii] = density;
+    W.nY[ii] = r2 / density;
+  }
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
+    T xj[3], hj;
+    JPos<T>::get(A, K, j, xj, hj);
+    if (sizeof(T) == 8) {
+      const uint8_t ph = A.phase[j];
+      if (!contr_dens(A.bc[j], pgc) || (ph != 1 && ph != 2)) return false;
+    } else if (hj < T(0)) {
+      return false;
+    }
+    dx[0] = (xs[0] + ox) - xj[0];
+    dx[1] = (xs[1] + oy) - xj[1];
+    dx[2] = (xs[2] + oz) - xj[2];
+    if (!own && !in_box<3, T>(dx, Lb)) return false;
+    if (!in_box<3, T>(dx, supp)) return false;
+    const T ks = T(o.ksupport * 0.5 * (1.0 + 1e-6)) * (hi + fabs(hj));
+    return in_box<3, T>(dx, ks);
+  }
+  __device__ __forceinline__ void math(uint32_t j, const T* ds) {
+    T hj, mj, rhoj, ej, ph;
+    if (sizeof(T) == 8) {
+      hj = T(A.h[j]); mj = T(A.mass[j]); rhoj = T(A.rho[j]); ej = T(A.e[j]); ph = T(A.phase[j]);
+    } else {
+      const float4 p = K.P[j], q = K.Q[j];
+      hj = T(p.w); mj = T(q.x); rhoj = T(q.y); ej = T(q.z); ph = T(q.w);
+    }
+    const T hh = T(0.5) * (hi + hj);
+    T sv[3];
+    const T ih = rcp<T>(hh);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hh : ds[k] * ih;
+    if (esm) {
+      T s_e[3];
+#pragma unroll
+      for (int k = 0; k < 3; k++) s_e[k] = (sizeof(T) == 8) ? T(E_SMOOTH) * ds[k] / hh : T(E_SMOOTH) * ds[k] * ih;
+      const T wm_e = kw<3, T>(o.kernel, s_e, (sizeof(T) == 8) ? hh / T(E_SMOOTH) : hh * T(0.25)) * mj;
+      const T irho = rcp<T>(rhoj);
+      wnorm_e.add((sizeof(T) == 8) ? wm_e / rhoj : wm_e * irho);
+      engr.add((sizeof(T) == 8) ? wm_e * ej / rhoj : wm_e * ej * irho);
+    }
+    const T wm = kw<3, T>(o.kernel, sv, hh) * mj;
+    if (ph == T(1))
+      rho1.add(wm);
+    else
+      rho2.add(wm);
+  }
+};
+
+// density record: P (xr,yr,zr,+-h: - when not contributing), Q (m,rho,e,phase)
+__global__ void k_pack_dens(Dev A, Packed K, Work W, int pgc, const int* __restrict__ d_count) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  const uint8_t ph = A.phase[j];
+  const bool c = contr_dens(A.bc[j], pgc) && (ph == 1 || ph == 2);
+  const float h = (float)A.h[j];
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], c ? h : -h);
+  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.e[j], (float)ph);
+}
+
+// ------------------------------------------------------------ velocity
+template <typename T>
+struct WVel {
+  const Dev& A;
+  const Packed& K;
+  const Opt& o;
+  T xs[3], hi, supp, ks, Lb, vi[3];
+  Acc<T> dv[3], wnorm;
+  __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
+  double vi_d[3];
+  __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double*, TimeState*,
+                                        double* xi, int* bi, double& R) {
+    xi[0] = A.x[ii]; xi[1] = A.y[ii]; xi[2] = A.z[ii];
+    bucket_coords<3>(g, A.bkt[ii], bi);
+    Pos<3, T>::load(A, W, ii, xs);
+    const double hi_d = A.h[ii];
+    hi = T(hi_d);
+    supp = T(o.cutoff2) * hi;
+    ks = T(o.ksupport * (1.0 + 1e-6)) * hi;
+    Lb = T(o.list_factor * W.hlist[ii]);
+    vi_d[0] = A.vx[ii]; vi_d[1] = A.vy[ii]; vi_d[2] = A.vz[ii];
+    vi[0] = T(vi_d[0]); vi[1] = T(vi_d[1]); vi[2] = T(vi_d[2]);
+    R = fmin(o.cutoff2, o.ksupport) * hi_d * (1.0 + 1e-10);
+    return true;
+  }
+  template <bool WARP>
+  __device__ __forceinline__ void finish(int ii, Work&, TimeState* ts) {
+    double d0 = (double)dv[0].get(), d1 = (double)dv[1].get(), d2 = (double)dv[2].get();
+    double wn = (double)wnorm.get();
+    if (WARP) {
+      d0 = warp_sum(d0); d1 = warp_sum(d1); d2 = warp_sum(d2); wn = warp_sum(wn);
+      if ((threadIdx.x & 31) != 0) return;
+    }
+    if (!(wn > 0)) {
+      set_status(ts, 4);
+      return;
+    }
+    A.vsx[ii] = vi_d[0] + d0 / wn;
+    A.vsy[ii] = vi_d[1] + d1 / wn;
+    A.vsz[ii] = vi_d[2] + d2 / wn;
+  }
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
+    T xj[3], flag;
+    JPos<T>::get(A, K, j, xj, flag);
+    if (sizeof(T) == 8) {
+      if (!contr_vel_smooth(A.bc[j])) return false;
+    } else if (flag < T(0)) {
+      return false;
+    }
+    dx[0] = (xs[0] + ox) - xj[0];
+    dx[1] = (xs[1] + oy) - xj[1];
+    dx[2] = (xs[2] + oz) - xj[2];
+    if (!own && !in_box<3, T>(dx, Lb)) return false;
+    if (!in_box<3, T>(dx, supp)) return false;
+    return in_box<3, T>(dx, ks);
+  }
+  __device__ __forceinline__ void math(uint32_t j, const T* ds) {
+    T mj, rhoj, vj[3];
+    if (sizeof(T) == 8) {
+      mj = T(A.mass[j]); rhoj = T(A.rho[j]);
+      vj[0] = T(A.vx[j]); vj[1] = T(A.vy[j]); vj[2] = T(A.vz[j]);
+    } else {
+      const float4 q = K.Q[j], r = K.R[j];
+      mj = T(q.x); rhoj = T(q.y); vj[0] = T(q.z); vj[1] = T(q.w); vj[2] = T(r.x);
+    }
+    T sv[3];
+    const T ih = rcp<T>(hi);
+#pragma unroll
+    for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hi : ds[k] * ih;
+    const T wght = kw<3, T>(o.kernel, sv, hi);
+    const T mvw = (sizeof(T) == 8) ? wght * mj / rhoj : wght * mj * rcp<T>(rhoj);
+#pragma unroll
+    for (int k = 0; k < 3; k++) dv[k].add(mvw * (vj[k] - vi[k]));
+    wnorm.add(mvw);
+  }
+};
+
+// velocity record: P (xr,yr,zr,+-1: - when not contributing), Q (m,rho,vx,vy), R (vz)
+__global__ void k_pack_vel(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], contr_vel_smooth(A.bc[j]) ? 1.f : -1.f);
+  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.vx[j], (float)A.vy[j]);
+  K.R[j] = make_float4((float)A.vz[j], 0.f, 0.f, 0.f);
+}
+
+
+// ------------------------------------------------------------ driver kernel
+// WARP = true: one warp per particle with ballot compaction (wp_walk);
+// WARP = false: one thread per particle walking its own rows.
+template <typename T, template <typename> class SW, bool WARP>
+__global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Packed K,
+                                                const uint32_t* __restrict__ cs,
+                                                const double* __restrict__ hmax,
+                                                const int* __restrict__ d_count, TimeState* ts) {
+  const int n = *d_count;
+  if (WARP) {
+    __shared__ WBuf<T> bufs[WP_WARPS];
+    WBuf<T>& B = bufs[threadIdx.x >> 5];
+    const int nw = gridDim.x * WP_WARPS;
+    for (int i = blockIdx.x * WP_WARPS + (threadIdx.x >> 5); i < n; i += nw) {
+      if (!need_neigh(A.bc[i])) continue;
+      SW<T> s(A, K, o);
+      double xi[3], R;
+      int bi[3];
+      if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) continue;
+      wp_walk<T>(g, cs, xi, bi, R, B, s);
+      s.template finish<true>(i, W, ts);
+    }
+  } else {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !need_neigh(A.bc[i])) return;
+    SW<T> s(A, K, o);
+    double xi[3], R;
+    int bi[3];
+    if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;
+    for_segments<3, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+      for (uint32_t j = j0; j < j1; j++) {
+        T dx[3];
+        if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+      }
+    });
+    s.template finish<false>(i, W, ts);
+  }
+}
+
+}  // namespace plume
