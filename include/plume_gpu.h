@@ -238,7 +238,7 @@ int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):
  * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket
- * max h, [3] momentum/energy sweep, [4] its commit + EOS, [5] density sweep,
+ * max h and per-step neighbour lists, [3] momentum/energy sweep, [4] its commit + EOS, [5] density sweep,
  * [6] its commit + EOS, [7] velocity filter, [8] position update and
  * re-bucketing, [9] dt reduction, [10] total.  n <= 11 entries. */
 int plume_phase_times(plume_ctx *ctx, float *ms, int n);

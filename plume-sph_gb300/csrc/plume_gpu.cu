@@ -30,7 +30,7 @@ using namespace plume;
 namespace {
 
 constexpr int NTHREADS = 128;
-// phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax, 3 momentum,
+// phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax + lists, 3 momentum,
 // 4 commit_mom, 5 density, 6 commit_dens, 7 velocity, 8 position, 9 dt,
 // 10 total
 constexpr int NPHASE = 11;
@@ -287,16 +287,29 @@ __global__ void k_scan_blocks(const unsigned int* __restrict__ cnt, int n, unsig
   if (i < n) out[i] = s[t] - cnt[i];
   if (t == 1023) sums[blockIdx.x] = s[t];
 }
+// exclusive scan of the m block sums by one CTA of 1024 threads
 __global__ void k_scan_sums(unsigned long long* sums, int m, unsigned long long* total) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    unsigned long long run = 0;
-    for (int b = 0; b < m; b++) {
-      unsigned long long v = sums[b];
-      sums[b] = run;
-      run += v;
-    }
-    *total = run;
+  __shared__ unsigned long long part[1024];
+  const int t = threadIdx.x;
+  const int per = (m + 1023) / 1024;
+  const int lo = t * per, hi = min(lo + per, m);
+  unsigned long long s = 0;
+  for (int b = lo; b < hi; b++) s += sums[b];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    unsigned long long v = (t >= off) ? part[t - off] : 0ull;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
   }
+  unsigned long long run = (t == 0) ? 0ull : part[t - 1];
+  for (int b = lo; b < hi; b++) {
+    unsigned long long v = sums[b];
+    sums[b] = run;
+    run += v;
+  }
+  if (t == 1023) *total = part[1023];
 }
 __global__ void k_scan_add(unsigned long long* out, int n, const unsigned long long* __restrict__ sums) {
   int i = blockIdx.x * 1024 + threadIdx.x;
@@ -344,6 +357,13 @@ struct plume_ctx {
   Dev A{}, B{};
   Work W{};
   Packed K{};  // FP32 pair records of the mixed path
+  NList L{};   // per-step masked neighbour lists (3D)
+  bool use_lists = true;
+  // compacted need_neigh indices of the step (3D list sweeps)
+  unsigned int* rflag = nullptr;
+  unsigned long long *roffs = nullptr, *rsums = nullptr, *rtot = nullptr;
+  uint32_t* real_idx = nullptr;
+  int* d_real = nullptr;
   // 3D sweep walk: one warp per particle (true) or one thread per particle;
   // default per precision, PLUME_SWEEP=warp|thread overrides
   bool sweep_warp = false;
@@ -467,15 +487,35 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
   k_hmax<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->hb, D);
   k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->g, ctx->hb, ctx->h27);
-  cudaEventRecord(ctx->ev[4], st);
   const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
   const bool mixed = sizeof(T) == 4;
+  const bool lists = (D == 3) && ctx->use_lists;
+  if constexpr (D == 3) {
+    if (lists) {
+      const int ns = n ? n : 1, nsb = (ns + 1023) / 1024;
+      k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->rflag);
+      k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, ns, ctx->roffs, ctx->rsums);
+      k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
+      k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, ns, ctx->rsums);
+      k_real_scatter<<<nb, NTHREADS, 0, st>>>(ctx->rflag, ctx->roffs, ns, ctx->real_idx, ctx->d_real, ctx->rtot);
+      ctx->launches += 5;
+      if (mixed) {
+        k_pack_pos<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
+        ctx->launches++;
+      }
+      k_build_lists<T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->L);
+      ctx->launches++;
+    }
+  }
+  cudaEventRecord(ctx->ev[4], st);
   if constexpr (D == 3) {
     if (mixed) {
       k_pack_mom<<<nb, NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->K, ctx->W, ctx->o.lans, ctx->d_count);
       ctx->launches++;
     }
-    if (ctx->sweep_warp)
+    if (lists)
+      k_sweep3_list<T, WMom><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+    else if (ctx->sweep_warp)
       k_sweep3<T, WMom, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
       k_sweep3<T, WMom, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
@@ -490,7 +530,9 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       k_pack_dens<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->o.pgc, ctx->d_count);
       ctx->launches++;
     }
-    if (ctx->sweep_warp)
+    if (lists)
+      k_sweep3_list<T, WDens><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+    else if (ctx->sweep_warp)
       k_sweep3<T, WDens, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
       k_sweep3<T, WDens, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
@@ -506,7 +548,9 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         k_pack_vel<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
         ctx->launches++;
       }
-      if (ctx->sweep_warp)
+      if (lists)
+        k_sweep3_list<T, WVel><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      else if (ctx->sweep_warp)
         k_sweep3<T, WVel, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
       else
         k_sweep3<T, WVel, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
@@ -642,8 +686,9 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
   ctx->cap = opt->capacity;
   ctx->sweep_warp = (opt->precision == PLUME_PREC_FP64);
   if (const char* sw = getenv("PLUME_SWEEP")) {
-    if (!strcmp(sw, "warp")) ctx->sweep_warp = true;
-    if (!strcmp(sw, "thread")) ctx->sweep_warp = false;
+    if (!strcmp(sw, "warp")) { ctx->sweep_warp = true; ctx->use_lists = false; }
+    if (!strcmp(sw, "thread")) { ctx->sweep_warp = false; ctx->use_lists = false; }
+    if (!strcmp(sw, "list")) { ctx->sweep_warp = false; ctx->use_lists = true; }
   }
   int rc = PLUME_OK;
   auto fail = [&](int code) {
@@ -667,6 +712,17 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
     if ((rc = dev_alloc(ctx, (void**)&ctx->W.xr, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->W.yr, 4 * c)) ||
         (rc = dev_alloc(ctx, (void**)&ctx->W.zr, 4 * c)))
       return fail(rc);
+    if (opt->dim == 3 && ctx->use_lists) {
+      if ((rc = dev_alloc(ctx, (void**)&ctx->L.e, sizeof(uint2) * (size_t)LCAP * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->L.cnt, sizeof(uint16_t) * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->rflag, 4 * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->roffs, 8 * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->rsums, 8 * (c / 1024 + 2))) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->rtot, 8)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->real_idx, 4 * c)) ||
+          (rc = dev_alloc(ctx, (void**)&ctx->d_real, sizeof(int))))
+        return fail(rc);
+    }
     if (opt->precision == PLUME_PREC_MIXED && opt->dim == 3) {
       if ((rc = dev_alloc(ctx, (void**)&ctx->K.P, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.Q, 16 * c)) ||
           (rc = dev_alloc(ctx, (void**)&ctx->K.R, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.S, 16 * c)))
@@ -1026,7 +1082,7 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
   unsigned long long total = 0;
   if (np) {
     k_scan_blocks<<<nbk, 1024, 0, st>>>(cnt, np, offs, sums);
-    k_scan_sums<<<1, 1, 0, st>>>(sums, nbk, tot);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, nbk, tot);
     k_scan_add<<<nbk, 1024, 0, st>>>(offs, np, sums);
     CK(cudaMemcpyAsync(&total, tot, 8, cudaMemcpyDeviceToHost, st));
   }

@@ -558,4 +558,188 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Pac
   }
 }
 
+
+// ------------------------------------------------------------ neighbour lists
+// Per-step masked neighbour lists.  One walk per step (after the adaptive
+// smoothing length, when positions and h are final for the step) records,
+// for every need_neigh particle, the windows of at most 32 consecutive
+// candidates of one row segment that hold at least one pair of the union
+// of the three sweeps' supports, as (window start | bucket-offset code << 26,
+// 32-bit mask).  The momentum, density and velocity sweeps then visit the
+// set bits in order (row, segment, index: the walk's order) and apply their
+// own exact tests, so the sums are those of the walk; the divergent
+// candidate filtering is paid once per step instead of once per sweep.
+constexpr int LCAP = 160;                 // windows per particle
+constexpr uint16_t NL_OVERFLOW = 0xFFFF;  // particle walks instead
+constexpr uint32_t NL_JMASK = (1u << 26) - 1u;
+
+struct NList {
+  uint2* e;        // capacity * LCAP entries
+  uint16_t* cnt;   // windows per particle, or NL_OVERFLOW
+};
+
+// like for_segments, with the bucket offset of the segment as a code
+// (dbx+1)*9 + (dby+1)*3 + (dbz+1), db = segment bucket - own bucket
+template <typename T, class F>
+__device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* __restrict__ cs,
+                                                  const double* xi, const int* bi, double R, F&& f) {
+  int lo[3], hi[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    int l = cell_axis(g, a, xi[a] - R, nullptr, nullptr);
+    int h = cell_axis(g, a, xi[a] + R, nullptr, nullptr);
+    lo[a] = max(l, max((bi[a] - 1) * g.s, 0));
+    hi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
+  }
+  for (int cz = lo[2]; cz <= hi[2]; cz++) {
+    const int bz = cz / g.s;
+    for (int cy = lo[1]; cy <= hi[1]; cy++) {
+      const int by = cy / g.s;
+      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      int cx = lo[0];
+      while (cx <= hi[0]) {
+        const int bx = cx / g.s;
+        const int e = min(hi[0], bx * g.s + g.s - 1);
+        const int code = (bx - bi[0] + 1) * 9 + (by - bi[1] + 1) * 3 + (bz - bi[2] + 1);
+        f(cs[rowbase + cx], cs[rowbase + e + 1], code);
+        cx = e + 1;
+      }
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void decode_offsets(const Geo& g, int code, bool& own, T& ox, T& oy, T& oz) {
+  own = (code == 13);
+  constexpr bool REL = sizeof(T) == 4;
+  const int dbx = code / 9 - 1, dby = (code / 3) % 3 - 1, dbz = code % 3 - 1;
+  ox = REL ? T(-dbx * g.del) : T(0);
+  oy = REL ? T(-dby * g.del) : T(0);
+  oz = REL ? T(-dbz * g.del) : T(0);
+}
+
+// union filter of the momentum, density and velocity sweeps
+template <typename T>
+__global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W, Packed K,
+                                                     const uint32_t* __restrict__ cs,
+                                                     const double* __restrict__ hmax,
+                                                     const int* __restrict__ d_count, NList L) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count) return;
+  if (!need_neigh(A.bc[i])) {
+    L.cnt[i] = 0;
+    return;
+  }
+  const double xi[3] = {A.x[i], A.y[i], A.z[i]};
+  const int b = A.bkt[i];
+  int bi[3];
+  bucket_coords<3>(g, b, bi);
+  T xs[3];
+  Pos<3, T>::load(A, W, i, xs);
+  const double hi_d = A.h[i];
+  const T hi = T(hi_d);
+  const T supp = T(o.cutoff2) * hi;
+  const T Lb = T(o.list_factor * W.hlist[i]);
+  const T kmarg = T(o.ksupport * (1.0 + 1e-6));
+  const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
+  uint2* out = L.e + (size_t)i * LCAP;
+  int cnt = 0;
+  for_segments_code<T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, int code) {
+    bool own;
+    T ox, oy, oz;
+    decode_offsets<T>(g, code, own, ox, oy, oz);
+    const T xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
+    for (uint32_t wb = j0; wb < j1; wb += 32) {
+      const int nb = (int)min(32u, j1 - wb);
+      uint32_t mask = 0;
+      for (int q = 0; q < nb; q++) {
+        T xj[3], hj;
+        JPos<T>::get(A, K, wb + q, xj, hj);
+        const T dx[3] = {xsh[0] - xj[0], xsh[1] - xj[1], xsh[2] - xj[2]};
+        if (!own && !in_box<3, T>(dx, Lb)) continue;
+        if (!in_box<3, T>(dx, supp)) continue;
+        const T hs = fmax(T(0.5) * (hi + fabs(hj)), hi);
+        if (in_box<3, T>(dx, kmarg * hs)) mask |= 1u << q;
+      }
+      if (mask) {
+        if (cnt < LCAP) out[cnt] = make_uint2(wb | ((uint32_t)code << 26), mask);
+        cnt++;
+      }
+    }
+  });
+  L.cnt[i] = (cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
+}
+
+// sweep over the lists (thread per particle, over the compacted need_neigh
+// indices); particles whose list overflowed walk their rows.  The window and
+// bit loops are flattened so that every iteration hands each thread exactly
+// one pair (threads of a warp stay converged while they have pairs left).
+template <typename T, template <typename> class SW>
+__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geo g, Dev A, Work W, Packed K,
+                                                     const uint32_t* __restrict__ cs,
+                                                     const double* __restrict__ hmax,
+                                                     const int* __restrict__ d_real,
+                                                     const uint32_t* __restrict__ real_idx, TimeState* ts,
+                                                     NList L) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *d_real) return;
+  const int i = (int)real_idx[r];
+  SW<T> s(A, K, o);
+  double xi[3], R;
+  int bi[3];
+  if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;
+  const uint16_t c = L.cnt[i];
+  if (c == NL_OVERFLOW) {
+    for_segments<3, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+      for (uint32_t j = j0; j < j1; j++) {
+        T dx[3];
+        if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+      }
+    });
+  } else if (c > 0) {
+    const uint2* ent = L.e + (size_t)i * LCAP;
+    int q = 0;
+    uint2 en = ent[0];
+    uint32_t mask = en.y;
+    bool own;
+    T ox, oy, oz;
+    decode_offsets<T>(g, (int)(en.x >> 26), own, ox, oy, oz);
+    while (true) {
+      if (mask == 0) {  // stored windows are never empty: one step suffices
+        if (++q >= c) break;
+        en = ent[q];
+        mask = en.y;
+        decode_offsets<T>(g, (int)(en.x >> 26), own, ox, oy, oz);
+      }
+      const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
+      mask &= mask - 1;
+      T dx[3];
+      if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+    }
+  }
+  s.template finish<false>(i, W, ts);
+}
+
+// compacted indices of the need_neigh particles (sorted order kept)
+__global__ void k_real_flags(Dev A, const int* __restrict__ d_count, int n, unsigned int* __restrict__ flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = (i < *d_count && need_neigh(A.bc[i])) ? 1u : 0u;
+}
+__global__ void k_real_scatter(const unsigned int* __restrict__ flag, const unsigned long long* __restrict__ offs,
+                               int n, uint32_t* __restrict__ real_idx, int* __restrict__ d_real,
+                               const unsigned long long* __restrict__ total) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *d_real = (int)*total;
+  if (i >= n) return;
+  if (flag[i]) real_idx[offs[i]] = (uint32_t)i;
+}
+
+// position records for the list build: P (xr, yr, zr, h)
+__global__ void k_pack_pos(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], (float)A.h[j]);
+}
+
 }  // namespace plume

@@ -148,7 +148,7 @@ class Solver:
     def phase_times(self):
         ms = (C.c_float * 11)()
         self._check(self.L.plume_phase_times(self.ctx, ms, 11), "plume_phase_times")
-        names = ["search", "adaptive", "hmax", "momentum", "commit_mom", "density", "commit_dens",
+        names = ["search", "adaptive", "lists", "momentum", "commit_mom", "density", "commit_dens",
                  "velocity", "position", "dt", "total"]
         return dict(zip(names, list(ms)))
 
