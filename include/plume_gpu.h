@@ -250,6 +250,25 @@ int plume_launch_count(plume_ctx *ctx, uint64_t *n);
  * NULL). */
 int plume_last_error(plume_ctx *ctx, char *buf, size_t len);
 
+/* Time step without allocating: dt_out[0] = cfl * min(h[i] / c[i]) over the
+ * particles with bc_type 100 or 99 (1.0e10 when there are none), from
+ * device arrays of n particles, on `stream` (a cudaStream_t; NULL = the
+ * default stream).  No counterpart in the reference: it is the dt reduction
+ * of plume_step offered to callers that cannot allocate GPU memory (hosts
+ * whose device memory belongs to their own pool, code paths where an
+ * allocation would synchronise the device).  Its scratch is a fixed device
+ * array of PLUME_NOALLOC_MAX_BLOCKS doubles that every GPU loading the
+ * library keeps until exit; n above PLUME_NOALLOC_MAX_BLOCKS *
+ * PLUME_NOALLOC_CHUNK returns PLUME_E_CAPACITY.  The first call on a device
+ * looks up that array's address; make it before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race.  A sound speed <= 0
+ * (or NaN) among those particles gives a NaN dt.  Asynchronous: read dt_out
+ * after synchronising the stream. */
+#define PLUME_NOALLOC_MAX_BLOCKS 1024
+#define PLUME_NOALLOC_CHUNK      16384
+int plume_timestep_noalloc(const double *h, const double *c, const uint8_t *bc_type,
+                           size_t n, double cfl, double *dt_out, void *stream);
+
 /* Library version string "major.minor.patch". */
 const char *plume_version(void);
 

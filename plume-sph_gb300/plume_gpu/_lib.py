@@ -36,7 +36,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not os.path.exists(nvcc) and os.path.exists("/usr/local/cuda/bin/nvcc"):
         nvcc = "/usr/local/cuda/bin/nvcc"
     tmp = LIBPATH + ".tmp"
-    cmd = [nvcc] + NVCC_FLAGS + ["-o", tmp, os.path.join(CSRC, "plume_gpu.cu")]
+    cmd = [nvcc] + NVCC_FLAGS + ["-o", tmp, os.path.join(CSRC, "plume_gpu.cu"),
+                                 os.path.join(CSRC, "timestep_noalloc.cu")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed:\n" + r.stderr[-4000:])
@@ -76,5 +77,7 @@ def lib():
         L.plume_launch_count.argtypes = [C.c_void_p, P(C.c_uint64)]
         L.plume_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
         L.plume_version.restype = C.c_char_p
+        L.plume_timestep_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                             C.c_double, C.c_void_p, C.c_void_p]
         _LIB = L
         return L
