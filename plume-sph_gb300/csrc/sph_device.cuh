@@ -104,14 +104,14 @@ __device__ __forceinline__ float w_gauss<3, float>(const float* s, float h) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
     if (fabsf(s[i]) > 3.0f) return 0.0f;
-  float r = float(T1_INV_SQRT_PI) / h;
+  float r = float(T1_INV_SQRT_PI) * __fdividef(1.0f, h);
   float expt = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
   return r * r * r * __expf(-expt);
 }
 template <>
 __device__ __forceinline__ float w_gauss<1, float>(const float* s, float h) {
   if (fabsf(s[0]) > 3.0f) return 0.0f;
-  return (float(T1_INV_SQRT_PI) / h) * __expf(-s[0] * s[0]);
+  return (float(T1_INV_SQRT_PI) * __fdividef(1.0f, h)) * __expf(-s[0] * s[0]);
 }
 // cubic B-spline, radial support 2h
 template <int D, typename T>

@@ -39,19 +39,20 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
     hi[a] = min(h, min(bh, g.G[a] - 1));
   }
   constexpr bool REL = sizeof(T) == 4;
+  const T delT = T(g.del);
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
     int bz = cz / g.s;
-    T oz = REL ? T((bi[2] - bz) * g.del) : T(0);
+    T oz = REL ? T(bi[2] - bz) * delT : T(0);
     for (int cy = lo[1]; cy <= hi[1]; cy++) {
       int by = cy / g.s;
-      T oy = REL ? T((bi[1] - by) * g.del) : T(0);
+      T oy = REL ? T(bi[1] - by) * delT : T(0);
       size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
       int cx = lo[0];
       while (cx <= hi[0]) {
         int bx = cx / g.s;
         int e = min(hi[0], bx * g.s + g.s - 1);
         bool own = (bx == bi[0]) && (by == bi[1]) && (bz == bi[2]);
-        f(cs[rowbase + cx], cs[rowbase + e + 1], own, REL ? T((bi[0] - bx) * g.del) : T(0), oy, oz);
+        f(cs[rowbase + cx], cs[rowbase + e + 1], own, REL ? T(bi[0] - bx) * delT : T(0), oy, oz);
         cx = e + 1;
       }
     }

@@ -41,14 +41,14 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <typename T>
 struct WBuf {
   int j[64];
-  T dx[3][64];
+  T dx[4][64];  // dx and h_j of the compacted pairs
 };
 
 // fast reciprocal for the mixed path, exact division for FP64
 template <typename T>
 __device__ __forceinline__ T rcp(T x) { return T(1) / x; }
 template <>
-__device__ __forceinline__ float rcp<float>(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ float rcp<float>(float x) { return __fdividef(1.0f, x); }
 
 // Walks the candidates of particle i (warp-uniform arguments) and calls
 // s.math(j, dx) for every survivor of s.filter(j, own, ox, oy, oz, dx).
@@ -67,12 +67,13 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
     hi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
   }
   constexpr bool REL = sizeof(T) == 4;
+  const T delT = T(g.del);
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
     const int bz = cz / g.s;
-    const T oz = REL ? T((bi[2] - bz) * g.del) : T(0);
+    const T oz = REL ? T(bi[2] - bz) * delT : T(0);
     for (int cy = lo[1]; cy <= hi[1]; cy++) {
       const int by = cy / g.s;
-      const T oy = REL ? T((bi[1] - by) * g.del) : T(0);
+      const T oy = REL ? T(bi[1] - by) * delT : T(0);
       const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
       int cx = lo[0];
       while (cx <= hi[0]) {
@@ -81,11 +82,11 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
         const uint32_t j0 = cs[rowbase + cx];
         const uint32_t j1 = cs[rowbase + e + 1];
         const bool own = (bx == bi[0]) && (by == bi[1]) && (bz == bi[2]);
-        const T ox = REL ? T((bi[0] - bx) * g.del) : T(0);
+        const T ox = REL ? T(bi[0] - bx) * delT : T(0);
         for (uint32_t jb = j0; jb < j1; jb += 32) {
           const uint32_t j = jb + lane;
-          T dx[3];
-          const bool take = (j < j1) && s.filter(j, own, ox, oy, oz, dx);
+          T dx[3], hj;
+          const bool take = (j < j1) && s.filter(j, own, ox, oy, oz, dx, hj);
           const unsigned m = __ballot_sync(WFULL, take);
           if (take) {
             const int slot = count + __popc(m & lt);
@@ -93,12 +94,13 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
             B.dx[0][slot] = dx[0];
             B.dx[1][slot] = dx[1];
             B.dx[2][slot] = dx[2];
+            B.dx[3][slot] = hj;
           }
           count += __popc(m);
           __syncwarp();
           if (count >= 32) {
             T d[3] = {B.dx[0][lane], B.dx[1][lane], B.dx[2][lane]};
-            s.math(B.j[lane], d);
+            s.math(B.j[lane], d, B.dx[3][lane]);
             __syncwarp();
             const int rest = count - 32;
             if (lane < rest) {
@@ -106,6 +108,7 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
               B.dx[0][lane] = B.dx[0][lane + 32];
               B.dx[1][lane] = B.dx[1][lane + 32];
               B.dx[2][lane] = B.dx[2][lane + 32];
+              B.dx[3][lane] = B.dx[3][lane + 32];
             }
             count = rest;
             __syncwarp();
@@ -117,7 +120,7 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
   }
   if (lane < count) {
     T d[3] = {B.dx[0][lane], B.dx[1][lane], B.dx[2][lane]};
-    s.math(B.j[lane], d);
+    s.math(B.j[lane], d, B.dx[3][lane]);
   }
   __syncwarp();
 }
@@ -151,6 +154,7 @@ struct WMom {
   bool lans;
   uint32_t i;
   T xs[3], hi, supp, Lb, rhoi, Vi, pvsqi, ci, tempi, Cp_i, veli[3];
+  T ks_half, ata, alpha, beta;  // option constants in the sweep's type
   Acc<T> rv[3], re;
   __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   // i-side set-up; returns false (with the status set) when i is skipped
@@ -183,6 +187,10 @@ struct WMom {
       veli[0] = T(A.vx[ii]); veli[1] = T(A.vy[ii]); veli[2] = T(A.vz[ii]);
     }
     R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hmax[b])) * (1.0 + 1e-10);
+    ks_half = T(o.ksupport * 0.5 * (1.0 + 1e-6));
+    ata = T(o.ata);
+    alpha = T(o.alpha);
+    beta = T(o.beta);
     return true;
   }
   template <bool WARP>
@@ -202,23 +210,24 @@ struct WMom {
     W.nv2[ii] = unew2;
     W.ne[ii] = A.e[ii] + dt * (e + (double)veli[2] * grav);
   }
-  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& hj) const {
     if (j == i) return false;
-    T xj[3], hj;
+    T xj[3];
     JPos<T>::get(A, K, j, xj, hj);
     dx[0] = (xs[0] + ox) - xj[0];
     dx[1] = (xs[1] + oy) - xj[1];
     dx[2] = (xs[2] + oz) - xj[2];
     if (!own && !in_box<3, T>(dx, Lb)) return false;
     if (!in_box<3, T>(dx, supp)) return false;
-    const T ks = T(o.ksupport * 0.5 * (1.0 + 1e-6)) * (hi + fabs(hj));
+    const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
-  __device__ __forceinline__ void load_j(uint32_t j, T& hj, T& mj, T& rhoj, T& pj, T& cj, T& Tj, T& cpj,
+  // j-side fields; pVVj = p_j V_j V_j, the reference's pressj * Vj * Vj
+  __device__ __forceinline__ void load_j(uint32_t j, T& mj, T& rhoj, T& Vj, T& pVVj, T& cj, T& Tj, T& cpj,
                                          T* vj) const;
-  __device__ __forceinline__ void math(uint32_t j, const T* dx) {
-    T hj, mj, rhoj, pressj, cj, Tj, cpj, vj[3];
-    load_j(j, hj, mj, rhoj, pressj, cj, Tj, cpj, vj);
+  __device__ __forceinline__ void math(uint32_t j, const T* dx, T hj) {
+    T mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj[3];
+    load_j(j, mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj);
     const T h = T(0.5) * (hi + hj);
     const T ih = rcp<T>(h);
     T si[3], dist_sq = 0;
@@ -227,26 +236,25 @@ struct WMom {
       si[k] = (sizeof(T) == 8) ? dx[k] / h : dx[k] * ih;
       dist_sq += dx[k] * dx[k];
     }
-    const T Vj = rcp<T>(rhoj);
     T velij[3] = {veli[0] - vj[0], veli[1] - vj[1], veli[2] - vj[2]};
     const T rhoab = T(0.5) * (rhoi + rhoj);
     const T sndspdab = T(0.5) * (ci + cj);
     T vrab = 0;
 #pragma unroll
     for (int k = 0; k < 3; k++) vrab += dx[k] * velij[k];
-    const T miuab = (sizeof(T) == 8) ? h * vrab / (dist_sq + T(o.ata) * h * h)
-                                     : h * vrab * rcp<T>(dist_sq + T(o.ata) * h * h);
+    const T miuab = (sizeof(T) == 8) ? h * vrab / (dist_sq + ata * h * h)
+                                     : h * vrab * rcp<T>(dist_sq + ata * h * h);
     T vis = 0;
     if (vrab < 0)
-      vis = (sizeof(T) == 8) ? (T(o.beta) * miuab - T(o.alpha) * sndspdab) * miuab / rhoab
-                             : (T(o.beta) * miuab - T(o.alpha) * sndspdab) * miuab * rcp<T>(rhoab);
+      vis = (sizeof(T) == 8) ? (beta * miuab - alpha * sndspdab) * miuab / rhoab
+                             : (beta * miuab - alpha * sndspdab) * miuab * rcp<T>(rhoab);
     T dotv = 0;
     if (lans) {
 #pragma unroll
       for (int k = 0; k < 3; k++) dotv += velij[k] * velij[k];
       vis -= T(EPS_HALF) * dotv * Vj;
     }
-    const T mpvsqij = mj * (pressj * Vj * Vj + pvsqi + vis);
+    const T mpvsqij = mj * (pVVj + pvsqi + vis);
     T dwdx[3];
     if (sizeof(T) == 8 || o.kernel == 1) {
       kdw<3, T>(o.kernel, si, h, dwdx);
@@ -288,10 +296,12 @@ struct WMom {
   }
 };
 template <>
-__device__ __forceinline__ void WMom<double>::load_j(uint32_t j, double& hj, double& mj, double& rhoj,
-                                                     double& pj, double& cj, double& Tj, double& cpj,
+__device__ __forceinline__ void WMom<double>::load_j(uint32_t j, double& mj, double& rhoj, double& Vj,
+                                                     double& pVVj, double& cj, double& Tj, double& cpj,
                                                      double* vj) const {
-  hj = A.h[j]; mj = A.mass[j]; rhoj = A.rho[j]; pj = A.p[j]; cj = A.c[j]; Tj = A.T[j]; cpj = A.cp[j];
+  mj = A.mass[j]; rhoj = A.rho[j]; cj = A.c[j]; Tj = A.T[j]; cpj = A.cp[j];
+  Vj = 1.0 / rhoj;
+  pVVj = A.p[j] * Vj * Vj;
   if (lans) {
     vj[0] = A.vsx[j]; vj[1] = A.vsy[j]; vj[2] = A.vsz[j];
   } else {
@@ -299,28 +309,27 @@ __device__ __forceinline__ void WMom<double>::load_j(uint32_t j, double& hj, dou
   }
 }
 template <>
-__device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& hj, float& mj, float& rhoj, float& pj,
+__device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& mj, float& rhoj, float& Vj, float& pVVj,
                                                     float& cj, float& Tj, float& cpj, float* vj) const {
-  const float4 p = K.P[j], q = K.Q[j], r = K.R[j], s = K.S[j];
-  hj = fabsf(p.w);
-  mj = q.x; rhoj = q.y; pj = q.z; cj = q.w;
-  Tj = r.x; cpj = r.y; vj[0] = r.z; vj[1] = r.w;
-  vj[2] = s.x;
+  const float4 q = K.Q[j], r = K.R[j], s = K.S[j];
+  mj = q.x; rhoj = q.y; Vj = q.z; pVVj = q.w;
+  cj = r.x; Tj = r.y; cpj = r.z; vj[0] = r.w;
+  vj[1] = s.x; vj[2] = s.y;
 }
 
-// momentum record: P (xr,yr,zr,h), Q (m,rho,p,c), R (T,cp,vx,vy), S (vz)
+// momentum record: P (xr,yr,zr,h), Q (m, rho, 1/rho, p/rho^2), R (c,T,cp,vx),
+// S (vy,vz); the quotients are formed in FP64 once per particle
 __global__ void k_pack_mom(Geo g, Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
+  const double rho = A.rho[j], V = 1.0 / rho;
   K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], (float)A.h[j]);
-  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.p[j], (float)A.c[j]);
-  if (lans) {
-    K.R[j] = make_float4((float)A.T[j], (float)A.cp[j], (float)A.vsx[j], (float)A.vsy[j]);
-    K.S[j] = make_float4((float)A.vsz[j], 0.f, 0.f, 0.f);
-  } else {
-    K.R[j] = make_float4((float)A.T[j], (float)A.cp[j], (float)A.vx[j], (float)A.vy[j]);
-    K.S[j] = make_float4((float)A.vz[j], 0.f, 0.f, 0.f);
-  }
+  K.Q[j] = make_float4((float)A.mass[j], (float)rho, (float)V, (float)(A.p[j] * V * V));
+  const double vx = lans ? A.vsx[j] : A.vx[j];
+  const double vy = lans ? A.vsy[j] : A.vy[j];
+  const double vz = lans ? A.vsz[j] : A.vz[j];
+  K.R[j] = make_float4((float)A.c[j], (float)A.T[j], (float)A.cp[j], (float)vx);
+  K.S[j] = make_float4((float)vy, (float)vz, 0.f, 0.f);
 }
 
 // ------------------------------------------------------------ density
@@ -330,7 +339,7 @@ struct WDens {
   const Packed& K;
   const Opt& o;
   int pgc;
-  T xs[3], hi, supp, Lb;
+  T xs[3], hi, supp, Lb, ks_half;
   Acc<T> rho1, rho2, wnorm_e, engr;
   bool esm;
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
@@ -347,6 +356,7 @@ struct WDens {
     supp = T(o.cutoff2) * hi;
     Lb = T(o.list_factor * W.hlist[ii]);
     R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hmax[b])) * (1.0 + 1e-10);
+    ks_half = T(o.ksupport * 0.5 * (1.0 + 1e-6));
     return true;
   }
   template <bool WARP>
@@ -374,8 +384,8 @@ struct WDens {
     W.nrho[ii] = density;
     W.nY[ii] = r2 / density;
   }
-  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
-    T xj[3], hj;
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& hj) const {
+    T xj[3];
     JPos<T>::get(A, K, j, xj, hj);
     if (sizeof(T) == 8) {
       const uint8_t ph = A.phase[j];
@@ -388,16 +398,18 @@ struct WDens {
     dx[2] = (xs[2] + oz) - xj[2];
     if (!own && !in_box<3, T>(dx, Lb)) return false;
     if (!in_box<3, T>(dx, supp)) return false;
-    const T ks = T(o.ksupport * 0.5 * (1.0 + 1e-6)) * (hi + fabs(hj));
+    const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
-  __device__ __forceinline__ void math(uint32_t j, const T* ds) {
-    T hj, mj, rhoj, ej, ph;
-    if (sizeof(T) == 8) {
-      hj = T(A.h[j]); mj = T(A.mass[j]); rhoj = T(A.rho[j]); ej = T(A.e[j]); ph = T(A.phase[j]);
+  __device__ __forceinline__ void math(uint32_t j, const T* ds, T hj) {
+    // FP64: the reference's fields; mixed: (m, m/rho, m e/rho, phase)
+    T mj, rhoj = 0, ej = 0, mvr = 0, mer = 0, ph;
+    if constexpr (sizeof(T) == 8) {
+      mj = A.mass[j]; rhoj = A.rho[j]; ej = A.e[j]; ph = T(A.phase[j]);
     } else {
-      const float4 p = K.P[j], q = K.Q[j];
-      hj = T(p.w); mj = T(q.x); rhoj = T(q.y); ej = T(q.z); ph = T(q.w);
+      const float4 q = K.Q[j];
+      mj = q.x; mvr = q.y; mer = q.z; ph = q.w;
+      hj = fabsf(hj);
     }
     const T hh = T(0.5) * (hi + hj);
     T sv[3];
@@ -408,10 +420,15 @@ struct WDens {
       T s_e[3];
 #pragma unroll
       for (int k = 0; k < 3; k++) s_e[k] = (sizeof(T) == 8) ? T(E_SMOOTH) * ds[k] / hh : T(E_SMOOTH) * ds[k] * ih;
-      const T wm_e = kw<3, T>(o.kernel, s_e, (sizeof(T) == 8) ? hh / T(E_SMOOTH) : hh * T(0.25)) * mj;
-      const T irho = rcp<T>(rhoj);
-      wnorm_e.add((sizeof(T) == 8) ? wm_e / rhoj : wm_e * irho);
-      engr.add((sizeof(T) == 8) ? wm_e * ej / rhoj : wm_e * ej * irho);
+      if constexpr (sizeof(T) == 8) {
+        const T wm_e = kw<3, T>(o.kernel, s_e, hh / T(E_SMOOTH)) * mj;
+        wnorm_e.add(wm_e / rhoj);
+        engr.add(wm_e * ej / rhoj);
+      } else {
+        const T w_e = kw<3, T>(o.kernel, s_e, hh * T(0.25));
+        wnorm_e.add(w_e * mvr);
+        engr.add(w_e * mer);
+      }
     }
     const T wm = kw<3, T>(o.kernel, sv, hh) * mj;
     if (ph == T(1))
@@ -421,15 +438,17 @@ struct WDens {
   }
 };
 
-// density record: P (xr,yr,zr,+-h: - when not contributing), Q (m,rho,e,phase)
+// density record: P (xr,yr,zr,+-h: - when not contributing),
+// Q (m, m/rho, m e/rho, phase)
 __global__ void k_pack_dens(Dev A, Packed K, Work W, int pgc, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
   const uint8_t ph = A.phase[j];
   const bool c = contr_dens(A.bc[j], pgc) && (ph == 1 || ph == 2);
   const float h = (float)A.h[j];
+  const double m = A.mass[j], mr = m / A.rho[j];
   K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], c ? h : -h);
-  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.e[j], (float)ph);
+  K.Q[j] = make_float4((float)m, (float)mr, (float)(mr * A.e[j]), (float)ph);
 }
 
 // ------------------------------------------------------------ velocity
@@ -473,8 +492,8 @@ struct WVel {
     A.vsy[ii] = vi_d[1] + d1 / wn;
     A.vsz[ii] = vi_d[2] + d2 / wn;
   }
-  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx) const {
-    T xj[3], flag;
+  __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& flag) const {
+    T xj[3];
     JPos<T>::get(A, K, j, xj, flag);
     if (sizeof(T) == 8) {
       if (!contr_vel_smooth(A.bc[j])) return false;
@@ -488,34 +507,35 @@ struct WVel {
     if (!in_box<3, T>(dx, supp)) return false;
     return in_box<3, T>(dx, ks);
   }
-  __device__ __forceinline__ void math(uint32_t j, const T* ds) {
-    T mj, rhoj, vj[3];
-    if (sizeof(T) == 8) {
-      mj = T(A.mass[j]); rhoj = T(A.rho[j]);
-      vj[0] = T(A.vx[j]); vj[1] = T(A.vy[j]); vj[2] = T(A.vz[j]);
+  __device__ __forceinline__ void math(uint32_t j, const T* ds, T) {
+    // FP64: the reference's fields; mixed: (m/rho, vx, vy, vz)
+    T mj = 0, rhoj = 0, mvr = 0, vj[3];
+    if constexpr (sizeof(T) == 8) {
+      mj = A.mass[j]; rhoj = A.rho[j];
+      vj[0] = A.vx[j]; vj[1] = A.vy[j]; vj[2] = A.vz[j];
     } else {
-      const float4 q = K.Q[j], r = K.R[j];
-      mj = T(q.x); rhoj = T(q.y); vj[0] = T(q.z); vj[1] = T(q.w); vj[2] = T(r.x);
+      const float4 q = K.Q[j];
+      mvr = q.x; vj[0] = q.y; vj[1] = q.z; vj[2] = q.w;
     }
     T sv[3];
     const T ih = rcp<T>(hi);
 #pragma unroll
     for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hi : ds[k] * ih;
     const T wght = kw<3, T>(o.kernel, sv, hi);
-    const T mvw = (sizeof(T) == 8) ? wght * mj / rhoj : wght * mj * rcp<T>(rhoj);
+    const T mvw = (sizeof(T) == 8) ? wght * mj / rhoj : wght * mvr;
 #pragma unroll
     for (int k = 0; k < 3; k++) dv[k].add(mvw * (vj[k] - vi[k]));
     wnorm.add(mvw);
   }
 };
 
-// velocity record: P (xr,yr,zr,+-1: - when not contributing), Q (m,rho,vx,vy), R (vz)
+// velocity record: P (xr,yr,zr,+-1: - when not contributing),
+// Q (m/rho, vx, vy, vz)
 __global__ void k_pack_vel(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
   K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], contr_vel_smooth(A.bc[j]) ? 1.f : -1.f);
-  K.Q[j] = make_float4((float)A.mass[j], (float)A.rho[j], (float)A.vx[j], (float)A.vy[j]);
-  K.R[j] = make_float4((float)A.vz[j], 0.f, 0.f, 0.f);
+  K.Q[j] = make_float4((float)(A.mass[j] / A.rho[j]), (float)A.vx[j], (float)A.vy[j], (float)A.vz[j]);
 }
 
 
@@ -550,8 +570,8 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Pac
     if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;
     for_segments<3, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
       for (uint32_t j = j0; j < j1; j++) {
-        T dx[3];
-        if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+        T dx[3], hj;
+        if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
       }
     });
     s.template finish<false>(i, W, ts);
@@ -608,14 +628,16 @@ __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* 
   }
 }
 
+// delT: the bucket edge in the sweep's type, formed once per particle (the
+// FP64 pipe of sm_103a is narrow: no double arithmetic per window)
 template <typename T>
-__device__ __forceinline__ void decode_offsets(const Geo& g, int code, bool& own, T& ox, T& oy, T& oz) {
+__device__ __forceinline__ void decode_offsets(T delT, int code, bool& own, T& ox, T& oy, T& oz) {
   own = (code == 13);
   constexpr bool REL = sizeof(T) == 4;
   const int dbx = code / 9 - 1, dby = (code / 3) % 3 - 1, dbz = code % 3 - 1;
-  ox = REL ? T(-dbx * g.del) : T(0);
-  oy = REL ? T(-dby * g.del) : T(0);
-  oz = REL ? T(-dbz * g.del) : T(0);
+  ox = REL ? T(-dbx) * delT : T(0);
+  oy = REL ? T(-dby) * delT : T(0);
+  oz = REL ? T(-dbz) * delT : T(0);
 }
 
 // union filter of the momentum, density and velocity sweeps
@@ -643,11 +665,12 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W
   const T kmarg = T(o.ksupport * (1.0 + 1e-6));
   const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
   uint2* out = L.e + (size_t)i * LCAP;
+  const T delT = T(g.del);
   int cnt = 0;
   for_segments_code<T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, int code) {
     bool own;
     T ox, oy, oz;
-    decode_offsets<T>(g, code, own, ox, oy, oz);
+    decode_offsets<T>(delT, code, own, ox, oy, oz);
     const T xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
     for (uint32_t wb = j0; wb < j1; wb += 32) {
       const int nb = (int)min(32u, j1 - wb);
@@ -692,29 +715,30 @@ __global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geo g, Dev A, Work W
   if (c == NL_OVERFLOW) {
     for_segments<3, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
       for (uint32_t j = j0; j < j1; j++) {
-        T dx[3];
-        if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+        T dx[3], hj;
+        if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
       }
     });
   } else if (c > 0) {
     const uint2* ent = L.e + (size_t)i * LCAP;
+    const T delT = T(g.del);
     int q = 0;
     uint2 en = ent[0];
     uint32_t mask = en.y;
     bool own;
     T ox, oy, oz;
-    decode_offsets<T>(g, (int)(en.x >> 26), own, ox, oy, oz);
+    decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
     while (true) {
       if (mask == 0) {  // stored windows are never empty: one step suffices
         if (++q >= c) break;
         en = ent[q];
         mask = en.y;
-        decode_offsets<T>(g, (int)(en.x >> 26), own, ox, oy, oz);
+        decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
       }
       const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
       mask &= mask - 1;
-      T dx[3];
-      if (s.filter(j, own, ox, oy, oz, dx)) s.math(j, dx);
+      T dx[3], hj;
+      if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
     }
   }
   s.template finish<false>(i, W, ts);
