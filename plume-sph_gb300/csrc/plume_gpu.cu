@@ -150,7 +150,8 @@ __global__ void k_gather(Geo g, Dev A, Dev B, Work W, const uint32_t* __restrict
   B.inv[p] = A.inv[q];
   int b = A.bkt[q];
   B.bkt[p] = b;
-  if (mixed) {
+  (void)mixed;  // bucket-relative coordinates serve both paths (cell ranges)
+  {
     int bi[3];
     if (g.dim == 3) {
       bi[0] = b % g.nb[0];
@@ -165,18 +166,20 @@ __global__ void k_gather(Geo g, Dev A, Dev B, Work W, const uint32_t* __restrict
   }
 }
 
-// cell_start[c] = first sorted index with key >= c, c in [0, ncells + 1]
+// cell_start[c] = first sorted index with key >= c, c in [0, ncells + 1]:
+// one thread per cell, binary search over the sorted keys (long runs of
+// empty cells above and below the particles cost nothing extra)
 __global__ void k_cell_start(const uint32_t* __restrict__ skeys, int n, uint32_t ncells,
                              uint32_t* __restrict__ cs, int* d_count) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p > n) return;
-  long long kp = (p < n) ? (long long)skeys[p] : (long long)ncells + 1;
-  long long kprev = (p == 0) ? -1 : (long long)skeys[p - 1];
-  if (kp > (long long)ncells + 1) kp = ncells + 1;
-  for (long long c = kprev + 1; c <= kp; c++) {
-    cs[c] = (uint32_t)p;
-    if (c == (long long)ncells) *d_count = p;
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c > (long long)ncells + 1) return;
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)skeys[mid] < c) lo = mid + 1; else hi = mid;
   }
+  cs[c] = (uint32_t)lo;
+  if (c == (long long)ncells) *d_count = lo;
 }
 
 __global__ void k_fill_cs(uint32_t* cs, uint32_t ncells, int* d_count) {
@@ -467,7 +470,7 @@ static int search(plume_ctx* ctx) {
   k_gather<<<nblocks(n), NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->B, ctx->W, ctx->perm, n,
                                             ctx->opt.precision == PLUME_PREC_MIXED);
   std::swap(ctx->A, ctx->B);
-  k_cell_start<<<nblocks((size_t)n + 1), NTHREADS, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
+  k_cell_start<<<nblocks((size_t)ctx->ncells + 2, 256), 256, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
   ctx->launches += 2;
   ctx->pending_dead = false;
   CK(cudaGetLastError());
@@ -677,6 +680,8 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
   g.del = grid->del;
   g.s = s;
   g.cw = grid->del / s;
+  g.idel = 1.0 / g.del;
+  g.icw = 1.0 / g.cw;
   g.dim = opt->dim;
   for (int a = 0; a < 3; a++) g.G[a] = (opt->dim == 3 || a == 0) ? g.nb[a] * s : 1;
   ctx->ncells = (uint32_t)((size_t)g.G[0] * g.G[1] * g.G[2]);

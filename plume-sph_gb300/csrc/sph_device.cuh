@@ -43,6 +43,7 @@ struct Geo {
   double mind[3];
   double del;
   double cw;  // fine cell edge = del / s
+  double idel, icw;  // 1/del, 1/cw (multiplies instead of FP64 divisions)
   int nb[3];
   int s;
   int G[3];   // fine cells per axis = nb * s
@@ -215,8 +216,11 @@ __device__ __forceinline__ void eos(const Opt& o, double rho, double Y, double e
 // ---------------------------------------------------------------- grid
 // bucket index per axis with the comparisons of Bucket::contains
 // (bucket.h:238-245) against mind + b*del; clamped into [0, nb-1]
-__device__ __forceinline__ int bucket_axis(double x, double mind, double del, int nb, bool* outside) {
-  double f = floor((x - mind) / del);
+__device__ __forceinline__ int bucket_axis(double x, double mind, double del, double idel, int nb,
+                                           bool* outside) {
+  // first guess by a multiply (the FP64 pipe of sm_103a is narrow), then the
+  // exact comparisons of Bucket::contains decide
+  double f = floor((x - mind) * idel);
   int b;
   if (!(f > -1.0)) {
     b = 0;
@@ -232,10 +236,10 @@ __device__ __forceinline__ int bucket_axis(double x, double mind, double del, in
 }
 // fine cell per axis: bucket * s + clamped sub-cell (monotone in x)
 __device__ __forceinline__ int cell_axis(const Geo& g, int a, double x, int* bucket, bool* outside) {
-  int b = bucket_axis(x, g.mind[a], g.del, g.nb[a], outside);
+  int b = bucket_axis(x, g.mind[a], g.del, g.idel, g.nb[a], outside);
   if (bucket) *bucket = b;
   double off = x - (g.mind[a] + b * g.del);
-  double f = floor(off / g.cw);
+  double f = floor(off * g.icw);
   int sub = (f > 0.0) ? (int)fmin(f, (double)(g.s - 1)) : 0;
   return b * g.s + sub;
 }

@@ -16,6 +16,22 @@
 namespace plume {
 
 // ---------------------------------------------------------------- segments
+// Conservative fine-cell range of [x - R, x + R] on axis a, from the
+// particle's bucket index and its FP32 bucket-relative coordinate: every
+// cell holding a particle within R is inside the range (the margin covers
+// FP32 rounding; exact tests follow in the sweeps), clipped to the 27
+// buckets around the particle's bucket and to the grid.  Keeps the range
+// arithmetic off the FP64 pipe.
+__device__ __forceinline__ void cell_range(const Geo& g, int a, int b, float xr, double R, int& lo, int& hi) {
+  const float cwf = (float)g.cw;
+  const float icw = 1.0f / cwf;
+  const float Rf = (float)R * 1.00001f + 1.0e-3f * cwf;
+  const int l = b * g.s + (int)floorf((xr - Rf) * icw);
+  const int h = b * g.s + (int)floorf((xr + Rf) * icw);
+  lo = max(l, max((b - 1) * g.s, 0));
+  hi = min(h, min((b + 2) * g.s - 1, g.G[a] - 1));
+}
+
 // Offsets (i's bucket - segment's bucket) * del are passed for the
 // bucket-relative FP32 coordinates of the mixed path; the FP64 path works on
 // absolute coordinates and gets zero offsets.
@@ -529,9 +545,9 @@ __global__ void k_update_pos(Opt o, Geo g, Dev A, const uint8_t* __restrict__ bf
     }
   }
   bool out = false, o1, o2, o3;
-  int bx = bucket_axis(pos[0], g.mind[0], g.del, g.nb[0], &o1);
-  int by = bucket_axis(pos[1], g.mind[1], g.del, g.nb[1], &o2);
-  int bz = bucket_axis(pos[2], g.mind[2], g.del, g.nb[2], &o3);
+  int bx = bucket_axis(pos[0], g.mind[0], g.del, g.idel, g.nb[0], &o1);
+  int by = bucket_axis(pos[1], g.mind[1], g.del, g.idel, g.nb[1], &o2);
+  int bz = bucket_axis(pos[2], g.mind[2], g.del, g.idel, g.nb[2], &o3);
   out = o1 || o2 || o3;
   if (out) {
     set_status(ts, 6);

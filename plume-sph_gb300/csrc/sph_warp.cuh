@@ -602,15 +602,10 @@ struct NList {
 // (dbx+1)*9 + (dby+1)*3 + (dbz+1), db = segment bucket - own bucket
 template <typename T, class F>
 __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* __restrict__ cs,
-                                                  const double* xi, const int* bi, double R, F&& f) {
+                                                  const float* xr, const int* bi, double R, F&& f) {
   int lo[3], hi[3];
 #pragma unroll
-  for (int a = 0; a < 3; a++) {
-    int l = cell_axis(g, a, xi[a] - R, nullptr, nullptr);
-    int h = cell_axis(g, a, xi[a] + R, nullptr, nullptr);
-    lo[a] = max(l, max((bi[a] - 1) * g.s, 0));
-    hi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
-  }
+  for (int a = 0; a < 3; a++) cell_range(g, a, bi[a], xr[a], R, lo[a], hi[a]);
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
     const int bz = cz / g.s;
     for (int cy = lo[1]; cy <= hi[1]; cy++) {
@@ -652,7 +647,6 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W
     L.cnt[i] = 0;
     return;
   }
-  const double xi[3] = {A.x[i], A.y[i], A.z[i]};
   const int b = A.bkt[i];
   int bi[3];
   bucket_coords<3>(g, b, bi);
@@ -666,8 +660,9 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W
   const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
   uint2* out = L.e + (size_t)i * LCAP;
   const T delT = T(g.del);
+  const float xrf[3] = {W.xr[i], W.yr[i], W.zr[i]};
   int cnt = 0;
-  for_segments_code<T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, int code) {
+  for_segments_code<T>(g, cs, xrf, bi, R, [&](uint32_t j0, uint32_t j1, int code) {
     bool own;
     T ox, oy, oz;
     decode_offsets<T>(delT, code, own, ox, oy, oz);
@@ -675,14 +670,33 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W
     for (uint32_t wb = j0; wb < j1; wb += 32) {
       const int nb = (int)min(32u, j1 - wb);
       uint32_t mask = 0;
-      for (int q = 0; q < nb; q++) {
-        T xj[3], hj;
-        JPos<T>::get(A, K, wb + q, xj, hj);
-        const T dx[3] = {xsh[0] - xj[0], xsh[1] - xj[1], xsh[2] - xj[2]};
-        if (!own && !in_box<3, T>(dx, Lb)) continue;
-        if (!in_box<3, T>(dx, supp)) continue;
-        const T hs = fmax(T(0.5) * (hi + fabs(hj)), hi);
-        if (in_box<3, T>(dx, kmarg * hs)) mask |= 1u << q;
+      if constexpr (sizeof(T) == 4) {
+        // branch-free tests, record loads issued 4 at a time
+        for (int q = 0; q < nb; q += 4) {
+          float4 pr[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            pr[u] = (q + u < nb) ? K.P[wb + q + u] : make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const float dx0 = fabsf(xsh[0] - pr[u].x), dx1 = fabsf(xsh[1] - pr[u].y), dx2 = fabsf(xsh[2] - pr[u].z);
+            const float m = fmaxf(dx0, fmaxf(dx1, dx2));
+            const float hs = fmaxf(0.5f * (hi + fabsf(pr[u].w)), hi);
+            const bool pass = (own || m <= Lb) && (m <= supp) && (m <= kmarg * hs);
+            mask |= (uint32_t)pass << (q + u);
+          }
+        }
+        mask &= (nb == 32) ? 0xffffffffu : ((1u << nb) - 1u);
+      } else {
+        for (int q = 0; q < nb; q++) {
+          T xj[3], hj;
+          JPos<T>::get(A, K, wb + q, xj, hj);
+          const T dx[3] = {xsh[0] - xj[0], xsh[1] - xj[1], xsh[2] - xj[2]};
+          if (!own && !in_box<3, T>(dx, Lb)) continue;
+          if (!in_box<3, T>(dx, supp)) continue;
+          const T hs = fmax(T(0.5) * (hi + fabs(hj)), hi);
+          if (in_box<3, T>(dx, kmarg * hs)) mask |= 1u << q;
+        }
       }
       if (mask) {
         if (cnt < LCAP) out[cnt] = make_uint2(wb | ((uint32_t)code << 26), mask);
