@@ -53,6 +53,9 @@ MOM_BYTES_WRITE = 4 * 8
 # algorithmic FLOPs of one in-support pair of the momentum sweep (3D with
 # LANS and heat terms): 80 FLOP + 2 SFU
 MOM_FLOP_PER_PAIR = 80
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the
+# momentum sweep on the small plume (253.3 MB for 778,952 particles)
+MOM_DRAM_BYTES_PER_PARTICLE = 253.3e6 / 778952
 
 
 def load_peaks():
@@ -270,7 +273,8 @@ def main():
     # dominant kernel: momentum sweep
     peak_hbm, peak_kind = load_peaks()
     nt, _ = sol.count()
-    mom_ms = phases["momentum"] / args.steps
+    # the momentum pair-sweep kernel alone (CUDA events around its launch)
+    mom_ms = phases["mom_kernel"] / args.steps
     alg_bytes = nt * MOM_BYTES_READ + n_real * MOM_BYTES_WRITE
     achieved_gbs = alg_bytes / (mom_ms / 1000.0) / 1e9
     npairs = None
@@ -285,12 +289,9 @@ def main():
     fp32_tflops = (npairs * MOM_FLOP_PER_PAIR / (mom_ms / 1000.0) / 1e12) if npairs else None
     sm_max = 2070.0
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FFMA lanes x 2 FLOP x clock
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "momentum_traffic.json")
-    if os.path.exists(tfile):
-        tj = json.load(open(tfile))
-        # DRAM bytes per particle of a captured small case, scaled by particles
-        traffic = tj.get("dram_bytes_per_particle", 0) * nt if tj.get("dram_bytes_per_particle") else None
+    # DRAM bytes of one launch: ncu's dram__bytes_read.sum + write.sum per
+    # particle on the small plume, scaled by the particles of this workload
+    traffic = MOM_DRAM_BYTES_PER_PARTICLE * nt
 
     # e2e: through the C ABI with pinned host buffers, every step
     # upload -> step -> download
@@ -364,7 +365,7 @@ def main():
             "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_hbm,
                          "unit": "GB/s", "frac": achieved_gbs / peak_hbm, "traffic": traffic,
-                         "kernel": "k_momentum<3,float>", "peak_kind": peak_kind,
+                         "kernel": "k_sweep3_list<float,WMom>", "peak_kind": peak_kind,
                          "pipe": {"bound": "fp32", "achieved_tflops": fp32_tflops,
                                   "peak_tflops": fp32_peak,
                                   "frac": (fp32_tflops / fp32_peak) if fp32_tflops else None,

@@ -240,7 +240,8 @@ int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
  * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket
  * max h and per-step neighbour lists, [3] momentum/energy sweep, [4] its commit + EOS, [5] density sweep,
  * [6] its commit + EOS, [7] velocity filter, [8] position update and
- * re-bucketing, [9] dt reduction, [10] total.  n <= 11 entries. */
+ * re-bucketing, [9] dt reduction, [10] total, [11] the momentum pair-sweep
+ * kernel alone (inside [3]).  n <= 12 entries. */
 int plume_phase_times(plume_ctx *ctx, float *ms, int n);
 
 /* Device kernel launches issued by the last plume_step/plume_steps call. */
@@ -249,6 +250,49 @@ int plume_launch_count(plume_ctx *ctx, uint64_t *n);
 /* Text of the last error of ctx (or of the last failed create if ctx is
  * NULL). */
 int plume_last_error(plume_ctx *ctx, char *buf, size_t len);
+
+/* ---------------------------------------------------------------- ensembles
+ * An ensemble context holds nmembers independent runs (members) in one
+ * particle table: every particle carries its member id; each member has its
+ * own bucket grid, time state (dt, time, step, output counter) and the
+ * per-member options (cfl, ng0, cvs, cvg, cva, rg, ra, vent_z, sml_phase2,
+ * max_time, timeoutput, stat_erupt, end_erupt, max_steps).  All other
+ * options must be equal across members.  Every kernel of a step covers the
+ * particles of all members in one launch; a member never sees another
+ * member's particles and computes what it would compute alone (bit for bit
+ * in FP64).  A member stops stepping at its own TimeProps::ifend
+ * (properties.h:76-79), or at its first error status (where the reference
+ * asserts and aborts the run), while the others go on: the ensemble entry
+ * points do not return members' statuses, plume_batch_time does.  No
+ * counterpart in the
+ * reference, which runs one problem per process: this is the batched path
+ * for parameter sweeps and ensembles.
+ *
+ * plume_batch_create: options[m] and grids[m] for m < nmembers; the
+ *   context's capacity is the sum of options[m].capacity.  The single-run
+ *   entry points (plume_step, plume_steps, plume_count, plume_download,
+ *   plume_neighbor_pairs, plume_set_ghost_state ...) work on ensembles too;
+ *   plume_get_time reports member 0 and plume_set_time sets every member.
+ * plume_batch_upload / plume_batch_append: particles of any members, member
+ *   ids per row (< nmembers).
+ * plume_batch_download: plume_download plus the member id of every row.
+ * plume_batch_time: per-member time, step, running flag (0 once the member
+ *   reached its end or failed) and status (PLUME_OK or the PLUME_E_* code
+ *   that stopped it); arrays of nmembers entries, any may be NULL.
+ * plume_batch_run: steps every running member until all have ended or
+ *   max_steps steps were issued.  graph_steps > 0 captures that many steps
+ *   into one CUDA graph and replays it (the host checks the members between
+ *   replays; ended members idle inside a replay); 0 issues steps one by
+ *   one.  Members of a single-run context are stopped at their end as well.
+ *   plume_phase_times reports the run's device time in [10]. */
+#define PLUME_MAX_MEMBERS 65535
+int plume_batch_create(const PlumeOptions *options, const PlumeGrid *grids, int nmembers,
+                       plume_ctx **out);
+int plume_batch_upload(plume_ctx *ctx, const PlumeSoA *host, const uint16_t *member, size_t n);
+int plume_batch_append(plume_ctx *ctx, const PlumeSoA *host, const uint16_t *member, size_t n);
+int plume_batch_download(plume_ctx *ctx, PlumeSoA *host, uint16_t *member, size_t cap, size_t *n);
+int plume_batch_time(plume_ctx *ctx, double *time, int *step, int *running, int *status);
+int plume_batch_run(plume_ctx *ctx, int max_steps, int graph_steps, int *steps_done);
 
 /* Time step without allocating: dt_out[0] = cfl * min(h[i] / c[i]) over the
  * particles with bc_type 100 or 99 (1.0e10 when there are none), from

@@ -32,27 +32,51 @@ namespace {
 constexpr int NTHREADS = 128;
 // phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax + lists, 3 momentum,
 // 4 commit_mom, 5 density, 6 commit_dens, 7 velocity, 8 position, 9 dt,
-// 10 total
-constexpr int NPHASE = 11;
-constexpr int NEV = 11;
+// 10 total, 11 the momentum pair-sweep kernel alone (part of 3)
+constexpr int NPHASE = 12;
+constexpr int NEV = 12;
 
 inline int nblocks(size_t n, int t = NTHREADS) { return (int)((n + t - 1) / t); }
 
 __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
-// ---- dt: min over need_neigh of h/c (timestep.cc:94-135) -----------------
-__global__ void k_dt_reduce(Dev A, const int* __restrict__ d_count, TimeState* ts) {
+// ---- dt: min over need_neigh of h/c (timestep.cc:94-135), per member ----
+// A block whose particles belong to one member (the common case: particles
+// are sorted by member) reduces in shared memory and issues one atomic per
+// quantity; a block that straddles members falls back to per-particle atomics.
+__global__ void k_dt_reduce(Dev A, const int* __restrict__ d_count, TimeState* ts_all) {
   __shared__ double red[NTHREADS];
   __shared__ unsigned int nr[NTHREADS];
+  __shared__ int bm, straddle;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   double v = 1.0e10;
   unsigned int real = 0;
+  int m = -1;
+  if (threadIdx.x == 0) { bm = -1; straddle = 0; }
+  __syncthreads();
   if (i < *d_count && need_neigh(A.bc[i])) {
-    double c = A.c[i];
-    if (!(c > 0)) set_status(ts, 4);
-    double t = A.h[i] / c;
-    if (t < v) v = t;
-    real = 1;
+    m = A.mem[i];
+    TimeState* ts = ts_all + m;
+    if (ts->active) {
+      double c = A.c[i];
+      if (!(c > 0)) set_status(ts, 4);
+      double t = A.h[i] / c;
+      if (t < v) v = t;
+      real = 1;
+      atomicCAS(&bm, -1, m);
+    } else {
+      m = -1;
+    }
+  }
+  __syncthreads();
+  if (m >= 0 && m != bm) straddle = 1;
+  __syncthreads();
+  if (straddle) {
+    if (m >= 0) {
+      if (v > 0 && v == v) atomicMin(&ts_all[m].dtmin_bits, dbits(v));
+      atomicAdd(&ts_all[m].n_real, 1ull);
+    }
+    return;
   }
   red[threadIdx.x] = v;
   nr[threadIdx.x] = real;
@@ -64,15 +88,20 @@ __global__ void k_dt_reduce(Dev A, const int* __restrict__ d_count, TimeState* t
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    double m = red[0];
-    if (m > 0 && m == m) atomicMin(&ts->dtmin_bits, dbits(m));
-    if (nr[0]) atomicAdd(&ts->n_real, (unsigned long long)nr[0]);
+  if (threadIdx.x == 0 && bm >= 0) {
+    double mn = red[0];
+    if (mn > 0 && mn == mn) atomicMin(&ts_all[bm].dtmin_bits, dbits(mn));
+    if (nr[0]) atomicAdd(&ts_all[bm].n_real, (unsigned long long)nr[0]);
   }
 }
 
-// TimeProps::incrtime and iferupt
-__global__ void k_incrtime(Opt o, TimeState* ts) {
+// TimeProps::incrtime and iferupt, one thread per member
+__global__ void k_incrtime(const Opt* __restrict__ mopt, TimeState* ts_all, int nmem) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Opt& o = mopt[m];
   double dt = o.cfl * __longlong_as_double((long long)ts->dtmin_bits);
   if ((ts->time + dt) > ts->ndtimeoutput) dt = ts->ndtimeoutput - ts->time;
   if ((ts->time + dt) > o.max_time) dt = o.max_time - ts->time;
@@ -82,26 +111,47 @@ __global__ void k_incrtime(Opt o, TimeState* ts) {
   ts->erupt = !((ts->time * 1.0) < o.stat_erupt) && !((ts->time * 1.0) > o.end_erupt);
 }
 
-// TimeProps::ifoutput; resets the per-step reductions
-__global__ void k_end_step(Opt o, TimeState* ts) {
+// TimeProps::ifoutput
+__global__ void k_end_step(const Opt* __restrict__ mopt, TimeState* ts_all, int nmem) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmem) return;
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Opt& o = mopt[m];
   if (ts->time >= ts->ndtimeoutput || ts->time == o.max_time) {
     ts->ioutput++;
     ts->ndtimeoutput = ((ts->ioutput + 1) * o.timeoutput) / 1.0;
   }
 }
-__global__ void k_begin_step(TimeState* ts) {
+// start of a step: which members step (a frozen member stops at
+// TimeProps::ifend, properties.h:76-79, or at its first error status, where
+// the reference asserts), reset of the per-step reductions, and the
+// context's step counter (adaptive_sml schedule)
+__global__ void k_begin_step(const Opt* __restrict__ mopt, TimeState* ts_all, int nmem, int* hstep) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m == 0) (*hstep)++;
+  if (m >= nmem) return;
+  TimeState* ts = ts_all + m;
+  const Opt& o = mopt[m];
+  ts->active = !(ts->freeze && ((ts->time >= o.max_time) || (ts->step > o.max_steps) || ts->status != 0));
   ts->dtmin_bits = dbits(1.0e10);
   ts->n_real = 0;
 }
 
 // ---- search --------------------------------------------------------------
-__global__ void k_keys(Geo g, Dev A, int n, uint32_t* __restrict__ keys, uint32_t ncells, TimeState* ts) {
+// key = the member's cell base + the fine cell inside the member's grid, so
+// that the sort groups particles by member, then by cell
+__global__ void k_keys(const Geo* __restrict__ geo, Dev A, int n, uint32_t* __restrict__ keys, uint32_t ncells,
+                       TimeState* ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (A.bc[i] == BC_DEAD) {
     keys[i] = ncells;
     return;
   }
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  const Geo g = geo[m];
   bool o1 = false, o2 = false, o3 = false;
   int b0, b1 = 0, b2 = 0;
   int c0 = cell_axis(g, 0, A.x[i], &b0, &o1);
@@ -116,14 +166,18 @@ __global__ void k_keys(Geo g, Dev A, int n, uint32_t* __restrict__ keys, uint32_
     A.bc[i] = BC_DEAD;
     return;
   }
-  keys[i] = (uint32_t)(((size_t)c2 * g.G[1] + c1) * g.G[0] + c0);
+  keys[i] = g.cell_base + (uint32_t)(((size_t)c2 * g.G[1] + c1) * g.G[0] + c0);
   A.bkt[i] = (g.dim == 3) ? (b2 * g.nb[1] + b1) * g.nb[0] + b0 : b0;
 }
 
-__global__ void k_gather(Geo g, Dev A, Dev B, Work W, const uint32_t* __restrict__ perm, int n, int mixed) {
+__global__ void k_gather(const Geo* __restrict__ geo, Dev A, Dev B, Work W, const uint32_t* __restrict__ perm,
+                         int n) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   int q = perm[p];
+  const int m = A.mem[q];
+  const Geo g = geo[m];
+  B.mem[p] = (uint16_t)m;
   B.key[p] = A.key[q];
   B.x[p] = A.x[q];
   B.vx[p] = A.vx[q];
@@ -150,8 +204,7 @@ __global__ void k_gather(Geo g, Dev A, Dev B, Work W, const uint32_t* __restrict
   B.inv[p] = A.inv[q];
   int b = A.bkt[q];
   B.bkt[p] = b;
-  (void)mixed;  // bucket-relative coordinates serve both paths (cell ranges)
-  {
+  {  // bucket-relative coordinates serve both paths (cell ranges)
     int bi[3];
     if (g.dim == 3) {
       bi[0] = b % g.nb[0];
@@ -193,21 +246,29 @@ __global__ void k_hmax_reset(unsigned long long* hb, int nbk) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < nbk) hb[b] = 0ull;
 }
-__global__ void k_hmax(Dev A, const int* __restrict__ d_count, unsigned long long* hb, int dim) {
+// per-bucket tables cover the buckets of every member (a 1D member has one
+// entry: the maximum over all its particles)
+__global__ void k_hmax(const Geo* __restrict__ geo, Dev A, const int* __restrict__ d_count,
+                       unsigned long long* hb, int dim) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (A.bc[i] == BC_DEAD) return;
   double h = A.h[i];
-  atomicMax(&hb[dim == 3 ? A.bkt[i] : 0], dbits(h));
+  const int base = geo[A.mem[i]].bucket_base;
+  atomicMax(&hb[base + (dim == 3 ? A.bkt[i] : 0)], dbits(h));
 }
-__global__ void k_hmax27(Geo g, const unsigned long long* __restrict__ hb, double* __restrict__ h27) {
-  int nbk = g.nb[0] * g.nb[1] * g.nb[2];
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_hmax27(const Geo* __restrict__ geo, const uint16_t* __restrict__ bmember, int nbk_all,
+                         const unsigned long long* __restrict__ hb_all, double* __restrict__ h27_all) {
+  int ba = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ba >= nbk_all) return;
+  const Geo& g = geo[bmember[ba]];
+  const unsigned long long* hb = hb_all + g.bucket_base;
+  const int b = ba - g.bucket_base;
   if (g.dim != 3) {
-    if (b == 0) h27[0] = __longlong_as_double((long long)hb[0]);
+    h27_all[ba] = __longlong_as_double((long long)hb[0]);
     return;
   }
-  if (b >= nbk) return;
+  double* h27 = h27_all + g.bucket_base;
   int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
   double m = 0;
   for (int dz = -1; dz <= 1; dz++)
@@ -222,9 +283,10 @@ __global__ void k_hmax27(Geo g, const unsigned long long* __restrict__ hb, doubl
 
 // ---- neighbour pairs (plume_neighbor_pairs) -------------------------------
 template <int D>
-__global__ void k_pairs(int mode, Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
-                        const int* __restrict__ d_count, const unsigned long long* __restrict__ offs,
-                        unsigned int* __restrict__ cnt, uint64_t* __restrict__ ki, uint64_t* __restrict__ kj) {
+__global__ void k_pairs(int mode, Opt o, const Geo* __restrict__ geo, Dev A, Work W,
+                        const uint32_t* __restrict__ cs_all, const int* __restrict__ d_count,
+                        const unsigned long long* __restrict__ offs, unsigned int* __restrict__ cnt,
+                        uint64_t* __restrict__ ki, uint64_t* __restrict__ kj) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = *d_count;
   if (i >= n) return;
@@ -232,6 +294,8 @@ __global__ void k_pairs(int mode, Opt o, Geo g, Dev A, Work W, const uint32_t* _
     if (!offs) cnt[i] = 0;
     return;
   }
+  const Geo g = geo[A.mem[i]];
+  const uint32_t* cs = cs_all + g.cell_base;
   double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
   bucket_coords<D>(g, A.bkt[i], bi);
@@ -246,8 +310,8 @@ __global__ void k_pairs(int mode, Opt o, Geo g, Dev A, Work W, const uint32_t* _
     }
     c++;
   };
-  if (mode == 0 && D == 1) {
-    for (int j = 0; j < n; j++)
+  if (mode == 0 && D == 1) {  // all particles of the member (add_air.cc:470-479)
+    for (uint32_t j = cs[0]; j < cs[g.G[0]]; j++)
       if (A.bc[j] != BC_DEAD) take(j);
   } else {
     double R = (mode == 0) ? fmax(Lb, g.del) * (1.0 + 1e-10) : o.cutoff2 * hi * (1.0 + 1e-10);
@@ -320,10 +384,12 @@ __global__ void k_scan_add(unsigned long long* out, int n, const unsigned long l
 }
 
 // ---- ghost state (plume_set_ghost_state) -----------------------------------
-__global__ void k_set_ghost(Opt o, Dev A, const int* __restrict__ d_count, const uint64_t* __restrict__ keys,
-                            const double* __restrict__ state, const double* __restrict__ Yin, int m, int dim) {
+__global__ void k_set_ghost(const Opt* __restrict__ mopt, Dev A, const int* __restrict__ d_count,
+                            const uint64_t* __restrict__ keys, const double* __restrict__ state,
+                            const double* __restrict__ Yin, int m, int dim) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
+  const Opt& o = mopt[A.mem[i]];
   uint64_t k = A.key[i];
   int lo = 0, hi = m;
   while (lo < hi) {
@@ -351,9 +417,25 @@ __global__ void k_set_ghost(Opt o, Dev A, const int* __restrict__ d_count, const
 static thread_local std::string g_create_error;
 
 struct plume_ctx {
-  PlumeOptions opt{};
-  Opt o{};
-  Geo g{};
+  PlumeOptions opt{};  // member 0's options
+  Opt o{};             // member 0's options: the fields every member shares
+  // ensemble members (one for a single run): grid, options and time state of
+  // each, on the host and on the device
+  int nmem = 1;
+  bool batch = false;
+  std::vector<Geo> hgeo;
+  std::vector<Opt> hopt;
+  Geo* d_geo = nullptr;
+  Opt* d_opt = nullptr;
+  uint16_t* bmember = nullptr;  // member of every per-bucket table entry
+  int* d_hstep = nullptr;       // steps issued (adaptive_sml schedule)
+  // CUDA graph of graph_steps steps (plume_batch_run)
+  bool capturing = false;
+  cudaGraphExec_t gexec = nullptr;
+  int gsteps = 0;
+  size_t gn = 0;
+  unsigned long long glaunches = 0;
+  cudaEvent_t run_ev[2] = {nullptr, nullptr};  // device time of plume_batch_run
   cudaStream_t st = nullptr;
   size_t cap = 0;
   size_t n_alloc = 0;  // rows in use (upper bound of live particles)
@@ -374,7 +456,7 @@ struct plume_ctx {
   uint32_t ncells = 0;
   int keybits = 1;
   int* d_count = nullptr;
-  TimeState* ts = nullptr;
+  TimeState* ts = nullptr;    // nmem entries
   TimeState* h_ts = nullptr;  // pinned mirror
   unsigned long long* hb = nullptr;
   double* h27 = nullptr;
@@ -426,6 +508,7 @@ static int alloc_dev(plume_ctx* ctx, Dev& D, size_t cap) {
   DALLOC(D.bc, cap);
   DALLOC(D.inv, cap);
   DALLOC(D.bkt, 4 * cap);
+  DALLOC(D.mem, 2 * cap);
   return PLUME_OK;
 }
 
@@ -439,20 +522,36 @@ static Opt make_opt(const PlumeOptions& p) {
   o.rg = p.rg; o.ra = p.ra; o.vent_z = p.vent_z; o.sml2 = p.sml_phase2; o.max_time = p.max_time;
   o.timeoutput = p.timeoutput; o.stat_erupt = p.stat_erupt; o.end_erupt = p.end_erupt;
   o.ksupport = (p.kernel == PLUME_KERNEL_M4) ? 2.0 : 3.0;
+  o.max_steps = p.max_steps;
   return o;
 }
 
+// waits for the stream, mirrors the members' time states and returns the
+// first member's nonzero status (cleared on the device).  An ensemble keeps
+// its members' statuses: a failed member stops, the others go on, and
+// plume_batch_time reports them.
 static int ctx_sync_status(plume_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->st));
-  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
-  int s = ctx->h_ts->status;
-  if (s) {
-    ctx->err = std::string("device status ") + std::to_string(s);
-    TimeState clr = *ctx->h_ts;
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyDeviceToHost));
+  if (ctx->batch) return PLUME_OK;
+  int s = 0;
+  for (int m = 0; m < ctx->nmem; m++) {
+    const int sm = ctx->h_ts[m].status;
+    if (!sm) continue;
+    if (!s) {
+      s = sm;
+      ctx->err = std::string("device status ") + std::to_string(sm) +
+                 (ctx->nmem > 1 ? std::string(" in member ") + std::to_string(m) : std::string());
+    }
+    TimeState clr = ctx->h_ts[m];
     clr.status = 0;
-    CK(cudaMemcpy(ctx->ts, &clr, sizeof(TimeState), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->ts + m, &clr, sizeof(TimeState), cudaMemcpyHostToDevice));
   }
   return s;
+}
+
+static void record_ev(plume_ctx* ctx, int k) {
+  if (!ctx->capturing) cudaEventRecord(ctx->ev[k], ctx->st);
 }
 
 // search: keys, radix sort, gather into B, swap, cell_start
@@ -464,11 +563,10 @@ static int search(plume_ctx* ctx) {
     ctx->launches++;
     return PLUME_OK;
   }
-  k_keys<<<nblocks(n), NTHREADS, 0, st>>>(ctx->g, ctx->A, n, ctx->keys, ctx->ncells, ctx->ts);
+  k_keys<<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, n, ctx->keys, ctx->ncells, ctx->ts);
   ctx->launches++;
   ctx->launches += ctx->sorter.sort(ctx->keys, ctx->perm, n, ctx->keybits, st);
-  k_gather<<<nblocks(n), NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->B, ctx->W, ctx->perm, n,
-                                            ctx->opt.precision == PLUME_PREC_MIXED);
+  k_gather<<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->B, ctx->W, ctx->perm, n);
   std::swap(ctx->A, ctx->B);
   k_cell_start<<<nblocks((size_t)ctx->ncells + 2, 256), 256, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
   ctx->launches += 2;
@@ -477,26 +575,29 @@ static int search(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
-template <int D, typename T>
+template <int D, typename T, bool MULTI>
 static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
+  const Geos<MULTI> gs{ctx->hgeo[0], ctx->d_geo};
   cudaStream_t st = ctx->st;
   const int n = (int)ctx->n_alloc;
   const int nb = nblocks(n);
-  if (adaptive_now) {
-    k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+  if (adaptive_now || (ctx->capturing && ctx->o.adaptive)) {
+    // a captured step decides on the device (step counter % interval)
+    k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
+                                              ctx->d_hstep, ctx->capturing ? 0 : 1);
     ctx->launches++;
   }
-  cudaEventRecord(ctx->ev[3], st);
+  record_ev(ctx, 3);
   k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
-  k_hmax<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->hb, D);
-  k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->g, ctx->hb, ctx->h27);
+  k_hmax<<<nb, NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->hb, D);
+  k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->nbk, ctx->hb, ctx->h27);
   const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
   const bool mixed = sizeof(T) == 4;
   const bool lists = (D == 3) && ctx->use_lists;
   if constexpr (D == 3) {
     if (lists) {
       const int ns = n ? n : 1, nsb = (ns + 1023) / 1024;
-      k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->rflag);
+      k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->ts, ctx->rflag);
       k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, ns, ctx->roffs, ctx->rsums);
       k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
       k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, ns, ctx->rsums);
@@ -506,45 +607,48 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         k_pack_pos<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
         ctx->launches++;
       }
-      k_build_lists<T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->L);
+      k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts, ctx->L);
       ctx->launches++;
     }
   }
-  cudaEventRecord(ctx->ev[4], st);
+  record_ev(ctx, 4);
   if constexpr (D == 3) {
     if (mixed) {
-      k_pack_mom<<<nb, NTHREADS, 0, st>>>(ctx->g, ctx->A, ctx->K, ctx->W, ctx->o.lans, ctx->d_count);
+      k_pack_mom<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->o.lans, ctx->d_count);
       ctx->launches++;
     }
+    record_ev(ctx, 11);
     if (lists)
-      k_sweep3_list<T, WMom><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      k_sweep3_list<T, WMom, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
     else if (ctx->sweep_warp)
-      k_sweep3<T, WMom, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+      k_sweep3<T, WMom, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
-      k_sweep3<T, WMom, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
-  } else
-    k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
-  cudaEventRecord(ctx->ev[5], st);
-  k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
+      k_sweep3<T, WMom, false, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  } else {
+    record_ev(ctx, 11);
+    k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  }
+  record_ev(ctx, 5);
+  k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, ctx->W, ctx->d_count, ctx->ts);
   ctx->launches += 5;
-  cudaEventRecord(ctx->ev[6], st);
+  record_ev(ctx, 6);
   if constexpr (D == 3) {
     if (mixed) {
       k_pack_dens<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->o.pgc, ctx->d_count);
       ctx->launches++;
     }
     if (lists)
-      k_sweep3_list<T, WDens><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      k_sweep3_list<T, WDens, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
     else if (ctx->sweep_warp)
-      k_sweep3<T, WDens, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+      k_sweep3<T, WDens, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
-      k_sweep3<T, WDens, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+      k_sweep3<T, WDens, false, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
   } else
-    k_density<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
-  cudaEventRecord(ctx->ev[7], st);
-  k_commit_dens<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->A, ctx->W, ctx->d_count);
+    k_density<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+  record_ev(ctx, 7);
+  k_commit_dens<D><<<nb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, ctx->W, ctx->d_count, ctx->ts);
   ctx->launches += 2;
-  cudaEventRecord(ctx->ev[8], st);
+  record_ev(ctx, 8);
   if (ctx->o.lans) {
     if constexpr (D == 3) {
       if (mixed) {
@@ -552,52 +656,57 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         ctx->launches++;
       }
       if (lists)
-        k_sweep3_list<T, WVel><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+        k_sweep3_list<T, WVel, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
       else if (ctx->sweep_warp)
-        k_sweep3<T, WVel, true><<<nbw, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+        k_sweep3<T, WVel, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
       else
-        k_sweep3<T, WVel, false><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+        k_sweep3<T, WVel, false, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     } else
-      k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+      k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
     ctx->launches++;
   }
-  cudaEventRecord(ctx->ev[9], st);
+  record_ev(ctx, 9);
 }
 
 // one step, no host synchronisation
 static int step_async(plume_ctx* ctx) {
   cudaStream_t st = ctx->st;
   const int n = (int)ctx->n_alloc;
-  cudaEventRecord(ctx->ev[0], st);
-  k_begin_step<<<1, 1, 0, st>>>(ctx->ts);
+  record_ev(ctx, 0);
+  const int mb = nblocks(ctx->nmem);
+  k_begin_step<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem, ctx->d_hstep);
   k_dt_reduce<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->ts);
-  k_incrtime<<<1, 1, 0, st>>>(ctx->o, ctx->ts);
+  k_incrtime<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem);
   ctx->launches += 3;
-  cudaEventRecord(ctx->ev[1], st);
+  record_ev(ctx, 1);
   int rc = search(ctx);
   if (rc) return rc;
-  cudaEventRecord(ctx->ev[2], st);
+  record_ev(ctx, 2);
   ctx->host_step++;
   bool adaptive_now = ctx->o.adaptive && (ctx->host_step % ctx->o.interval) == 0;
   const bool mixed = ctx->opt.precision == PLUME_PREC_MIXED;
   if (ctx->o.dim == 3) {
-    if (mixed) launch_sweeps<3, float>(ctx, adaptive_now); else launch_sweeps<3, double>(ctx, adaptive_now);
-    k_update_pos<3><<<nblocks(n), NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
+    if (ctx->nmem > 1) {
+      if (mixed) launch_sweeps<3, float, true>(ctx, adaptive_now); else launch_sweeps<3, double, true>(ctx, adaptive_now);
+    } else {
+      if (mixed) launch_sweeps<3, float, false>(ctx, adaptive_now); else launch_sweeps<3, double, false>(ctx, adaptive_now);
+    }
+    k_update_pos<3><<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
   } else {
-    if (mixed) launch_sweeps<1, float>(ctx, adaptive_now); else launch_sweeps<1, double>(ctx, adaptive_now);
-    k_update_pos<1><<<nblocks(n), NTHREADS, 0, st>>>(ctx->o, ctx->g, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
+    if (mixed) launch_sweeps<1, float, true>(ctx, adaptive_now); else launch_sweeps<1, double, true>(ctx, adaptive_now);
+    k_update_pos<1><<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
   }
-  k_end_step<<<1, 1, 0, st>>>(ctx->o, ctx->ts);
+  k_end_step<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem);
   ctx->launches += 2;
   ctx->pending_dead = true;
-  cudaEventRecord(ctx->ev[10], st);
+  record_ev(ctx, 10);
   CK(cudaGetLastError());
   return PLUME_OK;
 }
 
 // events of a step: 0 start, 1 after dt, 2 after search, 3 after adaptive,
 // 4 after hmax, 5 after momentum, 6 after commit, 7 after density, 8 after
-// commit, 9 after velocity, 10 end
+// commit, 9 after velocity, 10 end, 11 before the momentum pair sweep
 static void accumulate_phases(plume_ctx* ctx, const cudaEvent_t* e) {
   float t[NPHASE];
   cudaEventElapsedTime(&t[9], e[0], e[1]);
@@ -611,6 +720,7 @@ static void accumulate_phases(plume_ctx* ctx, const cudaEvent_t* e) {
   cudaEventElapsedTime(&t[7], e[8], e[9]);
   cudaEventElapsedTime(&t[8], e[9], e[10]);
   cudaEventElapsedTime(&t[10], e[0], e[10]);
+  cudaEventElapsedTime(&t[11], e[11], e[5]);
   for (int k = 0; k < NPHASE; k++) ctx->phase_ms[k] += t[k];
 }
 
@@ -638,27 +748,60 @@ int plume_last_error(plume_ctx* ctx, char* buf, size_t len) {
   return PLUME_OK;
 }
 
-int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out) {
-  if (!opt || !grid || !out) {
+// Options every member of an ensemble shares (the sweeps read them once per
+// launch); the others (cfl, mixture constants, vent, times, max_steps) are
+// per member.
+static bool same_shared_options(const PlumeOptions& a, const PlumeOptions& b) {
+  return a.dim == b.dim && a.precision == b.precision && a.kernel == b.kernel && a.lans == b.lans &&
+         a.energy_smooth == b.energy_smooth && a.pghost_contrib == b.pghost_contrib &&
+         a.adaptive_sml == b.adaptive_sml && a.sml_interval == b.sml_interval && a.num_loop == b.num_loop &&
+         a.thresh == b.thresh && a.c_smooth == b.c_smooth && a.eta_smooth == b.eta_smooth &&
+         a.alpha == b.alpha && a.beta == b.beta && a.ata == b.ata && a.cutoff2 == b.cutoff2 &&
+         a.list_factor == b.list_factor && a.g == b.g;
+}
+
+static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem, bool batch, plume_ctx** out) {
+  if (!opts || !grids || !out || nmem < 1) {
     g_create_error = "null argument";
     return PLUME_E_INVALID;
   }
+  if (nmem > PLUME_MAX_MEMBERS) {
+    g_create_error = "too many members";
+    return PLUME_E_INVALID;
+  }
+  const PlumeOptions* opt = &opts[0];
   if (opt->dim != 1 && opt->dim != 3) {
     g_create_error = "dim must be 1 or 3";
     return PLUME_E_INVALID;
   }
-  if (opt->capacity == 0 || opt->capacity > (size_t)0x7fffffff) {
+  size_t capacity = 0;
+  double ncell_tot = 0, nbk_tot = 0;
+  for (int m = 0; m < nmem; m++) {
+    const PlumeOptions& om = opts[m];
+    const PlumeGrid& gm = grids[m];
+    if (m > 0 && !same_shared_options(om, *opt)) {
+      g_create_error = "member " + std::to_string(m) + ": options differ from member 0 in a shared field";
+      return PLUME_E_INVALID;
+    }
+    if (om.capacity == 0) {
+      g_create_error = "capacity must be >= 1";
+      return PLUME_E_INVALID;
+    }
+    capacity += om.capacity;
+    if (gm.del <= 0 || gm.nb[0] < 1 || gm.nb[1] < 1 || gm.nb[2] < 1 ||
+        (opt->dim == 1 && (gm.nb[1] != 1 || gm.nb[2] != 1))) {
+      g_create_error = "invalid bucket grid" + (nmem > 1 ? " of member " + std::to_string(m) : std::string());
+      return PLUME_E_INVALID;
+    }
+    const int s = gm.subcells > 0 ? gm.subcells : 1;
+    ncell_tot += (double)gm.nb[0] * s * (opt->dim == 3 ? (double)gm.nb[1] * s * gm.nb[2] * s : 1.0);
+    nbk_tot += (opt->dim == 3) ? (double)gm.nb[0] * gm.nb[1] * gm.nb[2] : 1.0;
+  }
+  if (capacity > (size_t)0x7fffffff) {
     g_create_error = "capacity must be in [1, 2^31)";
     return PLUME_E_INVALID;
   }
-  if (grid->del <= 0 || grid->nb[0] < 1 || grid->nb[1] < 1 || grid->nb[2] < 1 ||
-      (opt->dim == 1 && (grid->nb[1] != 1 || grid->nb[2] != 1))) {
-    g_create_error = "invalid bucket grid";
-    return PLUME_E_INVALID;
-  }
-  int s = grid->subcells > 0 ? grid->subcells : 1;
-  double ncell_d = (double)grid->nb[0] * s * (opt->dim == 3 ? (double)grid->nb[1] * s * grid->nb[2] * s : 1.0);
-  if (ncell_d > 2.0e9) {
+  if (ncell_tot > 2.0e9 || nbk_tot > 2.0e9) {
     g_create_error = "too many fine cells";
     return PLUME_E_INVALID;
   }
@@ -670,30 +813,54 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
   plume_ctx* ctx = new plume_ctx();
   ctx->opt = *opt;
   ctx->o = make_opt(*opt);
-  Geo& g = ctx->g;
-  for (int a = 0; a < 3; a++) {
-    g.mind[a] = grid->mindom[a];
-    g.nb[a] = grid->nb[a];
-    g.lo[a] = grid->domain_lo[a];
-    g.hi[a] = grid->domain_hi[a];
+  ctx->nmem = nmem;
+  ctx->batch = batch;
+  ctx->hgeo.resize(nmem);
+  ctx->hopt.resize(nmem);
+  uint32_t cell_base = 0;
+  int bucket_base = 0;
+  std::vector<uint16_t> bmember;
+  for (int m = 0; m < nmem; m++) {
+    const PlumeGrid* grid = &grids[m];
+    const int s = grid->subcells > 0 ? grid->subcells : 1;
+    Geo& g = ctx->hgeo[m];
+    g = Geo{};
+    for (int a = 0; a < 3; a++) {
+      g.mind[a] = grid->mindom[a];
+      g.nb[a] = grid->nb[a];
+      g.lo[a] = grid->domain_lo[a];
+      g.hi[a] = grid->domain_hi[a];
+    }
+    g.del = grid->del;
+    g.s = s;
+    g.cw = grid->del / s;
+    g.idel = 1.0 / g.del;
+    g.icw = 1.0 / g.cw;
+    g.dim = opt->dim;
+    for (int a = 0; a < 3; a++) g.G[a] = (opt->dim == 3 || a == 0) ? g.nb[a] * s : 1;
+    g.nbk = (opt->dim == 3) ? g.nb[0] * g.nb[1] * g.nb[2] : 1;
+    g.cell_base = cell_base;
+    g.bucket_base = bucket_base;
+    cell_base += (uint32_t)((size_t)g.G[0] * g.G[1] * g.G[2]);
+    bucket_base += g.nbk;
+    bmember.insert(bmember.end(), (size_t)g.nbk, (uint16_t)m);
+    ctx->hopt[m] = make_opt(opts[m]);
   }
-  g.del = grid->del;
-  g.s = s;
-  g.cw = grid->del / s;
-  g.idel = 1.0 / g.del;
-  g.icw = 1.0 / g.cw;
-  g.dim = opt->dim;
-  for (int a = 0; a < 3; a++) g.G[a] = (opt->dim == 3 || a == 0) ? g.nb[a] * s : 1;
-  ctx->ncells = (uint32_t)((size_t)g.G[0] * g.G[1] * g.G[2]);
+  ctx->ncells = cell_base;
   ctx->keybits = 1;
   while ((1ull << ctx->keybits) <= (unsigned long long)ctx->ncells) ctx->keybits++;
-  ctx->nbk = (opt->dim == 3) ? g.nb[0] * g.nb[1] * g.nb[2] : 1;
-  ctx->cap = opt->capacity;
+  ctx->nbk = bucket_base;
+  ctx->cap = capacity;
   ctx->sweep_warp = (opt->precision == PLUME_PREC_FP64);
   if (const char* sw = getenv("PLUME_SWEEP")) {
     if (!strcmp(sw, "warp")) { ctx->sweep_warp = true; ctx->use_lists = false; }
     if (!strcmp(sw, "thread")) { ctx->sweep_warp = false; ctx->use_lists = false; }
     if (!strcmp(sw, "list")) { ctx->sweep_warp = false; ctx->use_lists = true; }
+  }
+  if (opt->dim == 3 && ctx->use_lists && capacity > (size_t)NL_JMASK) {
+    g_create_error = "capacity above the neighbour-list index range (2^26)";
+    delete ctx;
+    return PLUME_E_INVALID;
   }
   int rc = PLUME_OK;
   auto fail = [&](int code) {
@@ -736,38 +903,62 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
     if ((rc = dev_alloc(ctx, (void**)&ctx->keys, 4 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->perm, 4 * c)) ||
         (rc = dev_alloc(ctx, (void**)&ctx->cs, 4 * ((size_t)ctx->ncells + 2))) ||
         (rc = dev_alloc(ctx, (void**)&ctx->d_count, sizeof(int))) ||
-        (rc = dev_alloc(ctx, (void**)&ctx->ts, sizeof(TimeState))) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->ts, sizeof(TimeState) * (size_t)nmem)) ||
         (rc = dev_alloc(ctx, (void**)&ctx->hb, 8 * (size_t)ctx->nbk)) ||
-        (rc = dev_alloc(ctx, (void**)&ctx->h27, 8 * (size_t)ctx->nbk)))
+        (rc = dev_alloc(ctx, (void**)&ctx->h27, 8 * (size_t)ctx->nbk)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->d_geo, sizeof(Geo) * (size_t)nmem)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->d_opt, sizeof(Opt) * (size_t)nmem)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->bmember, 2 * (size_t)ctx->nbk)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->d_hstep, sizeof(int))))
       return fail(rc);
     if (ctx->sorter.reserve((int)c) != cudaSuccess) {
       ctx->err = "radix sort buffers";
       return fail(PLUME_E_CUDA);
     }
   }
-  if (opt->dim == 3 && grid->flags) {
+  bool any_flags = false, any_face = false;
+  for (int m = 0; m < nmem; m++) {
+    any_flags |= grids[m].flags != nullptr;
+    any_face |= grids[m].face_index != nullptr;
+  }
+  if (opt->dim == 3 && any_flags) {
+    std::vector<uint8_t> f((size_t)ctx->nbk, 0);
+    for (int m = 0; m < nmem; m++)
+      if (grids[m].flags) memcpy(f.data() + ctx->hgeo[m].bucket_base, grids[m].flags, ctx->hgeo[m].nbk);
     if ((rc = dev_alloc(ctx, (void**)&ctx->bflags, ctx->nbk))) return fail(rc);
-    cudaMemcpy(ctx->bflags, grid->flags, ctx->nbk, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->bflags, f.data(), ctx->nbk, cudaMemcpyHostToDevice);
   }
-  if (opt->dim == 3 && grid->face_index) {
+  if (opt->dim == 3 && any_face) {
+    std::vector<int8_t> f(6 * (size_t)ctx->nbk, 0);
+    for (int m = 0; m < nmem; m++)
+      if (grids[m].face_index)
+        memcpy(f.data() + 6 * (size_t)ctx->hgeo[m].bucket_base, grids[m].face_index, 6 * (size_t)ctx->hgeo[m].nbk);
     if ((rc = dev_alloc(ctx, (void**)&ctx->bface, 6 * (size_t)ctx->nbk))) return fail(rc);
-    cudaMemcpy(ctx->bface, grid->face_index, 6 * (size_t)ctx->nbk, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->bface, f.data(), 6 * (size_t)ctx->nbk, cudaMemcpyHostToDevice);
   }
-  if (cudaMallocHost(&ctx->h_ts, sizeof(TimeState)) != cudaSuccess) {
+  if (cudaMallocHost(&ctx->h_ts, sizeof(TimeState) * (size_t)nmem) != cudaSuccess) {
     ctx->err = "cudaMallocHost";
     return fail(PLUME_E_CUDA);
   }
-  TimeState t{};
-  t.time = 0;
-  t.ndtimeoutput = opt->timeoutput;
-  t.dtmin_bits = 0;
-  *ctx->h_ts = t;
-  if (cudaMemcpy(ctx->ts, &t, sizeof(TimeState), cudaMemcpyHostToDevice) != cudaSuccess) {
-    ctx->err = "init time state";
-    return fail(PLUME_E_CUDA);
+  for (int m = 0; m < nmem; m++) {
+    TimeState t{};
+    t.time = 0;
+    t.ndtimeoutput = opts[m].timeoutput;
+    t.dtmin_bits = 0;
+    t.active = 1;
+    t.freeze = batch ? 1 : 0;
+    ctx->h_ts[m] = t;
   }
   int zero = 0;
-  cudaMemcpy(ctx->d_count, &zero, sizeof(int), cudaMemcpyHostToDevice);
+  if (cudaMemcpy(ctx->ts, ctx->h_ts, sizeof(TimeState) * (size_t)nmem, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->d_geo, ctx->hgeo.data(), sizeof(Geo) * (size_t)nmem, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->d_opt, ctx->hopt.data(), sizeof(Opt) * (size_t)nmem, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->bmember, bmember.data(), 2 * (size_t)ctx->nbk, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->d_hstep, &zero, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->d_count, &zero, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    ctx->err = "init member tables";
+    return fail(PLUME_E_CUDA);
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) {
     ctx->err = "device init";
     return fail(PLUME_E_CUDA);
@@ -776,9 +967,20 @@ int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out
   return PLUME_OK;
 }
 
+int plume_create(const PlumeOptions* opt, const PlumeGrid* grid, plume_ctx** out) {
+  return create_ctx(opt, grid, 1, false, out);
+}
+
+int plume_batch_create(const PlumeOptions* opts, const PlumeGrid* grids, int nmembers, plume_ctx** out) {
+  return create_ctx(opts, grids, nmembers, true, out);
+}
+
 int plume_destroy(plume_ctx* ctx) {
   if (!ctx) return PLUME_OK;
   if (ctx->st) cudaStreamSynchronize(ctx->st);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  for (auto e : ctx->run_ev)
+    if (e) cudaEventDestroy(e);
   for (void* p : ctx->allocs) cudaFree(p);
   ctx->sorter.release();
   if (ctx->h_ts) cudaFreeHost(ctx->h_ts);
@@ -802,9 +1004,18 @@ static int check_soa(plume_ctx* ctx, const PlumeSoA* s) {
   return PLUME_OK;
 }
 
-static int copy_soa(plume_ctx* ctx, const PlumeSoA* s, size_t off, size_t n, cudaMemcpyKind kind) {
+// member ids: null = member 0 for every row (single runs)
+static int copy_soa(plume_ctx* ctx, const PlumeSoA* s, size_t off, size_t n, cudaMemcpyKind kind,
+                    const uint16_t* member = nullptr) {
   int rc = check_soa(ctx, s);
   if (rc) return rc;
+  if (member && kind == cudaMemcpyHostToDevice) {
+    for (size_t r = 0; r < n; r++)
+      if (member[r] >= ctx->nmem) {
+        ctx->err = "member id out of range at row " + std::to_string(r);
+        return PLUME_E_INVALID;
+      }
+  }
   const bool d3 = ctx->o.dim == 3;
   cudaStream_t st = ctx->st;
   Dev& A = ctx->A;
@@ -831,6 +1042,10 @@ static int copy_soa(plume_ctx* ctx, const PlumeSoA* s, size_t off, size_t n, cud
   CK(cudaMemcpyAsync(A.phase + off, s->phase, n, kind, st));
   CK(cudaMemcpyAsync(A.bc + off, s->bc_type, n, kind, st));
   CK(cudaMemcpyAsync(A.inv + off, s->involved, n, kind, st));
+  if (member)
+    CK(cudaMemcpyAsync(A.mem + off, member, 2 * n, kind, st));
+  else
+    CK(cudaMemsetAsync(A.mem + off, 0, 2 * n, st));
   return PLUME_OK;
 }
 
@@ -906,7 +1121,7 @@ int plume_set_ghost_state(plume_ctx* ctx, const uint64_t* keys, const double* st
   CK(cudaMemcpy(ds, s.data(), 8 * n * w, cudaMemcpyHostToDevice));
   if (Y) CK(cudaMemcpy(dy, y.data(), 8 * n, cudaMemcpyHostToDevice));
   k_set_ghost<<<nblocks(ctx->n_alloc ? ctx->n_alloc : 1), NTHREADS, 0, ctx->st>>>(
-      ctx->o, ctx->A, ctx->d_count, dk, ds, dy, (int)n, ctx->o.dim);
+      ctx->d_opt, ctx->A, ctx->d_count, dk, ds, dy, (int)n, ctx->o.dim);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->st));
   cudaFree(dk);
@@ -938,13 +1153,17 @@ int plume_steps(plume_ctx* ctx, int nsteps, PlumeStepLog* log) {
       accumulate_phases(ctx, ctx->ev);
       // the particle count shrinks only at the next search
       PlumeStepLog& L = log[k];
-      L.dt = ctx->h_ts->dtime;
-      L.time = ctx->h_ts->time;
-      L.step = ctx->h_ts->step;
+      L.dt = ctx->h_ts[0].dtime;
+      L.time = ctx->h_ts[0].time;
+      L.step = ctx->h_ts[0].step;
       L.status = s;
       L.n_total = ctx->n_alloc;
-      L.n_real = ctx->h_ts->n_real;
-      L.n_lost = ctx->h_ts->n_lost;
+      L.n_real = 0;
+      L.n_lost = 0;
+      for (int m = 0; m < ctx->nmem; m++) {
+        L.n_real += ctx->h_ts[m].n_real;
+        L.n_lost += ctx->h_ts[m].n_lost;
+      }
       if (s) return s;
     }
   }
@@ -967,11 +1186,11 @@ int plume_adapt_sml(plume_ctx* ctx) {
   const int nb = nblocks(ctx->n_alloc ? ctx->n_alloc : 1);
   const bool mixed = ctx->opt.precision == PLUME_PREC_MIXED;
   if (ctx->o.dim == 3) {
-    if (mixed) k_adaptive<3, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
-    else k_adaptive<3, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    if (mixed) k_adaptive<3, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts, ctx->d_hstep, 1);
+    else k_adaptive<3, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts, ctx->d_hstep, 1);
   } else {
-    if (mixed) k_adaptive<1, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
-    else k_adaptive<1, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
+    if (mixed) k_adaptive<1, float><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts, ctx->d_hstep, 1);
+    else k_adaptive<1, double><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts, ctx->d_hstep, 1);
   }
   CK(cudaGetLastError());
   return ctx_sync_status(ctx);
@@ -1041,7 +1260,7 @@ int plume_download(plume_ctx* ctx, PlumeSoA* host, size_t cap, size_t* n) {
 int plume_get_time(plume_ctx* ctx, double* time, int* step, int* ioutput) {
   if (!ctx) return PLUME_E_INVALID;
   CK(cudaStreamSynchronize(ctx->st));
-  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyDeviceToHost));
   if (time) *time = ctx->h_ts->time;
   if (step) *step = ctx->h_ts->step;
   if (ioutput) *ioutput = ctx->h_ts->ioutput;
@@ -1051,12 +1270,15 @@ int plume_get_time(plume_ctx* ctx, double* time, int* step, int* ioutput) {
 int plume_set_time(plume_ctx* ctx, double time, int step, int ioutput, double next_output) {
   if (!ctx) return PLUME_E_INVALID;
   CK(cudaStreamSynchronize(ctx->st));
-  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
-  ctx->h_ts->time = time;
-  ctx->h_ts->step = step;
-  ctx->h_ts->ioutput = ioutput;
-  ctx->h_ts->ndtimeoutput = next_output;
-  CK(cudaMemcpy(ctx->ts, ctx->h_ts, sizeof(TimeState), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyDeviceToHost));
+  for (int m = 0; m < ctx->nmem; m++) {  // every member of an ensemble
+    ctx->h_ts[m].time = time;
+    ctx->h_ts[m].step = step;
+    ctx->h_ts[m].ioutput = ioutput;
+    ctx->h_ts[m].ndtimeoutput = next_output;
+  }
+  CK(cudaMemcpy(ctx->ts, ctx->h_ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_hstep, &step, sizeof(int), cudaMemcpyHostToDevice));
   ctx->host_step = step;
   return PLUME_OK;
 }
@@ -1081,9 +1303,9 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
   cudaStream_t st = ctx->st;
   const int nb = nblocks(np ? np : 1);
   if (ctx->o.dim == 3)
-    k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+    k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
   else
-    k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+    k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
   unsigned long long total = 0;
   if (np) {
     k_scan_blocks<<<nbk, 1024, 0, st>>>(cnt, np, offs, sums);
@@ -1098,9 +1320,9 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
     CK(cudaMalloc(&dki, 8 * total));
     CK(cudaMalloc(&dkj, 8 * total));
     if (ctx->o.dim == 3)
-      k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+      k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
     else
-      k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->g, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+      k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
     CK(cudaMemcpyAsync(key_i, dki, 8 * total, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(key_j, dkj, 8 * total, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1113,6 +1335,152 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
   cudaFree(tot);
   CK(cudaGetLastError());
   return PLUME_OK;
+}
+
+// ---------------------------------------------------------------- ensembles
+int plume_batch_upload(plume_ctx* ctx, const PlumeSoA* host, const uint16_t* member, size_t n) {
+  if (!ctx || !member) return PLUME_E_INVALID;
+  if (n > ctx->cap) {
+    ctx->err = "particle count exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  int rc = copy_soa(ctx, host, 0, n, cudaMemcpyHostToDevice, member);
+  if (rc) return rc;
+  rc = set_count(ctx, n);
+  if (rc) return rc;
+  ctx->pending_dead = true;
+  return PLUME_OK;
+}
+
+int plume_batch_append(plume_ctx* ctx, const PlumeSoA* host, const uint16_t* member, size_t n) {
+  if (!ctx || !member) return PLUME_E_INVALID;
+  if (ctx->n_alloc + n > ctx->cap) {
+    ctx->err = "append exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  int rc = copy_soa(ctx, host, ctx->n_alloc, n, cudaMemcpyHostToDevice, member);
+  if (rc) return rc;
+  rc = set_count(ctx, ctx->n_alloc + n);
+  ctx->pending_dead = true;
+  return rc;
+}
+
+int plume_batch_download(plume_ctx* ctx, PlumeSoA* host, uint16_t* member, size_t cap, size_t* n) {
+  int rc = plume_download(ctx, host, cap, n);
+  if (rc) return rc;
+  if (member && *n) {
+    CK(cudaMemcpy(member, ctx->A.mem, 2 * (*n), cudaMemcpyDeviceToHost));
+  }
+  return PLUME_OK;
+}
+
+// TimeProps::ifend (properties.h:76-79) of member m, or its error status,
+// from the host mirror
+static bool member_ended(const plume_ctx* ctx, int m) {
+  const TimeState& t = ctx->h_ts[m];
+  const Opt& o = ctx->hopt[m];
+  return (t.time >= o.max_time) || (t.step > o.max_steps) || (ctx->batch && t.status != 0);
+}
+
+int plume_batch_time(plume_ctx* ctx, double* time, int* step, int* running, int* status) {
+  if (!ctx) return PLUME_E_INVALID;
+  CK(cudaStreamSynchronize(ctx->st));
+  CK(cudaMemcpy(ctx->h_ts, ctx->ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyDeviceToHost));
+  for (int m = 0; m < ctx->nmem; m++) {
+    if (time) time[m] = ctx->h_ts[m].time;
+    if (step) step[m] = ctx->h_ts[m].step;
+    if (running) running[m] = member_ended(ctx, m) ? 0 : 1;
+    if (status) status[m] = ctx->h_ts[m].status;
+  }
+  return PLUME_OK;
+}
+
+// captures k steps of the context's stream into one CUDA graph
+static int capture_steps(plume_ctx* ctx, int k) {
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  const int saved_step = ctx->host_step;
+  const unsigned long long saved_launches = ctx->launches;
+  ctx->capturing = true;
+  CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+  int rc = PLUME_OK;
+  for (int q = 0; q < k && rc == PLUME_OK; q++) rc = step_async(ctx);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
+  ctx->capturing = false;
+  ctx->host_step = saved_step;
+  ctx->glaunches = ctx->launches - saved_launches;
+  ctx->launches = saved_launches;
+  if (rc != PLUME_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    if (rc == PLUME_OK) ctx->err = std::string("stream capture: ") + cudaGetErrorString(e);
+    return rc != PLUME_OK ? rc : PLUME_E_CUDA;
+  }
+  e = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    ctx->gexec = nullptr;
+    ctx->err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+    return PLUME_E_CUDA;
+  }
+  ctx->gsteps = k;
+  ctx->gn = ctx->n_alloc;
+  return PLUME_OK;
+}
+
+int plume_batch_run(plume_ctx* ctx, int max_steps, int graph_steps, int* steps_done) {
+  if (!ctx || max_steps < 0 || graph_steps < 0) return PLUME_E_INVALID;
+  for (auto& v : ctx->phase_ms) v = 0;
+  ctx->launches = 0;
+  if (steps_done) *steps_done = 0;
+  for (auto& e : ctx->run_ev)
+    if (!e) CK(cudaEventCreate(&e));
+  int rc = ensure_events(ctx, 1);
+  if (rc) return rc;
+  ctx->ev = ctx->evs.data();
+  int s = ctx_sync_status(ctx);
+  if (s) return s;
+  // every member stops at its TimeProps::ifend inside the run
+  bool refreeze = false;
+  for (int m = 0; m < ctx->nmem; m++)
+    if (!ctx->h_ts[m].freeze) {
+      ctx->h_ts[m].freeze = 1;
+      refreeze = true;
+    }
+  if (refreeze) CK(cudaMemcpy(ctx->ts, ctx->h_ts, sizeof(TimeState) * ctx->nmem, cudaMemcpyHostToDevice));
+  bool any = false;
+  for (int m = 0; m < ctx->nmem; m++) any |= !member_ended(ctx, m);
+  int done = 0;
+  CK(cudaEventRecord(ctx->run_ev[0], ctx->st));
+  while (any && done < max_steps) {
+    const int k = graph_steps > 0 ? std::min(graph_steps, max_steps - done) : 1;
+    if (graph_steps > 0) {
+      if (!ctx->gexec || ctx->gsteps != k || ctx->n_alloc > ctx->gn) {
+        rc = capture_steps(ctx, k);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(ctx->gexec, ctx->st));
+      ctx->host_step += k;
+      ctx->launches += ctx->glaunches;
+    } else {
+      rc = step_async(ctx);
+      if (rc) return rc;
+    }
+    done += k;
+    s = finish_steps(ctx);
+    if (s) break;
+    any = false;
+    for (int m = 0; m < ctx->nmem; m++) any |= !member_ended(ctx, m);
+  }
+  CK(cudaEventRecord(ctx->run_ev[1], ctx->st));
+  CK(cudaEventSynchronize(ctx->run_ev[1]));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->run_ev[0], ctx->run_ev[1]);
+  ctx->phase_ms[10] = ms;
+  if (steps_done) *steps_done = done;
+  return s;
 }
 
 int plume_phase_times(plume_ctx* ctx, float* ms, int n) {

@@ -37,6 +37,7 @@ struct Opt {
   double ng0, cvs, cvg, cva, rg, ra, vent_z, sml2;
   double max_time, timeoutput, stat_erupt, end_erupt;
   double ksupport;  // kernel support in units of h (3 Gaussian box, 2 M4)
+  int max_steps;
 };
 
 struct Geo {
@@ -49,13 +50,19 @@ struct Geo {
   int G[3];   // fine cells per axis = nb * s
   int dim;
   double lo[3], hi[3];  // original domain (escape planes)
+  // place of the member's grid in the context's tables: its fine cells are
+  // [cell_base, cell_base + G0*G1*G2) of the cell-start table, its buckets
+  // [bucket_base, bucket_base + nbk) of the per-bucket tables
+  uint32_t cell_base;
+  int bucket_base, nbk;
 };
 
 struct Dev {  // particle arrays (one buffer set)
   uint64_t* key;
   double *x, *y, *z, *vx, *vy, *vz, *vsx, *vsy, *vsz, *mass, *h, *rho, *e, *p, *Y, *gam, *c, *T, *cp;
   uint8_t *phase, *bc, *inv;
-  int32_t* bkt;  // linear bucket id at the last search
+  int32_t* bkt;   // member-local linear bucket id at the last search
+  uint16_t* mem;  // ensemble member of the particle (0 for a single run)
 };
 
 struct Work {  // per-step scratch arrays (sorted order)
@@ -72,6 +79,8 @@ struct TimeState {  // TimeProps on the device, properties.h:17-83
   int erupt;                      // iferupt() after incrtime
   unsigned long long n_lost;
   unsigned long long n_real;
+  int active;  // the member steps (false once it reached TimeProps::ifend when frozen)
+  int freeze;  // stop the member at ifend (ensembles); single runs step on
 };
 
 __device__ __forceinline__ void set_status(TimeState* ts, int code) { atomicCAS(&ts->status, 0, code); }
@@ -109,10 +118,14 @@ __device__ __forceinline__ float w_gauss<3, float>(const float* s, float h) {
   float expt = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
   return r * r * r * __expf(-expt);
 }
+// 1D: accurate expf and division.  The 1D sweeps are cheap, and the
+// particles next to the tube-end ghosts amplify per-step errors by orders of
+// magnitude, so the fast exponential's error (up to ~1e-6 relative at
+// |s| = 3) is not worth its saving there.
 template <>
 __device__ __forceinline__ float w_gauss<1, float>(const float* s, float h) {
   if (fabsf(s[0]) > 3.0f) return 0.0f;
-  return (float(T1_INV_SQRT_PI) * __fdividef(1.0f, h)) * __expf(-s[0] * s[0]);
+  return (float(T1_INV_SQRT_PI) / h) * expf(-s[0] * s[0]);
 }
 // cubic B-spline, radial support 2h
 template <int D, typename T>

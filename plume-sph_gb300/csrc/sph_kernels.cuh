@@ -10,6 +10,12 @@
 // segment.  A candidate j is in the reference's neighbour list of i iff it
 // is in the own bucket (neighs.cc:89-92) or inside the list_factor * h_i box
 // (neighs.cc:84,128-131), with h_i the smoothing length at the search.
+//
+// Ensembles: every particle carries its member id; a kernel reads the
+// member's grid (Geo), time state and options from per-member tables and
+// indexes the cell-start and per-bucket tables from the member's bases, so
+// that members never see each other's particles and a member computes what
+// it would compute alone.
 #pragma once
 #include "sph_device.cuh"
 
@@ -133,12 +139,20 @@ __device__ __forceinline__ bool in_box(const T* dx, T r) {
 // ---------------------------------------------------------------- adaptive
 // adaptive_sml (neighs.cc:479-693, ADAPTIVE_SML 1): up to num_loop fixed-point
 // iterations h <- eta * (m / rho*)^(1/D), rho* = sum m_j W(dx / 2h, 2h)
+// Runs on the steps with hstep % interval == 0 unless forced.
 template <int D, typename T>
-__global__ void k_adaptive(Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
-                           const int* __restrict__ d_count, TimeState* ts) {
+__global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                           const int* __restrict__ d_count, TimeState* ts_all, const int* __restrict__ hstep,
+                           int force) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
+  if (!force && (*hstep % o.interval) != 0) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Geo g = geo[m];
+  const uint32_t* cs = cs_all + g.cell_base;
   double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
   bucket_coords<D>(g, A.bkt[i], bi);
@@ -185,11 +199,18 @@ __global__ void k_adaptive(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
 // ---------------------------------------------------------------- momentum
 // mom_engr_update, USE_GSPH == 0 (mom_engr_update.cc:96-354)
 template <int D, typename T>
-__global__ void k_momentum(Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
-                           const double* __restrict__ hmax, const int* __restrict__ d_count, TimeState* ts) {
+__global__ void k_momentum(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                           const double* __restrict__ hmax_all, const int* __restrict__ d_count,
+                           TimeState* ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Geo g = geo[m];
+  const uint32_t* cs = cs_all + g.cell_base;
+  const double* hmax = hmax_all + g.bucket_base;
   const double dt = ts->dtime;
   double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
@@ -320,10 +341,14 @@ __global__ void k_momentum(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
 
 // commit loop of mom_engr_update.cc:412-432
 template <int D>
-__global__ void k_commit_mom(Opt o, Dev A, Work W, const int* __restrict__ d_count) {
+__global__ void k_commit_mom(const Opt* __restrict__ mopt, Dev A, Work W, const int* __restrict__ d_count,
+                             const TimeState* __restrict__ ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  if (!ts_all[m].active) return;
+  const Opt& o = mopt[m];
   A.vx[i] = W.nv0[i];
   if (D == 3) { A.vy[i] = W.nv1[i]; A.vz[i] = W.nv2[i]; }
   double e = W.ne[i];
@@ -337,11 +362,18 @@ __global__ void k_commit_mom(Opt o, Dev A, Work W, const int* __restrict__ d_cou
 // smooth_density (density_massfrac.cc:64-333), DENSITY_UPDATE_SML 11,
 // DENSITY_UPDATE_SPH 11, optional normalised energy smoothing
 template <int D, typename T>
-__global__ void k_density(Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
-                          const double* __restrict__ hmax, const int* __restrict__ d_count, TimeState* ts) {
+__global__ void k_density(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                          const double* __restrict__ hmax_all, const int* __restrict__ d_count,
+                          TimeState* ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Geo g = geo[m];
+  const uint32_t* cs = cs_all + g.cell_base;
+  const double* hmax = hmax_all + g.bucket_base;
   double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
   const int b = A.bkt[i];
@@ -409,10 +441,14 @@ __global__ void k_density(Opt o, Geo g, Dev A, Work W, const uint32_t* __restric
 
 // commit loop of density_massfrac.cc:337-352
 template <int D>
-__global__ void k_commit_dens(Opt o, Dev A, Work W, const int* __restrict__ d_count) {
+__global__ void k_commit_dens(const Opt* __restrict__ mopt, Dev A, Work W, const int* __restrict__ d_count,
+                              const TimeState* __restrict__ ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  if (!ts_all[m].active) return;
+  const Opt& o = mopt[m];
   double Y = W.nY[i];
   A.Y[i] = Y;
   if (Y >= MSFRC_TH && A.inv[i] != 2) A.inv[i] = 2;
@@ -431,11 +467,16 @@ __global__ void k_commit_dens(Opt o, Dev A, Work W, const int* __restrict__ d_co
 // ---------------------------------------------------------------- velocity
 // smooth_velocity (smooth_velocity.cc:25-165), HAVE_TURBULENCE_LANS 1
 template <int D, typename T>
-__global__ void k_velocity(Opt o, Geo g, Dev A, Work W, const uint32_t* __restrict__ cs,
-                           const int* __restrict__ d_count, TimeState* ts) {
+__global__ void k_velocity(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                           const int* __restrict__ d_count, TimeState* ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!need_neigh(A.bc[i])) return;
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Geo g = geo[m];
+  const uint32_t* cs = cs_all + g.cell_base;
   double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
   bucket_coords<D>(g, A.bkt[i], bi);
@@ -488,10 +529,18 @@ __global__ void k_velocity(Opt o, Geo g, Dev A, Work W, const uint32_t* __restri
 // update_pos (update_pos.cc:34-168) and the deletions of
 // update_particles_in_bucket (update_pos.cc:171-463, serial case)
 template <int D>
-__global__ void k_update_pos(Opt o, Geo g, Dev A, const uint8_t* __restrict__ bflags,
-                             const int8_t* __restrict__ bface, const int* __restrict__ d_count, TimeState* ts) {
+__global__ void k_update_pos(const Opt* __restrict__ mopt, const Geo* __restrict__ geo, Dev A,
+                             const uint8_t* __restrict__ bflags_all, const int8_t* __restrict__ bface_all,
+                             const int* __restrict__ d_count, TimeState* ts_all) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
+  const int m = A.mem[i];
+  TimeState* ts = ts_all + m;
+  if (!ts->active) return;
+  const Opt& o = mopt[m];
+  const Geo g = geo[m];
+  const uint8_t* bflags = bflags_all ? bflags_all + g.bucket_base : nullptr;
+  const int8_t* bface = bface_all ? bface_all + 6 * (size_t)g.bucket_base : nullptr;
   uint8_t bc = A.bc[i];
   const double dt = ts->dtime;
   double pos[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};

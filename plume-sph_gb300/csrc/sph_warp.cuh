@@ -23,6 +23,18 @@ namespace plume {
 constexpr unsigned WFULL = 0xffffffffu;
 constexpr int WP_WARPS = 4;  // warps per block (128 threads)
 
+// Grid of a particle's member.  A single run (MULTI = false) reads its one
+// grid from the kernel parameters (constant bank, no registers held across
+// the pair loops); an ensemble (MULTI = true) reads the member's entry of
+// the per-member table.
+template <bool MULTI>
+struct Geos {
+  Geo g0;
+  const Geo* __restrict__ tab;
+  __device__ __forceinline__ int member(const Dev& A, int i) const { return MULTI ? (int)A.mem[i] : 0; }
+  __device__ __forceinline__ const Geo& of(int m) const { return MULTI ? tab[m] : g0; }
+};
+
 // packed FP32 records of the mixed path (one set, rewritten per sweep)
 struct Packed {
   float4* P;  // (xr, yr, zr, h or -h when the particle does not contribute)
@@ -319,7 +331,7 @@ __device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& mj, float
 
 // momentum record: P (xr,yr,zr,h), Q (m, rho, 1/rho, p/rho^2), R (c,T,cp,vx),
 // S (vy,vz); the quotients are formed in FP64 once per particle
-__global__ void k_pack_mom(Geo g, Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
+__global__ void k_pack_mom(Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
   const double rho = A.rho[j], V = 1.0 / rho;
@@ -542,11 +554,11 @@ __global__ void k_pack_vel(Dev A, Packed K, Work W, const int* __restrict__ d_co
 // ------------------------------------------------------------ driver kernel
 // WARP = true: one warp per particle with ballot compaction (wp_walk);
 // WARP = false: one thread per particle walking its own rows.
-template <typename T, template <typename> class SW, bool WARP>
-__global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Packed K,
-                                                const uint32_t* __restrict__ cs,
-                                                const double* __restrict__ hmax,
-                                                const int* __restrict__ d_count, TimeState* ts) {
+template <typename T, template <typename> class SW, bool WARP, bool MULTI>
+__global__ void __launch_bounds__(128) k_sweep3(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                const uint32_t* __restrict__ cs_all,
+                                                const double* __restrict__ hmax_all,
+                                                const int* __restrict__ d_count, TimeState* ts_all) {
   const int n = *d_count;
   if (WARP) {
     __shared__ WBuf<T> bufs[WP_WARPS];
@@ -554,6 +566,12 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Pac
     const int nw = gridDim.x * WP_WARPS;
     for (int i = blockIdx.x * WP_WARPS + (threadIdx.x >> 5); i < n; i += nw) {
       if (!need_neigh(A.bc[i])) continue;
+      const int m = geo.member(A, i);
+      TimeState* ts = ts_all + m;
+      if (!ts->active) continue;
+      const Geo& g = geo.of(m);
+      const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+      const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
       SW<T> s(A, K, o);
       double xi[3], R;
       int bi[3];
@@ -564,6 +582,12 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geo g, Dev A, Work W, Pac
   } else {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !need_neigh(A.bc[i])) return;
+    const int m = geo.member(A, i);
+    TimeState* ts = ts_all + m;
+    if (!ts->active) return;
+    const Geo& g = geo.of(m);
+    const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+    const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
     SW<T> s(A, K, o);
     double xi[3], R;
     int bi[3];
@@ -636,17 +660,22 @@ __device__ __forceinline__ void decode_offsets(T delT, int code, bool& own, T& o
 }
 
 // union filter of the momentum, density and velocity sweeps
-template <typename T>
-__global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W, Packed K,
-                                                     const uint32_t* __restrict__ cs,
-                                                     const double* __restrict__ hmax,
-                                                     const int* __restrict__ d_count, NList L) {
+template <typename T, bool MULTI>
+__global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                     const uint32_t* __restrict__ cs_all,
+                                                     const double* __restrict__ hmax_all,
+                                                     const int* __restrict__ d_count,
+                                                     const TimeState* __restrict__ ts_all, NList L) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
-  if (!need_neigh(A.bc[i])) {
+  const int m = geo.member(A, i);
+  if (!need_neigh(A.bc[i]) || !ts_all[m].active) {
     L.cnt[i] = 0;
     return;
   }
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
   const int b = A.bkt[i];
   int bi[3];
   bucket_coords<3>(g, b, bi);
@@ -711,16 +740,21 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geo g, Dev A, Work W
 // indices); particles whose list overflowed walk their rows.  The window and
 // bit loops are flattened so that every iteration hands each thread exactly
 // one pair (threads of a warp stay converged while they have pairs left).
-template <typename T, template <typename> class SW>
-__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geo g, Dev A, Work W, Packed K,
-                                                     const uint32_t* __restrict__ cs,
-                                                     const double* __restrict__ hmax,
+template <typename T, template <typename> class SW, bool MULTI>
+__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                     const uint32_t* __restrict__ cs_all,
+                                                     const double* __restrict__ hmax_all,
                                                      const int* __restrict__ d_real,
-                                                     const uint32_t* __restrict__ real_idx, TimeState* ts,
+                                                     const uint32_t* __restrict__ real_idx, TimeState* ts_all,
                                                      NList L) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= *d_real) return;
   const int i = (int)real_idx[r];
+  const int m = geo.member(A, i);  // real_idx holds particles of active members only
+  TimeState* ts = ts_all + m;
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
   SW<T> s(A, K, o);
   double xi[3], R;
   int bi[3];
@@ -758,11 +792,13 @@ __global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geo g, Dev A, Work W
   s.template finish<false>(i, W, ts);
 }
 
-// compacted indices of the need_neigh particles (sorted order kept)
-__global__ void k_real_flags(Dev A, const int* __restrict__ d_count, int n, unsigned int* __restrict__ flag) {
+// compacted indices of the need_neigh particles of the stepping members
+// (sorted order kept)
+__global__ void k_real_flags(Dev A, const int* __restrict__ d_count, int n, const TimeState* __restrict__ ts_all,
+                             unsigned int* __restrict__ flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  flag[i] = (i < *d_count && need_neigh(A.bc[i])) ? 1u : 0u;
+  flag[i] = (i < *d_count && need_neigh(A.bc[i]) && ts_all[A.mem[i]].active) ? 1u : 0u;
 }
 __global__ void k_real_scatter(const unsigned int* __restrict__ flag, const unsigned long long* __restrict__ offs,
                                int n, uint32_t* __restrict__ real_idx, int* __restrict__ d_real,

@@ -79,5 +79,12 @@ def lib():
         L.plume_version.restype = C.c_char_p
         L.plume_timestep_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
                                              C.c_double, C.c_void_p, C.c_void_p]
+        L.plume_batch_create.argtypes = [P(PlumeOptions), P(PlumeGrid), C.c_int, P(C.c_void_p)]
+        L.plume_batch_upload.argtypes = [C.c_void_p, P(PlumeSoA), P(C.c_uint16), C.c_size_t]
+        L.plume_batch_append.argtypes = [C.c_void_p, P(PlumeSoA), P(C.c_uint16), C.c_size_t]
+        L.plume_batch_download.argtypes = [C.c_void_p, P(PlumeSoA), P(C.c_uint16), C.c_size_t,
+                                           P(C.c_size_t)]
+        L.plume_batch_time.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int), P(C.c_int)]
+        L.plume_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_int)]
         _LIB = L
         return L

@@ -131,13 +131,14 @@ def options_1d(kernel=KERNEL_GAUSS, eta=1.0, cfl=0.1, cva=717.0, precision=PREC_
                    stat_erupt=0.0, end_erupt=7200.0)
 
 
-def _grid_1d(ps: ParticleSet, opt: Options, cells_per_h: float = 0.5) -> Grid:
+def _grid_1d(ps: ParticleSet, opt: Options, cells_per_h: float = 0.5, travel: float = 0.0) -> Grid:
     """A 1D cell grid over the particle span (tiling of the GPU sweeps only;
-    1D neighbour lists are every particle, add_air.cc:470-479)."""
+    1D neighbour lists are every particle, add_air.cc:470-479), padded by
+    `travel` for particles that move out of the initial span."""
     span_lo = float(ps.x.min())
     span_hi = float(ps.x.max())
     hmax = float(ps.h.max())
-    pad = 8.0 * max(hmax, (span_hi - span_lo) * 1e-3)
+    pad = 8.0 * max(hmax, (span_hi - span_lo) * 1e-3) + travel
     lo = span_lo - pad
     hi = span_hi + pad
     cell = max(hmax * cells_per_h, (hi - lo) / 2.0e6)
@@ -195,6 +196,45 @@ def shock_tube_1d(test: int = 1, s0: float = 0.003, kernel: int = KERNEL_GAUSS,
     opt.capacity = ps.n
     return Case("shock_tube_1d", opt, _grid_1d(ps, opt), ps, pre_adaptive=True,
                 info={"s0": s0})
+
+
+def riemann_member(rho_l, p_l, u_l, rho_r, p_r, u_r, n_real: int, ghosts: int = 10,
+                   kernel: int = KERNEL_GAUSS, precision: int = PREC_FP64,
+                   t_end: float = 0.2, name: str = "riemann") -> Case:
+    """One 1D Riemann problem on [0,1] split at 0.5 with equal-mass particles
+    (about n_real of them, h = 1.3 m/rho), ideal gas gamma = 1.4, alpha=1,
+    beta=2, CFL 0.3, `ghosts` ghosts per end, run to t_end: the Sod set-up
+    with other states.  The grid is padded for the ghosts' travel
+    (|u| t_end)."""
+    s0 = _f32(0.5 * (1.0 + rho_r / rho_l) / n_real)
+    ps = _shock_tube(rho_l, p_l, u_l, rho_r, p_r, u_r, 0.5, 0.0, 1.0, s0, ghosts, 0, 0, True)
+    opt = options_1d(kernel=kernel, eta=1.3, cfl=0.3, cva=717.5, precision=precision,
+                     max_time=t_end, timeoutput=t_end / 2)
+    opt.max_steps = 1 << 30
+    opt.capacity = ps.n
+    travel = 1.5 * max(abs(u_l), abs(u_r)) * t_end + 0.05
+    return Case(name, opt, _grid_1d(ps, opt, travel=travel), ps, pre_adaptive=True,
+                info={"s0": s0, "states": ((rho_l, p_l, u_l), (rho_r, p_r, u_r)),
+                      "n_real": int(ps.need_neigh().sum())})
+
+
+def riemann_ensemble(members: int = 256, seed: int = 1, n_lo: int = 500, n_hi: int = 8000,
+                     kernel: int = KERNEL_GAUSS, precision: int = PREC_FP64,
+                     t_end: float = 0.2) -> list:
+    """The 1D ensemble workload: `members` Riemann problems with real
+    particle counts log-uniform in [n_lo, n_hi] and left/right states drawn
+    from `seed` (rho in [0.1, 1], p in [0.01, 1], u in [-1, 1] per side)."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k in range(members):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        rl, rr = rng.uniform(0.1, 1.0, 2)
+        pl, pr = rng.uniform(0.01, 1.0, 2)
+        ul, ur = rng.uniform(-1.0, 1.0, 2)
+        cases.append(riemann_member(float(rl), float(pl), float(ul), float(rr), float(pr), float(ur),
+                                    n, kernel=kernel, precision=precision, t_end=t_end,
+                                    name=f"riemann_{k}"))
+    return cases
 
 
 # ----------------------------------------------------------------------------
@@ -385,3 +425,28 @@ def plume_small(seed=0, precision=PREC_FP64, subcells=4) -> Case:
 def plume_config2(seed=0, precision=PREC_FP64, subcells=4) -> Case:
     """The full 3D plume workload: 20 x 20 x 20 km at 150 m (134^3 air)."""
     return plume_3d(seed=seed, precision=precision, subcells=subcells, name="plume_3d_config2")
+
+
+def plume_ensemble(members: int = 64, seed: int = 2, dx: float = 60.0, n_lo: float = 5.0e4,
+                   n_hi: float = 4.0e5, precision: int = PREC_FP64, subcells: int = 4,
+                   vent_radius: float = 100.0, duct_depth: float | None = None) -> list:
+    """The 3D ensemble workload: `members` small copies of the plume at `dx`
+    spacing, each a cube whose side gives about N_k air particles, N_k
+    log-uniform in [n_lo, n_hi]; vent velocity U[80, 200] m/s, temperature
+    U[900, 1200] K and ash mass fraction U[0.9, 0.98] per member, drawn from
+    `seed` (the lattice jitter of member k uses seed + 1000 k)."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k in range(members):
+        n = math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))
+        side = dx * n ** (1.0 / 3.0)
+        v = float(rng.uniform(80.0, 200.0))
+        T = float(rng.uniform(900.0, 1200.0))
+        ash = float(rng.uniform(0.9, 0.98))
+        c = plume_3d(half_width=0.5 * side, height=side, dx=dx, vent_radius=vent_radius,
+                     vent_velocity=v, vent_T=T, ash=ash, duct_depth=duct_depth,
+                     seed=seed + 1000 * k, precision=precision, subcells=subcells,
+                     name=f"plume_member_{k}")
+        c.info.update({"vent_velocity": v, "vent_T": T, "ash": ash})
+        cases.append(c)
+    return cases

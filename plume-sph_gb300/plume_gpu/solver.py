@@ -14,7 +14,8 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .abi import (DOUBLE_FIELDS, STATUS_NAMES, ParticleSet, PlumeSoA, PlumeStepLog)
+from .abi import (DOUBLE_FIELDS, STATUS_NAMES, ParticleSet, PlumeGrid, PlumeOptions, PlumeSoA,
+                  PlumeStepLog)
 
 
 class PlumeError(RuntimeError):
@@ -146,13 +147,106 @@ class Solver:
         return ki, kj
 
     def phase_times(self):
-        ms = (C.c_float * 11)()
-        self._check(self.L.plume_phase_times(self.ctx, ms, 11), "plume_phase_times")
+        ms = (C.c_float * 12)()
+        self._check(self.L.plume_phase_times(self.ctx, ms, 12), "plume_phase_times")
         names = ["search", "adaptive", "lists", "momentum", "commit_mom", "density", "commit_dens",
-                 "velocity", "position", "dt", "total"]
+                 "velocity", "position", "dt", "total", "mom_kernel"]
         return dict(zip(names, list(ms)))
 
     def launches(self) -> int:
         n = C.c_uint64()
         self._check(self.L.plume_launch_count(self.ctx, C.byref(n)), "plume_launch_count")
         return int(n.value)
+
+
+class Ensemble(Solver):
+    """Independent runs (members) stepped together in one context.
+
+    `cases` are per-member `Case`s (options, grid, particles).  Members
+    share the options the sweeps read (kernel, switches, viscosity,
+    cut-offs); their grids, particles, mixture constants, end times and
+    time states are their own.  Particle keys are the members' own keys:
+    a downloaded row is identified by (member, key)."""
+
+    def __init__(self, cases):
+        self.cases = list(cases)
+        self.case = self.cases[0]
+        self.L = _lib.lib()
+        m = len(self.cases)
+        self._opts = (PlumeOptions * m)()
+        self._grids = (PlumeGrid * m)()
+        for k, c in enumerate(self.cases):
+            o = c.options.to_c()
+            if o.capacity == 0:
+                o.capacity = max(c.particles.n, 1)
+            self._opts[k] = o
+            self._grids[k] = c.grid.to_c()
+        self.nmem = m
+        self.ctx = C.c_void_p()
+        rc = self.L.plume_batch_create(self._opts, self._grids, m, C.byref(self.ctx))
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.L.plume_last_error(None, buf, 512)
+            raise PlumeError(rc, "plume_batch_create", buf.value.decode())
+        parts = [c.particles for c in self.cases]
+        members = np.concatenate([np.full(p.n, k, dtype=np.uint16) for k, p in enumerate(parts)])
+        self.upload_members(ParticleSet.concat(parts), members)
+
+    def upload_members(self, ps: ParticleSet, members):
+        members = np.ascontiguousarray(members, dtype=np.uint16)
+        s = ps.soa()
+        self._check(self.L.plume_batch_upload(self.ctx, C.byref(s),
+                                              members.ctypes.data_as(C.POINTER(C.c_uint16)), ps.n),
+                    "plume_batch_upload")
+
+    def append_members(self, ps: ParticleSet, members):
+        members = np.ascontiguousarray(members, dtype=np.uint16)
+        s = ps.soa()
+        self._check(self.L.plume_batch_append(self.ctx, C.byref(s),
+                                              members.ctypes.data_as(C.POINTER(C.c_uint16)), ps.n),
+                    "plume_batch_append")
+
+    def download_members(self):
+        """(ParticleSet in device order, member id of every row)"""
+        nt, _ = self.count()
+        ps = ParticleSet(nt)
+        mem = np.zeros(nt, dtype=np.uint16)
+        s = ps.soa()
+        n = C.c_size_t()
+        self._check(self.L.plume_batch_download(self.ctx, C.byref(s),
+                                                mem.ctypes.data_as(C.POINTER(C.c_uint16)), nt,
+                                                C.byref(n)), "plume_batch_download")
+        if n.value != nt:
+            ps, mem = ps.take(np.arange(n.value)), mem[:n.value]
+        return ps, mem
+
+    def split(self):
+        """per-member ParticleSets, rows sorted by key"""
+        ps, mem = self.download_members()
+        out = []
+        for k in range(self.nmem):
+            idx = np.nonzero(mem == k)[0]
+            sub = ps.take(idx)
+            out.append(sub.take(np.argsort(sub.key, kind="stable")))
+        return out
+
+    def member_times(self):
+        """(time, step, running, status) per member"""
+        t = np.zeros(self.nmem)
+        st = np.zeros(self.nmem, dtype=np.int32)
+        run = np.zeros(self.nmem, dtype=np.int32)
+        status = np.zeros(self.nmem, dtype=np.int32)
+        self._check(self.L.plume_batch_time(self.ctx, t.ctypes.data_as(C.POINTER(C.c_double)),
+                                            st.ctypes.data_as(C.POINTER(C.c_int)),
+                                            run.ctypes.data_as(C.POINTER(C.c_int)),
+                                            status.ctypes.data_as(C.POINTER(C.c_int))),
+                    "plume_batch_time")
+        return t, st, run.astype(bool), status
+
+    def run(self, max_steps: int, graph_steps: int = 0) -> int:
+        """steps every running member until all reached their end time (or
+        max_steps); graph_steps > 0 replays CUDA graphs of that many steps"""
+        done = C.c_int()
+        self._check(self.L.plume_batch_run(self.ctx, max_steps, graph_steps, C.byref(done)),
+                    "plume_batch_run")
+        return done.value
