@@ -18,6 +18,10 @@ need_neigh particles x steps / seconds.
   roofline  the momentum/energy sweep (dominant kernel)
   cpu_baseline  the CPU oracle (restatement of the reference path) on a
             bounded sample of the same workload, all host threads
+  ensembles the batched path (many members per launch, CUDA graphs):
+            256 1D Riemann problems (500-8,000 particles each, seed 1) and
+            64 small 3D plumes (60 m lattice, 5e4-4e5 air particles each,
+            seed 2), mixed and FP64, on a bounded number of steps
 
 `--impl reference` times the reference's CPU path (the oracle port: the
 reference's own build is x86-only and does not travel) on the host cores.
@@ -182,6 +186,90 @@ def cpu_sample(case, budget_s: float = 12.0, nthreads: int = 0):
     return nt2, t2
 
 
+def _member_l1(pa, pb, fa, fb):
+    """per-member relative L1 density error of b against a (members that
+    stopped on an error in either run are left out)"""
+    out = []
+    for k, (a, b) in enumerate(zip(pa, pb)):
+        if fa[k] or fb[k]:
+            continue
+        r = a.need_neigh()
+        out.append(float(np.abs(b.rho[r] - a.rho[r]).sum() / np.abs(a.rho[r]).sum()))
+    return np.array(out)
+
+
+def ensemble_1d(steps=400, warm=50, graph=50, members=256):
+    """The 1D ensemble: `members` Riemann problems stepped together; the mixed
+    run replays CUDA graphs of `graph` steps, the FP64 run the same.
+    Particle-steps count each member's real particles for the steps it took."""
+    from plume_gpu import PREC_FP64, PREC_MIXED, Ensemble, cases
+    res, parts = {}, {}
+    for prec in (PREC_MIXED, PREC_FP64):
+        cs = cases.riemann_ensemble(members, seed=1, precision=prec)
+        nreal = np.array([c.info["n_real"] for c in cs], dtype=np.float64)
+        e = Ensemble(cs)
+        e.adaptive_sml()
+        e.run(warm, graph_steps=graph)
+        st0 = e.member_times()[1]
+        n = e.run(steps, graph_steps=graph)
+        t = e.phase_times()["total"] / 1000.0
+        _, st1, run1, status = e.member_times()
+        ps = float((nreal * (st1 - st0)).sum())
+        res[prec] = {"value": ps / t, "unit": METRIC, "steps": n, "ms_per_step": 1000.0 * t / max(n, 1),
+                     "members_running": int(run1.sum()), "members_failed": int((status != 0).sum()),
+                     "launches": e.launches()}
+        parts[prec] = (e.split(), status != 0)
+        e.close()
+    err = _member_l1(parts[PREC_FP64][0], parts[PREC_MIXED][0], parts[PREC_FP64][1], parts[PREC_MIXED][1])
+    return {"workload": f"riemann1d_{members}_members_500_8000", "members": members,
+            "particles": int(sum(c.particles.n for c in cases.riemann_ensemble(members, seed=1))),
+            "graph_steps": graph, "warmup_steps": warm,
+            "mixed": res[PREC_MIXED], "fp64": res[PREC_FP64],
+            "mixed_over_fp64": res[PREC_MIXED]["value"] / res[PREC_FP64]["value"],
+            "l1_density_vs_fp64": {"after_steps": warm + steps, "members": int(len(err)),
+                                   "median": float(np.median(err)) if len(err) else None,
+                                   "max": float(err.max()) if len(err) else None,
+                                   "frac_le_1e-4": float((err <= 1e-4).mean()) if len(err) else None},
+            "note": "members stop where the reference asserts (sound speed or density <= 0 next to "
+                    "the moving tube-end ghosts); particles next to those ghosts amplify per-step "
+                    "differences, so late errors grow on some members (one-step error ~1e-7)"}
+
+
+def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
+    """The 3D ensemble: `members` small plumes (60 m lattice) stepped
+    together, mixed with CUDA graphs of `steps` steps; FP64 for a few steps."""
+    from plume_gpu import PREC_FP64, PREC_MIXED, Ensemble, cases
+    out = {}
+    cs = cases.plume_ensemble(members, seed=2, precision=PREC_MIXED)
+    n_air = int(sum(c.info["n_air"] for c in cs))
+    n_all = int(sum(c.particles.n for c in cs))
+    e = Ensemble(cs)
+    e.run(warm, graph_steps=steps)
+    _, nr0 = e.count()
+    n = e.run(steps, graph_steps=steps)
+    t = e.phase_times()["total"] / 1000.0
+    _, nr1 = e.count()
+    status = e.member_times()[3]
+    out["mixed"] = {"value": 0.5 * (nr0 + nr1) * n / t, "unit": METRIC, "steps": n,
+                    "ms_per_step": 1000.0 * t / n, "members_failed": int((status != 0).sum()),
+                    "launches": e.launches()}
+    e.close()
+    del cs
+    cs = cases.plume_ensemble(members, seed=2, precision=PREC_FP64)
+    e = Ensemble(cs)
+    e.run(1)
+    _, nr0 = e.count()
+    n = e.run(fp64_steps)
+    t = e.phase_times()["total"] / 1000.0
+    _, nr1 = e.count()
+    out["fp64"] = {"value": 0.5 * (nr0 + nr1) * n / t, "unit": METRIC, "steps": n,
+                   "ms_per_step": 1000.0 * t / n}
+    e.close()
+    return {"workload": f"plume3d_{members}_members_60m", "members": members, "n_air": n_air,
+            "particles": n_all, "graph_steps": steps, **out,
+            "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
+
+
 def run_reference(args, dist, rank, ws):
     """--impl reference: the reference CPU path (oracle port) on host cores"""
     if rank != 0:
@@ -225,6 +313,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true", help="test-size workload")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, rank, ws = dist_init()
@@ -346,6 +435,18 @@ def main():
         except Exception as e:  # the oracle is optional on the box
             cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
+    ens = None
+    if not args.no_ensemble and not args.small:
+        ens = {}
+        try:
+            ens["riemann1d"] = ensemble_1d()
+        except Exception as e:
+            ens["riemann1d"] = {"failed": str(e)}
+        try:
+            ens["plume3d"] = ensemble_3d()
+        except Exception as e:
+            ens["plume3d"] = {"failed": str(e)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -372,6 +473,7 @@ def main():
                                   "pairs_per_launch": npairs,
                                   "flop_per_pair": MOM_FLOP_PER_PAIR}},
             "cpu_baseline": cpu,
+            "ensembles": ens,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -85,10 +85,12 @@ def _shock_tube(rho_l, p_l, u_l, rho_r, p_r, u_r, middle, lo, hi, s0, nb, nnsrp_
         d = rho_at(x)
         rows.append((x, d * dx_l, smlen, d, u_at(x), p_at(x), BC_REAL, 2))
         x += dx_l
+    # right-state particles from one right spacing after the last left one
+    # (with rho_l < rho_r the first of them can sit just left of `middle`;
+    # it still carries the right state, so every real has the same mass)
     x = x - dx_l + dx_r
     while x <= hi:
-        d = rho_at(x)
-        rows.append((x, d * dx_r, smlen, d, u_at(x), p_at(x), BC_REAL, 2))
+        rows.append((x, rho_r * dx_r, smlen, rho_r, u_r, p_r, BC_REAL, 2))
         x += dx_r
     for k in range(nnsrp_r):
         d = rho_at(x)

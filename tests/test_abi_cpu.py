@@ -108,3 +108,41 @@ def test_config2_size():
     c = cases.plume_config2()
     air = int(c.particles.need_neigh().sum())
     assert 2.3e6 < air < 2.5e6
+
+
+def test_riemann_ensemble_builder():
+    a = cases.riemann_ensemble(256, seed=1)
+    b = cases.riemann_ensemble(256, seed=1)
+    n = np.array([c.info["n_real"] for c in a])
+    assert len(a) == 256 and n.min() >= 480 and n.max() <= 8100
+    # log-uniform counts: about half the members below the geometric mean
+    assert 0.35 < (n < np.sqrt(500 * 8000)).mean() < 0.65
+    for ca, cb in zip(a, b):
+        assert ca.info["states"] == cb.info["states"]
+        (rl, pl, ul), (rr, pr, ur) = ca.info["states"]
+        assert 0.1 <= min(rl, rr) and max(rl, rr) <= 1.0
+        assert 0.01 <= min(pl, pr) and max(pl, pr) <= 1.0
+        assert -1.0 <= min(ul, ur) and max(ul, ur) <= 1.0
+        ps = ca.particles
+        r = ps.need_neigh()
+        np.testing.assert_allclose(ps.mass[r], ps.mass[r][0], rtol=1e-6)  # equal mass
+        # the grid covers the ghosts' travel to t_end
+        g = ca.grid
+        lo, hi = g.mindom[0], g.mindom[0] + g.nb[0] * g.del_
+        reach = max(abs(ul), abs(ur)) * ca.options.max_time
+        assert lo < ps.x.min() - reach and hi > ps.x.max() + reach
+
+
+def test_plume_ensemble_builder():
+    cs = cases.plume_ensemble(6, seed=2, dx=60.0, n_lo=2.0e3, n_hi=2.0e4, duct_depth=300.0)
+    for c in cs:
+        assert 80.0 <= c.info["vent_velocity"] <= 200.0
+        assert 900.0 <= c.info["vent_T"] <= 1200.0
+        assert 0.9 <= c.info["ash"] <= 0.98
+        assert abs(c.options.ng0 - (1.0 - c.info["ash"])) < 1e-12
+        assert 1.0e3 <= c.info["n_air"] <= 4.0e4
+        assert c.options.capacity >= c.particles.n
+    # the shared options are equal across members (the batch create checks it)
+    keys = ["dim", "precision", "kernel", "lans", "alpha", "beta", "cutoff2", "list_factor"]
+    for k in keys:
+        assert len({getattr(c.options, k) for c in cs}) == 1, k
