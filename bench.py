@@ -204,8 +204,14 @@ def ensemble_1d(steps=400, warm=50, graph=50, members=256):
     Particle-steps count each member's real particles for the steps it took."""
     from plume_gpu import PREC_FP64, PREC_MIXED, Ensemble, cases
     res, parts = {}, {}
-    for prec in (PREC_MIXED, PREC_FP64):
-        cs = cases.riemann_ensemble(members, seed=1, precision=prec)
+    for prec in (PREC_MIXED, PREC_FP64, "fp64_perturbed"):
+        cs = cases.riemann_ensemble(members, seed=1,
+                                    precision=PREC_FP64 if prec == "fp64_perturbed" else prec)
+        if prec == "fp64_perturbed":
+            # FP64 from positions moved by one FP32 rounding (2^-24 relative):
+            # the spread an FP32-size change of the state alone produces
+            for c in cs:
+                c.particles.x[:] = c.particles.x * (1.0 + 2.0 ** -24)
         nreal = np.array([c.info["n_real"] for c in cs], dtype=np.float64)
         e = Ensemble(cs)
         e.adaptive_sml()
@@ -221,6 +227,8 @@ def ensemble_1d(steps=400, warm=50, graph=50, members=256):
         parts[prec] = (e.split(), status != 0)
         e.close()
     err = _member_l1(parts[PREC_FP64][0], parts[PREC_MIXED][0], parts[PREC_FP64][1], parts[PREC_MIXED][1])
+    ctl = _member_l1(parts[PREC_FP64][0], parts["fp64_perturbed"][0], parts[PREC_FP64][1],
+                     parts["fp64_perturbed"][1])
     return {"workload": f"riemann1d_{members}_members_500_8000", "members": members,
             "particles": int(sum(c.particles.n for c in cases.riemann_ensemble(members, seed=1))),
             "graph_steps": graph, "warmup_steps": warm,
@@ -230,6 +238,10 @@ def ensemble_1d(steps=400, warm=50, graph=50, members=256):
                                    "median": float(np.median(err)) if len(err) else None,
                                    "max": float(err.max()) if len(err) else None,
                                    "frac_le_1e-4": float((err <= 1e-4).mean()) if len(err) else None},
+            "l1_density_fp64_fp32_perturbed_vs_fp64": {
+                "members": int(len(ctl)), "median": float(np.median(ctl)) if len(ctl) else None,
+                "max": float(ctl.max()) if len(ctl) else None,
+                "frac_le_1e-4": float((ctl <= 1e-4).mean()) if len(ctl) else None},
             "note": "members stop where the reference asserts (sound speed or density <= 0 next to "
                     "the moving tube-end ghosts); particles next to those ghosts amplify per-step "
                     "differences, so late errors grow on some members (one-step error ~1e-7)"}
