@@ -251,8 +251,13 @@ def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
     """The 3D ensemble: `members` small plumes (60 m lattice) stepped
     together, mixed with CUDA graphs of `steps` steps; FP64 for a few steps."""
     from plume_gpu import PREC_FP64, PREC_MIXED, Ensemble, cases
+    from plume_gpu.autotune import tune_ensemble, with_subcells
     out = {}
     cs = cases.plume_ensemble(members, seed=2, precision=PREC_MIXED)
+    t0 = time.perf_counter()
+    cs, tuning = tune_ensemble(cs, candidates=(2, 3, 4, 5, 6), classes=3, steps=3)
+    tuning["seconds"] = time.perf_counter() - t0
+    tiles = [c.grid.subcells for c in cs]
     n_air = int(sum(c.info["n_air"] for c in cs))
     n_all = int(sum(c.particles.n for c in cs))
     e = Ensemble(cs)
@@ -267,7 +272,8 @@ def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
                     "launches": e.launches()}
     e.close()
     del cs
-    cs = cases.plume_ensemble(members, seed=2, precision=PREC_FP64)
+    cs = [with_subcells(c, s) for c, s in
+          zip(cases.plume_ensemble(members, seed=2, precision=PREC_FP64), tiles)]
     e = Ensemble(cs)
     e.run(1)
     _, nr0 = e.count()
@@ -278,8 +284,16 @@ def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
                    "ms_per_step": 1000.0 * t / n}
     e.close()
     return {"workload": f"plume3d_{members}_members_60m", "members": members, "n_air": n_air,
-            "particles": n_all, "graph_steps": steps, **out,
+            "particles": n_all, "graph_steps": steps, "autotune": tuning, **out,
             "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
+
+
+def small_plume(prec):
+    """the test-size workload of --small (4 km tall plume at 50 m)"""
+    from plume_gpu import cases
+    return cases.plume_3d(half_width=2000.0, height=4000.0, dx=50.0, vent_radius=50.0,
+                          vent_dx=25.0, duct_depth=600.0, seed=0, precision=prec,
+                          name="plume_small_bench")
 
 
 def run_reference(args, dist, rank, ws):
@@ -287,7 +301,7 @@ def run_reference(args, dist, rank, ws):
     if rank != 0:
         return 0
     from plume_gpu import cases
-    case = cases.plume_config2(seed=0)
+    case = small_plume(0) if args.small else cases.plume_config2(seed=0)
     ncores = os.cpu_count() or 1
     vals = []
     nt = None
@@ -305,7 +319,8 @@ def run_reference(args, dist, rank, ws):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * case.particles.need_neigh().sum() / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "n_air": int(case.particles.need_neigh().sum()),
+        "data": "synthetic", "config": {"workload": WORKLOAD if not args.small else "plume3d_small",
+                                         "n_air": int(case.particles.need_neigh().sum()),
                                          "inputs": "host memory"},
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": ncores, "kind": "port",
                          "sample": f"{nt} air particles per step (neighbour lists + all sweeps), "
@@ -326,6 +341,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true", help="test-size workload")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
+    ap.add_argument("--no-tune", action="store_true", help="fixed cell tiles (4^3 per bucket)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, rank, ws = dist_init()
@@ -344,12 +360,18 @@ def main():
 
     def make(prec):
         if args.small:
-            return cases.plume_3d(half_width=2000.0, height=4000.0, dx=50.0, vent_radius=50.0,
-                                  vent_dx=25.0, duct_depth=600.0, seed=0, precision=prec,
-                                  name="plume_small_bench")
+            return small_plume(prec)
         return cases.plume_config2(seed=0, precision=prec)
 
     case = make(PREC_MIXED)
+    tuning = None
+    from plume_gpu.autotune import tune_subcells, with_subcells
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        best, table = tune_subcells(case, candidates=(3, 4, 5, 6), steps=3, warmup=2)
+        tuning = {"subcells": best, "ms_per_step": {str(k): round(v, 3) for k, v in table.items()},
+                  "seconds": time.perf_counter() - t0}
+        case = with_subcells(case, best)
     n_air0 = int(case.particles.need_neigh().sum())
     sol = Solver(case)
     # warm-up (not timed)
@@ -423,7 +445,7 @@ def main():
     # FP64 path on the same workload (shorter)
     fp64 = None
     if not args.no_fp64:
-        c64 = make(PREC_FP64)
+        c64 = with_subcells(make(PREC_FP64), case.grid.subcells)
         s64 = Solver(c64)
         s64.steps(3)
         k64 = max(2, min(args.steps, 3))
@@ -468,7 +490,8 @@ def main():
             "config": {"workload": WORKLOAD if not args.small else "plume3d_small",
                        "n_air": n_air0, "n_particles": int(case.particles.n),
                        "precision": "fp32 pair arithmetic, fp64 positions and updates",
-                       "parallelism": f"replicas{ws}", "l2": "working set > L2 (state ~0.6 GB)"},
+                       "parallelism": f"replicas{ws}", "l2": "working set > L2 (state ~0.6 GB)",
+                       "subcells": int(case.grid.subcells), "autotune": tuning},
             "gpu_launches": launches,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
             "clocks": clk.summary(),

@@ -205,3 +205,23 @@ def test_status_on_nonpositive_sound_speed():
     ok = cases.sod_1d(n_real=200)
     s.upload(ok.particles)
     s.step()
+
+
+@pytest.mark.parametrize("subcells", [2, 3, 6])
+def test_every_cell_tile_matches_oracle(subcells):
+    # the autotuner may pick any fine-cell size: each must keep FP64 parity
+    from plume_gpu.autotune import tune_subcells, with_subcells
+    case = with_subcells(cases.plume_small(seed=0), subcells)
+    case.step0 = 49
+    s = Solver(case)
+    s.steps(2)
+    o = OracleRun(case)
+    o.steps(2)
+    _check_fields(s.download(), o.ps, FP64_TOL)
+
+
+def test_autotuner_returns_a_measured_candidate():
+    from plume_gpu.autotune import tune_subcells
+    best, table = tune_subcells(cases.plume_small(seed=0, precision=PREC_MIXED),
+                                candidates=(2, 4), steps=2, warmup=1)
+    assert set(table) == {2, 4} and best in table and all(v > 0 for v in table.values())
