@@ -294,6 +294,29 @@ int plume_batch_download(plume_ctx *ctx, PlumeSoA *host, uint16_t *member, size_
 int plume_batch_time(plume_ctx *ctx, double *time, int *step, int *running, int *status);
 int plume_batch_run(plume_ctx *ctx, int max_steps, int graph_steps, int *steps_done);
 
+/* ---------------------------------------------------------------- adjoint
+ * Reverse-mode derivatives of a window of particle steps (one 3D run, FP64,
+ * Gaussian kernel).  No counterpart in the reference.
+ *
+ * plume_adjoint_record: runs nsteps steps like plume_steps and keeps the
+ *   state every checkpoint_every steps (and at the end).
+ * plume_adjoint_backward: given the adjoint of a scalar objective J with
+ *   respect to the window's final state (final_bar: rows matched by key to
+ *   the particles alive at the end; PlumeSoA fields x .. cp, gamma ignored,
+ *   NULL arrays = zero), returns dJ/d(first state) in initial_bar (rows in
+ *   the order of the window's first state, keys filled; cap >= its row
+ *   count, returned in n_initial) and dJ/d ng0 (the mixture constant of the
+ *   EOS).  Each checkpoint segment is recomputed with per-step snapshots and
+ *   differentiated stage by stage (position, LANS filter, density + EOS,
+ *   momentum/energy, adaptive h, dt).  The discrete decisions of the
+ *   recorded run are kept: neighbour lists, the particle that sets dt,
+ *   erupt-to-real conversions, deletions; a dt clipped to an output or end
+ *   time inside the window is rejected (PLUME_E_INVALID).  After the call
+ *   the context holds the window's final state again. */
+int plume_adjoint_record(plume_ctx *ctx, int nsteps, int checkpoint_every);
+int plume_adjoint_backward(plume_ctx *ctx, const PlumeSoA *final_bar, size_t n_final,
+                           PlumeSoA *initial_bar, size_t cap, size_t *n_initial, double *ng0_bar);
+
 /* Time step without allocating: dt_out[0] = cfl * min(h[i] / c[i]) over the
  * particles with bc_type 100 or 99 (1.0e10 when there are none), from
  * device arrays of n particles, on `stream` (a cudaStream_t; NULL = the

@@ -24,6 +24,7 @@
 #include "radix_sort.cuh"
 #include "sph_kernels.cuh"
 #include "sph_warp.cuh"
+#include "sph_adjoint.cuh"
 
 using namespace plume;
 
@@ -416,6 +417,38 @@ __global__ void k_set_ghost(const Opt* __restrict__ mopt, Dev A, const int* __re
 // ============================================================================
 static thread_local std::string g_create_error;
 
+// Adjoint (plume_adjoint_record / plume_adjoint_backward): one step of a
+// recomputed segment, as the backward of the step reads it (sorted order of
+// the step).
+struct AdjRec {
+  Dev S;                                 // state after the sort, before adaptive h
+  double *h1, *hit;                      // h after adaptive h; its iterates
+  uint8_t* nit;
+  double *v1x, *v1y, *v1z, *e1;          // after the momentum commit
+  double *rho2, *Y2, *e2;                // after the density commit
+  double *vs3x, *vs3y, *vs3z;            // after the LANS filter
+  double *wnd, *wnv;                     // filter normalisations
+  uint8_t* bc3;                          // bc after the position update
+  uint32_t* perm;                        // sorted row -> row before the sort
+  NList L;
+  uint32_t* real_idx;
+  int* d_real;
+  uint32_t* cs;
+  double* h27;
+  TimeState* ts;                         // time state after the step
+  int* argmin;                           // the particle that set dt
+  int* d_count;                          // live rows after the sort
+  int adaptive;                          // adaptive h ran in this step
+};
+// state at a checkpoint
+struct AdjCkpt {
+  Dev A;
+  int* d_count;
+  TimeState* ts;
+  size_t n_alloc;
+  int host_step;
+};
+
 struct plume_ctx {
   PlumeOptions opt{};  // member 0's options
   Opt o{};             // member 0's options: the fields every member shares
@@ -473,6 +506,13 @@ struct plume_ctx {
   cudaEvent_t* ev = nullptr;  // event set of the step being issued
   float phase_ms[NPHASE] = {};
   unsigned long long launches = 0;
+  // adjoint
+  AdjRec* rec = nullptr;        // snapshot target of the step being issued
+  std::vector<AdjRec> recs;     // one per step of a segment
+  std::vector<AdjCkpt> ckpts;   // every adj_every steps, then the final state
+  std::vector<void*> adj_allocs;
+  int adj_every = 0, adj_steps = 0;
+  size_t adj_rows = 0;
 };
 
 #define CK(call)                                                                      \
@@ -554,6 +594,38 @@ static void record_ev(plume_ctx* ctx, int k) {
   if (!ctx->capturing) cudaEventRecord(ctx->ev[k], ctx->st);
 }
 
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
+static void dcopy(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+}
+// every particle array of a Dev, rows [0, n)
+static void copy_dev(const Dev& d, const Dev& s, size_t n, cudaStream_t st) {
+  dcopy(d.key, s.key, 8 * n, st);
+  double* const dd[19] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.vsx, d.vsy, d.vsz, d.mass,
+                          d.h, d.rho, d.e, d.p, d.Y, d.gam, d.c, d.T, d.cp};
+  double* const ss[19] = {s.x, s.y, s.z, s.vx, s.vy, s.vz, s.vsx, s.vsy, s.vsz, s.mass,
+                          s.h, s.rho, s.e, s.p, s.Y, s.gam, s.c, s.T, s.cp};
+  for (int f = 0; f < 19; f++) dcopy(dd[f], ss[f], 8 * n, st);
+  dcopy(d.phase, s.phase, n, st);
+  dcopy(d.bc, s.bc, n, st);
+  dcopy(d.inv, s.inv, n, st);
+  dcopy(d.bkt, s.bkt, 4 * n, st);
+  dcopy(d.mem, s.mem, 2 * n, st);
+}
+
+// adjoint snapshots of the step being issued (ctx->rec set)
+static void snap_search(plume_ctx* ctx) {
+  AdjRec* r = ctx->rec;
+  const size_t n = ctx->n_alloc;
+  cudaStream_t st = ctx->st;
+  copy_dev(r->S, ctx->A, n, st);
+  dcopy(r->perm, ctx->perm, 4 * n, st);
+  dcopy(r->d_count, ctx->d_count, sizeof(int), st);
+  k_set_int<<<1, 1, 0, st>>>(r->argmin, 0x7fffffff);
+  k_dt_argmin<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->ts, r->argmin);
+}
+
 // search: keys, radix sort, gather into B, swap, cell_start
 static int search(plume_ctx* ctx) {
   const int n = (int)ctx->n_alloc;
@@ -571,6 +643,7 @@ static int search(plume_ctx* ctx) {
   k_cell_start<<<nblocks((size_t)ctx->ncells + 2, 256), 256, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
   ctx->launches += 2;
   ctx->pending_dead = false;
+  if (ctx->rec) snap_search(ctx);
   CK(cudaGetLastError());
   return PLUME_OK;
 }
@@ -581,11 +654,19 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   cudaStream_t st = ctx->st;
   const int n = (int)ctx->n_alloc;
   const int nb = nblocks(n);
+  AdjRec* rec = ctx->rec;
   if (adaptive_now || (ctx->capturing && ctx->o.adaptive)) {
     // a captured step decides on the device (step counter % interval)
     k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
-                                              ctx->d_hstep, ctx->capturing ? 0 : 1);
+                                              ctx->d_hstep, ctx->capturing ? 0 : 1, rec ? rec->hit : nullptr,
+                                              rec ? rec->nit : nullptr, n);
     ctx->launches++;
+  }
+  if (rec) {
+    dcopy(rec->h1, ctx->A.h, 8 * (size_t)n, st);
+    rec->adaptive = adaptive_now ? 1 : 0;
+    ctx->W.wnd = rec->wnd;
+    ctx->W.wnv = rec->wnv;
   }
   record_ev(ctx, 3);
   k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
@@ -609,6 +690,14 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       }
       k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts, ctx->L);
       ctx->launches++;
+      if (rec) {
+        dcopy(rec->L.e, ctx->L.e, sizeof(uint2) * (size_t)LCAP * n, st);
+        dcopy(rec->L.cnt, ctx->L.cnt, sizeof(uint16_t) * (size_t)n, st);
+        dcopy(rec->real_idx, ctx->real_idx, 4 * (size_t)n, st);
+        dcopy(rec->d_real, ctx->d_real, sizeof(int), st);
+        dcopy(rec->cs, ctx->cs, 4 * ((size_t)ctx->ncells + 2), st);
+        dcopy(rec->h27, ctx->h27, 8 * (size_t)ctx->nbk, st);
+      }
     }
   }
   record_ev(ctx, 4);
@@ -631,6 +720,12 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   record_ev(ctx, 5);
   k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, ctx->W, ctx->d_count, ctx->ts);
   ctx->launches += 5;
+  if (rec) {
+    dcopy(rec->v1x, ctx->A.vx, 8 * (size_t)n, st);
+    dcopy(rec->v1y, ctx->A.vy, 8 * (size_t)n, st);
+    dcopy(rec->v1z, ctx->A.vz, 8 * (size_t)n, st);
+    dcopy(rec->e1, ctx->A.e, 8 * (size_t)n, st);
+  }
   record_ev(ctx, 6);
   if constexpr (D == 3) {
     if (mixed) {
@@ -648,6 +743,11 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   record_ev(ctx, 7);
   k_commit_dens<D><<<nb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, ctx->W, ctx->d_count, ctx->ts);
   ctx->launches += 2;
+  if (rec) {
+    dcopy(rec->rho2, ctx->A.rho, 8 * (size_t)n, st);
+    dcopy(rec->Y2, ctx->A.Y, 8 * (size_t)n, st);
+    dcopy(rec->e2, ctx->A.e, 8 * (size_t)n, st);
+  }
   record_ev(ctx, 8);
   if (ctx->o.lans) {
     if constexpr (D == 3) {
@@ -664,6 +764,13 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
     } else
       k_velocity<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts);
     ctx->launches++;
+  }
+  if (rec) {
+    dcopy(rec->vs3x, ctx->A.vsx, 8 * (size_t)n, st);
+    dcopy(rec->vs3y, ctx->A.vsy, 8 * (size_t)n, st);
+    dcopy(rec->vs3z, ctx->A.vsz, 8 * (size_t)n, st);
+    ctx->W.wnd = nullptr;
+    ctx->W.wnv = nullptr;
   }
   record_ev(ctx, 9);
 }
@@ -699,6 +806,10 @@ static int step_async(plume_ctx* ctx) {
   k_end_step<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem);
   ctx->launches += 2;
   ctx->pending_dead = true;
+  if (ctx->rec) {
+    dcopy(ctx->rec->bc3, ctx->A.bc, (size_t)n, st);
+    dcopy(ctx->rec->ts, ctx->ts, sizeof(TimeState), st);
+  }
   record_ev(ctx, 10);
   CK(cudaGetLastError());
   return PLUME_OK;
@@ -979,6 +1090,7 @@ int plume_destroy(plume_ctx* ctx) {
   if (!ctx) return PLUME_OK;
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  for (void* p : ctx->adj_allocs) cudaFree(p);
   for (auto e : ctx->run_ev)
     if (e) cudaEventDestroy(e);
   for (void* p : ctx->allocs) cudaFree(p);
@@ -1481,6 +1593,336 @@ int plume_batch_run(plume_ctx* ctx, int max_steps, int graph_steps, int* steps_d
   ctx->phase_ms[10] = ms;
   if (steps_done) *steps_done = done;
   return s;
+}
+
+// ---------------------------------------------------------------- adjoint
+static int adj_alloc(plume_ctx* ctx, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("adjoint storage: ") + cudaGetErrorString(e);
+    return PLUME_E_CUDA;
+  }
+  ctx->adj_allocs.push_back(*p);
+  return PLUME_OK;
+}
+#define AALLOC(ptr, bytes)                                            \
+  do {                                                                \
+    int rc_ = adj_alloc(ctx, (void**)&(ptr), (bytes));                \
+    if (rc_) return rc_;                                              \
+  } while (0)
+
+static int alloc_dev_adj(plume_ctx* ctx, Dev& D, size_t n) {
+  AALLOC(D.key, 8 * n);
+  double** f[] = {&D.x, &D.y, &D.z, &D.vx, &D.vy, &D.vz, &D.vsx, &D.vsy, &D.vsz, &D.mass,
+                  &D.h, &D.rho, &D.e, &D.p, &D.Y, &D.gam, &D.c, &D.T, &D.cp};
+  for (auto p : f) AALLOC(*p, 8 * n);
+  AALLOC(D.phase, n);
+  AALLOC(D.bc, n);
+  AALLOC(D.inv, n);
+  AALLOC(D.bkt, 4 * n);
+  AALLOC(D.mem, 2 * n);
+  return PLUME_OK;
+}
+static int alloc_adj(plume_ctx* ctx, Adj& B, size_t n) {
+  double** f[] = {&B.x, &B.y, &B.z, &B.vx, &B.vy, &B.vz, &B.vsx, &B.vsy, &B.vsz,
+                  &B.m, &B.h, &B.rho, &B.e, &B.p, &B.Y, &B.c, &B.T, &B.cp};
+  for (auto p : f) AALLOC(*p, 8 * n);
+  return PLUME_OK;
+}
+static void zero_adj(const Adj& B, size_t n, cudaStream_t st) {
+  double* const f[18] = {B.x, B.y, B.z, B.vx, B.vy, B.vz, B.vsx, B.vsy, B.vsz,
+                         B.m, B.h, B.rho, B.e, B.p, B.Y, B.c, B.T, B.cp};
+  for (auto p : f) cudaMemsetAsync(p, 0, 8 * n, st);
+}
+static int alloc_rec(plume_ctx* ctx, AdjRec& r, size_t n) {
+  r = AdjRec{};
+  int rc = alloc_dev_adj(ctx, r.S, n);
+  if (rc) return rc;
+  const int nl = ctx->opt.num_loop > 0 ? ctx->opt.num_loop : 1;
+  AALLOC(r.h1, 8 * n);
+  AALLOC(r.hit, 8 * n * (size_t)(nl + 1));
+  AALLOC(r.nit, n);
+  double** d[] = {&r.v1x, &r.v1y, &r.v1z, &r.e1, &r.rho2, &r.Y2, &r.e2, &r.vs3x, &r.vs3y, &r.vs3z,
+                  &r.wnd, &r.wnv};
+  for (auto p : d) AALLOC(*p, 8 * n);
+  AALLOC(r.bc3, n);
+  AALLOC(r.perm, 4 * n);
+  AALLOC(r.L.e, sizeof(uint2) * (size_t)LCAP * n);
+  AALLOC(r.L.cnt, sizeof(uint16_t) * n);
+  AALLOC(r.real_idx, 4 * n);
+  AALLOC(r.d_real, sizeof(int));
+  AALLOC(r.cs, 4 * ((size_t)ctx->ncells + 2));
+  AALLOC(r.h27, 8 * (size_t)ctx->nbk);
+  AALLOC(r.ts, sizeof(TimeState));
+  AALLOC(r.argmin, sizeof(int));
+  AALLOC(r.d_count, sizeof(int));
+  return PLUME_OK;
+}
+static void save_ckpt(plume_ctx* ctx, AdjCkpt& c) {
+  copy_dev(c.A, ctx->A, ctx->n_alloc, ctx->st);
+  dcopy(c.d_count, ctx->d_count, sizeof(int), ctx->st);
+  dcopy(c.ts, ctx->ts, sizeof(TimeState), ctx->st);
+  c.n_alloc = ctx->n_alloc;
+  c.host_step = ctx->host_step;
+}
+static int restore_ckpt(plume_ctx* ctx, const AdjCkpt& c) {
+  copy_dev(ctx->A, c.A, c.n_alloc, ctx->st);
+  dcopy(ctx->d_count, c.d_count, sizeof(int), ctx->st);
+  dcopy(ctx->ts, c.ts, sizeof(TimeState), ctx->st);
+  ctx->n_alloc = c.n_alloc;
+  ctx->host_step = c.host_step;
+  CK(cudaMemcpyAsync(ctx->d_hstep, &ctx->host_step, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  ctx->pending_dead = true;
+  return PLUME_OK;
+}
+
+// scratch of the backward of one step
+struct AdjTmp {
+  double *ox, *oy, *oz, *oe, *orho, *oY, *oh;
+  double *dtbar, *ng0bar;
+};
+
+// backward of one recorded step: adjoints `cur` (sorted order of the step,
+// i.e. the order of the state after it) -> `prev` (order before its sort)
+static int adj_step_back(plume_ctx* ctx, const AdjRec& r, const TimeState& hts, int nlive, Adj& cur, Adj& prev,
+                         const AdjTmp& t) {
+  cudaStream_t st = ctx->st;
+  const int n = (int)ctx->adj_rows;
+  const int nb = nblocks(n ? n : 1);
+  const Opt& o = ctx->o;
+  const Geo& g = ctx->hgeo[0];
+  const double dt = hts.dtime;
+  const bool lans = o.lans != 0;
+  CK(cudaMemsetAsync(t.dtbar, 0, sizeof(double), st));
+  Work Wv{};
+  Wv.hlist = r.S.h;  // h at the search
+  Packed K{};
+  // P
+  k_adj_pos<<<nb, NTHREADS, 0, st>>>(r.S, r.bc3, r.vs3x, r.vs3y, r.vs3z, r.v1x, r.v1y, r.v1z, n, dt,
+                                     hts.erupt, lans ? 1 : 0, cur, t.dtbar);
+  AdjIn in{};
+  in.dtbar = t.dtbar;
+  in.ng0bar = t.ng0bar;
+  // V: reads v after M, rho after D, h after A
+  if (lans) {
+    k_adj_vel_pre<<<nb, NTHREADS, 0, st>>>(r.S, n, cur, t.ox, t.oy, t.oz);
+    Dev Sv = r.S;
+    Sv.h = r.h1;
+    Sv.rho = r.rho2;
+    Sv.vx = r.v1x; Sv.vy = r.v1y; Sv.vz = r.v1z;
+    AdjIn iv = in;
+    iv.vsx = t.ox; iv.vsy = t.oy; iv.vsz = t.oz;
+    iv.vsx_new = r.vs3x; iv.vsy_new = r.vs3y; iv.vsz_new = r.vs3z;
+    iv.wnv = r.wnv;
+    k_adj_sweep<VVel><<<nb, NTHREADS, 0, st>>>(o, g, Sv, Wv, K, r.cs, r.h27, r.d_real, r.real_idx, ctx->ts,
+                                               r.L, cur, iv, dt);
+  }
+  // D: reads rho before D, e after M, h after A
+  {
+    k_adj_dens_pre<<<nb, NTHREADS, 0, st>>>(o, r.S, r.rho2, r.Y2, r.e2, n, cur, t.orho, t.oY, t.oe, t.ng0bar);
+    Dev Sd = r.S;
+    Sd.h = r.h1;
+    Sd.e = r.e1;
+    AdjIn id = in;
+    id.rho = t.orho; id.Y = t.oY; id.ee = t.oe;
+    id.rho_new = r.rho2; id.Y_new = r.Y2; id.e_new = r.e2;
+    id.wnd = r.wnd;
+    k_adj_sweep<VDens><<<nb, NTHREADS, 0, st>>>(o, g, Sd, Wv, K, r.cs, r.h27, r.d_real, r.real_idx, ctx->ts,
+                                                r.L, cur, id, dt);
+  }
+  // M: reads the state after the sort with h after A
+  {
+    k_adj_mom_pre<<<nb, NTHREADS, 0, st>>>(r.S, n, cur, t.ox, t.oy, t.oz, t.oe);
+    Dev Sm = r.S;
+    Sm.h = r.h1;
+    AdjIn im = in;
+    im.vx = t.ox; im.vy = t.oy; im.vz = t.oz; im.e = t.oe;
+    k_adj_sweep<VMom><<<nb, NTHREADS, 0, st>>>(o, g, Sm, Wv, K, r.cs, r.h27, r.d_real, r.real_idx, ctx->ts,
+                                               r.L, cur, im, dt);
+  }
+  // A
+  if (r.adaptive) {
+    k_adj_adapt_pre<<<nb, NTHREADS, 0, st>>>(r.S, r.nit, n, cur, t.oh);
+    k_adj_adaptive<<<nb, NTHREADS, 0, st>>>(o, g, r.S, Wv, r.cs, n, r.hit, r.nit, n, t.oh, cur);
+  }
+  // dt (state before the step: h before A, c)
+  k_adj_dt<<<1, 1, 0, st>>>(r.S, r.argmin, o.cfl, t.dtbar, cur);
+  // back to the order before the sort
+  zero_adj(prev, (size_t)n, st);
+  if (nlive > 0) k_adj_unperm<<<nblocks(nlive), NTHREADS, 0, st>>>(cur, prev, r.perm, nlive);
+  std::swap(cur, prev);
+  CK(cudaGetLastError());
+  return PLUME_OK;
+}
+
+int plume_adjoint_record(plume_ctx* ctx, int nsteps, int checkpoint_every) {
+  if (!ctx || nsteps < 1 || checkpoint_every < 1) return PLUME_E_INVALID;
+  if (ctx->nmem != 1 || ctx->o.dim != 3 || ctx->opt.precision != PLUME_PREC_FP64 ||
+      ctx->opt.kernel != PLUME_KERNEL_GAUSS || !ctx->use_lists) {
+    ctx->err = "adjoint: one 3D FP64 run with the Gaussian kernel and neighbour lists";
+    return PLUME_E_INVALID;
+  }
+  for (void* p : ctx->adj_allocs) cudaFree(p);
+  ctx->adj_allocs.clear();
+  ctx->ckpts.clear();
+  ctx->recs.clear();
+  if (ctx->pending_dead) {  // the recorded window starts from a sorted state
+    int rc = search(ctx);
+    if (rc) return rc;
+    int s = finish_steps(ctx);
+    if (s) return s;
+  }
+  const size_t n = ctx->n_alloc;
+  ctx->adj_rows = n;
+  ctx->adj_every = checkpoint_every;
+  ctx->adj_steps = nsteps;
+  const int nseg = (nsteps + checkpoint_every - 1) / checkpoint_every;
+  ctx->ckpts.resize((size_t)nseg + 1);
+  for (auto& c : ctx->ckpts) {
+    int rc = alloc_dev_adj(ctx, c.A, n);
+    if (rc) return rc;
+    AALLOC(c.d_count, sizeof(int));
+    AALLOC(c.ts, sizeof(TimeState));
+  }
+  for (auto& v : ctx->phase_ms) v = 0;
+  ctx->launches = 0;
+  int rc = ensure_events(ctx, 1);
+  if (rc) return rc;
+  ctx->ev = ctx->evs.data();
+  for (int k = 0; k < nsteps; k++) {
+    if (k % checkpoint_every == 0) save_ckpt(ctx, ctx->ckpts[(size_t)(k / checkpoint_every)]);
+    rc = step_async(ctx);
+    if (rc) return rc;
+  }
+  // the window keeps the row count of its start (deleted rows sort last)
+  CK(cudaStreamSynchronize(ctx->st));
+  save_ckpt(ctx, ctx->ckpts.back());
+  int s = finish_steps(ctx);
+  ctx->ckpts.back().n_alloc = n;
+  return s;
+}
+
+// PlumeSoA field k of the adjoint field order of Adj
+static double* soa_field(const PlumeSoA* s, int f) {
+  double* const p[18] = {s->x, s->y, s->z, s->vx, s->vy, s->vz, s->vsx, s->vsy, s->vsz,
+                         s->mass, s->h, s->rho, s->e, s->p, s->Y, s->c, s->T, s->cp};
+  return p[f];
+}
+static double* adj_field(const Adj& B, int f) {
+  double* const p[18] = {B.x, B.y, B.z, B.vx, B.vy, B.vz, B.vsx, B.vsy, B.vsz,
+                         B.m, B.h, B.rho, B.e, B.p, B.Y, B.c, B.T, B.cp};
+  return p[f];
+}
+
+int plume_adjoint_backward(plume_ctx* ctx, const PlumeSoA* final_bar, size_t n_final, PlumeSoA* initial_bar,
+                           size_t cap, size_t* n_initial, double* ng0_bar) {
+  if (!ctx || !final_bar || !final_bar->key || !initial_bar || !initial_bar->key || !n_initial)
+    return PLUME_E_INVALID;
+  if (ctx->ckpts.empty()) {
+    ctx->err = "adjoint: no recorded window (plume_adjoint_record)";
+    return PLUME_E_INVALID;
+  }
+  const size_t n = ctx->adj_rows;
+  const AdjCkpt& c0 = ctx->ckpts.front();
+  *n_initial = c0.n_alloc;
+  if (c0.n_alloc > cap) {
+    ctx->err = "adjoint: initial_bar capacity too small";
+    return PLUME_E_CAPACITY;
+  }
+  cudaStream_t st = ctx->st;
+  // storage of the backward (kept for further calls)
+  const int every = ctx->adj_every;
+  if (ctx->recs.empty()) {
+    ctx->recs.resize((size_t)every);
+    for (auto& r : ctx->recs) {
+      int rc = alloc_rec(ctx, r, n);
+      if (rc) return rc;
+    }
+  }
+  Adj cur{}, prev{};
+  AdjTmp t{};
+  {
+    int rc;
+    if ((rc = alloc_adj(ctx, cur, n)) || (rc = alloc_adj(ctx, prev, n))) return rc;
+    double** tp[] = {&t.ox, &t.oy, &t.oz, &t.oe, &t.orho, &t.oY, &t.oh};
+    for (auto p : tp) AALLOC(*p, 8 * n);
+    AALLOC(t.dtbar, sizeof(double));
+    AALLOC(t.ng0bar, sizeof(double));
+  }
+  // adjoint of the final state, by key, in the final state's rows
+  {
+    const AdjCkpt& cf = ctx->ckpts.back();
+    std::vector<uint64_t> keys(n);
+    std::vector<uint8_t> bc(n);
+    CK(cudaMemcpy(keys.data(), cf.A.key, 8 * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(bc.data(), cf.A.bc, n, cudaMemcpyDeviceToHost));
+    std::vector<std::pair<uint64_t, uint32_t>> kr;
+    kr.reserve(n);
+    for (size_t r = 0; r < n; r++)
+      if (bc[r] != BC_DEAD) kr.push_back({keys[r], (uint32_t)r});
+    std::sort(kr.begin(), kr.end());
+    std::vector<double> h(18 * n, 0.0);
+    for (size_t q = 0; q < n_final; q++) {
+      auto it = std::lower_bound(kr.begin(), kr.end(), std::make_pair(final_bar->key[q], (uint32_t)0));
+      if (it == kr.end() || it->first != final_bar->key[q]) continue;  // not in the final state
+      for (int f = 0; f < 18; f++) {
+        const double* src = soa_field(final_bar, f);
+        if (src) h[(size_t)f * n + it->second] = src[q];
+      }
+    }
+    for (int f = 0; f < 18; f++)
+      CK(cudaMemcpy(adj_field(cur, f), h.data() + (size_t)f * n, 8 * n, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemset(t.ng0bar, 0, sizeof(double)));
+  const int nseg = (int)ctx->ckpts.size() - 1;
+  std::vector<TimeState> hts((size_t)every);
+  std::vector<int> nlive((size_t)every);
+  for (int seg = nseg - 1; seg >= 0; seg--) {
+    int rc = restore_ckpt(ctx, ctx->ckpts[(size_t)seg]);
+    if (rc) return rc;
+    const int len = std::min(every, ctx->adj_steps - seg * every);
+    for (int k = 0; k < len; k++) {
+      ctx->rec = &ctx->recs[(size_t)k];
+      rc = step_async(ctx);
+      ctx->rec = nullptr;
+      if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < len; k++) {
+      CK(cudaMemcpy(&hts[(size_t)k], ctx->recs[(size_t)k].ts, sizeof(TimeState), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(&nlive[(size_t)k], ctx->recs[(size_t)k].d_count, sizeof(int), cudaMemcpyDeviceToHost));
+      double dtmin;
+      memcpy(&dtmin, &hts[(size_t)k].dtmin_bits, sizeof(double));
+      if (hts[(size_t)k].status) {
+        ctx->err = "adjoint: recomputed step failed with status " + std::to_string(hts[(size_t)k].status);
+        return hts[(size_t)k].status;
+      }
+      if (hts[(size_t)k].dtime != ctx->o.cfl * dtmin) {
+        ctx->err = "adjoint: dt clipped to an output or end time inside the window";
+        return PLUME_E_INVALID;
+      }
+    }
+    for (int k = len - 1; k >= 0; k--) {
+      rc = adj_step_back(ctx, ctx->recs[(size_t)k], hts[(size_t)k], nlive[(size_t)k], cur, prev, t);
+      if (rc) return rc;
+    }
+  }
+  CK(cudaStreamSynchronize(st));
+  // rows of the window's first state
+  {
+    const size_t n0 = c0.n_alloc;
+    CK(cudaMemcpy(initial_bar->key, c0.A.key, 8 * n0, cudaMemcpyDeviceToHost));
+    for (int f = 0; f < 18; f++) {
+      double* dst = soa_field(initial_bar, f);
+      if (dst) CK(cudaMemcpy(dst, adj_field(cur, f), 8 * n0, cudaMemcpyDeviceToHost));
+    }
+  }
+  if (ng0_bar) CK(cudaMemcpy(ng0_bar, t.ng0bar, sizeof(double), cudaMemcpyDeviceToHost));
+  // the context continues from the window's final state
+  int rc = restore_ckpt(ctx, ctx->ckpts.back());
+  if (rc) return rc;
+  return finish_steps(ctx);
 }
 
 int plume_phase_times(plume_ctx* ctx, float* ms, int n) {

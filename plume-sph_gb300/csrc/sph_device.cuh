@@ -69,6 +69,9 @@ struct Work {  // per-step scratch arrays (sorted order)
   double* hlist;  // h at the last search (list radius base, neighs.cc:84)
   double *nv0, *nv1, *nv2, *ne, *nrho, *nY, *nE;
   float *xr, *yr, *zr;  // bucket-relative coordinates (mixed path)
+  // recorded for the adjoint (null otherwise): the energy-smoothing and LANS
+  // normalisations sum_j (m_j / rho_j) W of the density and velocity sweeps
+  double *wnd, *wnv;
 };
 
 struct TimeState {  // TimeProps on the device, properties.h:17-83

@@ -140,10 +140,13 @@ __device__ __forceinline__ bool in_box(const T* dx, T r) {
 // adaptive_sml (neighs.cc:479-693, ADAPTIVE_SML 1): up to num_loop fixed-point
 // iterations h <- eta * (m / rho*)^(1/D), rho* = sum m_j W(dx / 2h, 2h)
 // Runs on the steps with hstep % interval == 0 unless forced.
+// hit / nit (adjoint recording, null otherwise): the iterates h_0..h_K in
+// rows of nrow and the iteration count K of every particle.
 template <int D, typename T>
 __global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
                            const int* __restrict__ d_count, TimeState* ts_all, const int* __restrict__ hstep,
-                           int force) {
+                           int force, double* __restrict__ hit = nullptr, uint8_t* __restrict__ nit = nullptr,
+                           int nrow = 0) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count) return;
   if (!force && (*hstep % o.interval) != 0) return;
@@ -161,8 +164,11 @@ __global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
   const T Lb = T(o.list_factor * W.hlist[i]);
   const double mi = A.mass[i];
   double hcur = A.h[i];
+  int done = 0;
   for (int loop = 0; loop < o.num_loop; loop++) {
     double H_old = hcur;
+    if (hit) hit[(size_t)loop * nrow + i] = H_old;
+    done = loop + 1;
     double H_star_d = H_old * o.c_smooth;
     T H_star = T(H_star_d);
     T supp = T(o.cutoff2) * H_star;
@@ -192,6 +198,10 @@ __global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
     }
     double err = fabs((H_new - H_old) / H_old);
     if (err < o.thresh) break;
+  }
+  if (hit) {
+    hit[(size_t)done * nrow + i] = hcur;
+    nit[i] = (uint8_t)done;
   }
   A.h[i] = hcur;
 }

@@ -385,6 +385,7 @@ struct WDens {
         return;
       }
       W.nE[ii] = en / wn;
+      if (W.wnd) W.wnd[ii] = wn;
     }
     double density = 0.0;
     density += r1;
@@ -489,7 +490,7 @@ struct WVel {
     return true;
   }
   template <bool WARP>
-  __device__ __forceinline__ void finish(int ii, Work&, TimeState* ts) {
+  __device__ __forceinline__ void finish(int ii, Work& W, TimeState* ts) {
     double d0 = (double)dv[0].get(), d1 = (double)dv[1].get(), d2 = (double)dv[2].get();
     double wn = (double)wnorm.get();
     if (WARP) {
@@ -500,6 +501,7 @@ struct WVel {
       set_status(ts, 4);
       return;
     }
+    if (W.wnv) W.wnv[ii] = wn;
     A.vsx[ii] = vi_d[0] + d0 / wn;
     A.vsy[ii] = vi_d[1] + d1 / wn;
     A.vsz[ii] = vi_d[2] + d2 / wn;
@@ -738,27 +740,12 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
 
 // sweep over the lists (thread per particle, over the compacted need_neigh
 // indices); particles whose list overflowed walk their rows.  The window and
-// bit loops are flattened so that every iteration hands each thread exactly
-// one pair (threads of a warp stay converged while they have pairs left).
-template <typename T, template <typename> class SW, bool MULTI>
-__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
-                                                     const uint32_t* __restrict__ cs_all,
-                                                     const double* __restrict__ hmax_all,
-                                                     const int* __restrict__ d_real,
-                                                     const uint32_t* __restrict__ real_idx, TimeState* ts_all,
-                                                     NList L) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= *d_real) return;
-  const int i = (int)real_idx[r];
-  const int m = geo.member(A, i);  // real_idx holds particles of active members only
-  TimeState* ts = ts_all + m;
-  const Geo& g = geo.of(m);
-  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
-  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
-  SW<T> s(A, K, o);
-  double xi[3], R;
-  int bi[3];
-  if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;
+// Visits the candidates of particle i in the walk's order: the particle's
+// stored windows (set bits, in order), or the cell rows when its windows
+// overflowed; s.math(j, dx, hj) for every candidate s.filter passes.
+template <typename T, class S>
+__device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint32_t* __restrict__ cs,
+                                          const double* xi, const int* bi, double R, const NList& L) {
   const uint16_t c = L.cnt[i];
   if (c == NL_OVERFLOW) {
     for_segments<3, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
@@ -789,6 +776,30 @@ __global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev
       if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
     }
   }
+}
+
+// bit loops are flattened so that every iteration hands each thread exactly
+// one pair (threads of a warp stay converged while they have pairs left).
+template <typename T, template <typename> class SW, bool MULTI>
+__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                     const uint32_t* __restrict__ cs_all,
+                                                     const double* __restrict__ hmax_all,
+                                                     const int* __restrict__ d_real,
+                                                     const uint32_t* __restrict__ real_idx, TimeState* ts_all,
+                                                     NList L) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *d_real) return;
+  const int i = (int)real_idx[r];
+  const int m = geo.member(A, i);  // real_idx holds particles of active members only
+  TimeState* ts = ts_all + m;
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
+  SW<T> s(A, K, o);
+  double xi[3], R;
+  int bi[3];
+  if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;
+  list_walk<T>(s, i, g, cs, xi, bi, R, L);
   s.template finish<false>(i, W, ts);
 }
 

@@ -86,5 +86,8 @@ def lib():
                                            P(C.c_size_t)]
         L.plume_batch_time.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int), P(C.c_int)]
         L.plume_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_int)]
+        L.plume_adjoint_record.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
+                                             P(C.c_size_t), P(C.c_double)]
         _LIB = L
         return L

@@ -125,6 +125,26 @@ class Solver:
         self._check(self.L.plume_steps(self.ctx, n, None), "plume_steps")
         return None
 
+    # -- adjoint --------------------------------------------------------------
+    def adjoint_record(self, nsteps: int, checkpoint_every: int = 25):
+        """nsteps steps keeping checkpoints for adjoint_backward"""
+        self._adj_n0 = self.count()[0]
+        self._check(self.L.plume_adjoint_record(self.ctx, nsteps, checkpoint_every),
+                    "plume_adjoint_record")
+
+    def adjoint_backward(self, final_bar: ParticleSet):
+        """(adjoint of the window's first state as a ParticleSet with keys,
+        adjoint of ng0) from the adjoint of the final state (rows by key)"""
+        out = ParticleSet(self._adj_n0)
+        s_in, s_out = final_bar.soa(), out.soa()
+        n0 = C.c_size_t()
+        g = C.c_double()
+        self._check(self.L.plume_adjoint_backward(self.ctx, C.byref(s_in), final_bar.n, C.byref(s_out),
+                                                  out.n, C.byref(n0), C.byref(g)), "plume_adjoint_backward")
+        if n0.value != out.n:
+            out = out.take(np.arange(n0.value))
+        return out, g.value
+
     def time(self):
         t, s, o = C.c_double(), C.c_int(), C.c_int()
         self._check(self.L.plume_get_time(self.ctx, C.byref(t), C.byref(s), C.byref(o)),
