@@ -288,6 +288,44 @@ def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
             "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
 
 
+def adjoint_leg(steps=300, every=25, n_air=2.0e5, fd_rels=()):
+    """Gradient of the plume observable w.r.t. (vent velocity, temperature,
+    ash fraction) through the hand-written adjoint on the config-4 geometry
+    (60 m lattice) sized for n_air air particles: the time of one FP64
+    forward solve, of the recorded forward + backward, their ratio, and
+    central differences of full forward runs for each relative step in
+    fd_rels.  The forward map is piecewise smooth (erupt-to-real
+    conversions, the Gaussian's box cut-off): differences with steps that
+    cross its jumps measure the jumps; small steps converge to the adjoint."""
+    import torch
+    from plume_gpu import adjoint, cases
+    dx = 60.0
+    side = dx * n_air ** (1.0 / 3.0)
+    case = cases.plume_3d(half_width=0.5 * side, height=side, dx=dx, vent_radius=100.0, seed=2,
+                          name="plume_adjoint")
+    theta = np.array([150.0, 1053.0, 0.95])
+    obj = dict(z_ash=3000.0, width=50.0, z_target=1000.0, r_scale=200.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J0 = adjoint.forward_value(theta, case, steps, **obj)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    J, g = adjoint.value_and_grad(theta, case, steps, every, **obj)
+    t_grad = time.perf_counter() - t0
+    out = {"workload": f"plume3d_60m_{int(case.info['n_air'])}air", "n_particles": int(case.particles.n),
+           "steps": steps, "checkpoint_every": every, "objective": obj, "J": J, "J_forward": J0,
+           "grad": g.tolist(), "forward_s": t_fwd, "gradient_s": t_grad,
+           "gradient_over_forward": t_grad / t_fwd}
+    out["fd"] = []
+    for rel in fd_rels:
+        t0 = time.perf_counter()
+        gf = adjoint.finite_difference(theta, case, steps, rel=rel, **obj)
+        out["fd"].append({"rel_step": rel, "grad": gf.tolist(),
+                          "rel_err": (np.abs(g - gf) / np.maximum(np.abs(g), 1e-300)).tolist(),
+                          "seconds": time.perf_counter() - t0})
+    return out
+
+
 def small_plume(prec):
     """the test-size workload of --small (4 km tall plume at 50 m)"""
     from plume_gpu import cases
@@ -342,6 +380,10 @@ def main():
     ap.add_argument("--small", action="store_true", help="test-size workload")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     ap.add_argument("--no-tune", action="store_true", help="fixed cell tiles (4^3 per bucket)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--adjoint-fd", action="store_true",
+                    help="also check the adjoint gradient by central differences, relative "
+                         "steps 1e-4 and 1e-10 (12 forward solves)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist, rank, ws = dist_init()
@@ -481,6 +523,13 @@ def main():
         except Exception as e:
             ens["plume3d"] = {"failed": str(e)}
 
+    adj = None
+    if not args.no_adjoint and not args.small:
+        try:
+            adj = adjoint_leg(fd_rels=(1e-4, 1e-10) if args.adjoint_fd else ())
+        except Exception as e:
+            adj = {"failed": str(e)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -509,6 +558,7 @@ def main():
                                   "flop_per_pair": MOM_FLOP_PER_PAIR}},
             "cpu_baseline": cpu,
             "ensembles": ens,
+            "adjoint": adj,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
