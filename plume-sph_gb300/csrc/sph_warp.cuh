@@ -780,8 +780,30 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
 
 // bit loops are flattened so that every iteration hands each thread exactly
 // one pair (threads of a warp stay converged while they have pairs left).
+// minimum resident blocks per SM of each list sweep (caps its registers;
+// measured on the 134^3 plume: momentum 6 blocks = 80 registers, 5.41 ms
+// against 7.08 ms uncapped at 102 registers and 8.01 ms at 64 with spills;
+// density and LANS filter 8 blocks = 64 registers, 8 % faster than 7)
+#ifndef PLUME_MINB_MOM
+#define PLUME_MINB_MOM 6
+#endif
+#ifndef PLUME_MINB_DENS
+#define PLUME_MINB_DENS 8
+#endif
+#ifndef PLUME_MINB_VEL
+#define PLUME_MINB_VEL 8
+#endif
+template <template <typename> class SW>
+struct SweepMinBlocks { static constexpr int v = 1; };
+template <>
+struct SweepMinBlocks<WMom> { static constexpr int v = PLUME_MINB_MOM; };
+template <>
+struct SweepMinBlocks<WDens> { static constexpr int v = PLUME_MINB_DENS; };
+template <>
+struct SweepMinBlocks<WVel> { static constexpr int v = PLUME_MINB_VEL; };
+
 template <typename T, template <typename> class SW, bool MULTI>
-__global__ void __launch_bounds__(128) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+__global__ void __launch_bounds__(128, SweepMinBlocks<SW>::v) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
                                                      const uint32_t* __restrict__ cs_all,
                                                      const double* __restrict__ hmax_all,
                                                      const int* __restrict__ d_real,
