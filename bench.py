@@ -381,6 +381,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     ap.add_argument("--no-tune", action="store_true", help="fixed cell tiles (4^3 per bucket)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-wall-bc", action="store_true",
+                    help="leave the wall ghosts' states fixed (no apply_bcond in the step)")
     ap.add_argument("--adjoint-fd", action="store_true",
                     help="also check the adjoint gradient by central differences, relative "
                          "steps 1e-4 and 1e-10 (12 forward solves)")
@@ -415,7 +417,10 @@ def main():
                   "seconds": time.perf_counter() - t0}
         case = with_subcells(case, best)
     n_air0 = int(case.particles.need_neigh().sum())
+    images = None if args.no_wall_bc else cases.wall_images(case)
     sol = Solver(case)
+    if images is not None:
+        sol.set_wall_images(*images)
     # warm-up (not timed)
     sol.steps(args.warmup)
     barrier(dist)
@@ -489,6 +494,8 @@ def main():
     if not args.no_fp64:
         c64 = with_subcells(make(PREC_FP64), case.grid.subcells)
         s64 = Solver(c64)
+        if images is not None:
+            s64.set_wall_images(*images)
         s64.steps(3)
         k64 = max(2, min(args.steps, 3))
         _, nr0 = s64.count()
@@ -540,7 +547,8 @@ def main():
                        "n_air": n_air0, "n_particles": int(case.particles.n),
                        "precision": "fp32 pair arithmetic, fp64 positions and updates",
                        "parallelism": f"replicas{ws}", "l2": "working set > L2 (state ~0.6 GB)",
-                       "subcells": int(case.grid.subcells), "autotune": tuning},
+                       "subcells": int(case.grid.subcells), "autotune": tuning,
+                       "wall_images": 0 if images is None else int(len(images[0]))},
             "gpu_launches": launches,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
             "clocks": clk.summary(),

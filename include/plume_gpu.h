@@ -294,6 +294,23 @@ int plume_batch_download(plume_ctx *ctx, PlumeSoA *host, uint16_t *member, size_
 int plume_batch_time(plume_ctx *ctx, double *time, int *step, int *running, int *status);
 int plume_batch_run(plume_ctx *ctx, int max_steps, int graph_steps, int *steps_done);
 
+/* ---------------------------------------------------------------- wall boundary
+ * The wall-ghost states of apply_bcond (src/plume/bcond.cc:24-249, the
+ * reference's BC_FOR_KX 1), on the device.  plume_set_wall_images sets the
+ * image table that search_bnd_images (datstr/bnd_image.cc:35-245) builds:
+ * for each wall ghost (bc_type 2, key ghost_keys[i]) its image point
+ * image_xyz[3i..3i+2]; n = 0 clears it.  Every step then starts, after its
+ * sort, by setting each such ghost's rho, v, e, Y to the normalised SPH
+ * averages of the real and pressure-ghost particles around its image (the
+ * image's bucket and its 26 neighbours), the velocity reflected in the wall,
+ * and its EOS fields -- where the reference applies the same at the end of
+ * the previous step and once before its loop.  plume_apply_bcond applies it
+ * now (a host that downloads after plume_steps and wants the states the
+ * reference writes at the end of the last step).  3D, keys unique in the
+ * context; the adjoint entry points reject a context with images. */
+int plume_set_wall_images(plume_ctx *ctx, const uint64_t *ghost_keys, const double *image_xyz, size_t n);
+int plume_apply_bcond(plume_ctx *ctx);
+
 /* ---------------------------------------------------------------- adjoint
  * Reverse-mode derivatives of a window of particle steps (one 3D run, FP64,
  * Gaussian kernel).  No counterpart in the reference.

@@ -50,6 +50,13 @@ def lib():
                                                  C.POINTER(PlumeSoA), C.c_size_t, C.c_size_t,
                                                  C.c_int]
         L.oracle_sample_step_seconds.restype = C.c_double
+        L.oracle_apply_bcond.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                         C.POINTER(PlumeSoA), C.c_size_t, C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_double), C.c_size_t]
+        L.oracle_steps_bc.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                      C.POINTER(PlumeSoA), C.POINTER(C.c_size_t),
+                                      C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_size_t]
         _LIB = L
     return _LIB
 
@@ -72,12 +79,32 @@ class OracleRun:
         if rc:
             raise RuntimeError(f"oracle_adaptive failed: {rc}")
 
+    def set_images(self, keys, xyz):
+        """wall images (apply_bcond): applied at the end of every step"""
+        self.img_key = np.ascontiguousarray(keys, dtype=np.uint64)
+        self.img_xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+
+    def apply_bcond(self):
+        s = self.ps.soa()
+        rc = lib().oracle_apply_bcond(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n,
+                                      self.img_key.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                      self.img_xyz.ctypes.data_as(C.POINTER(C.c_double)), len(self.img_key))
+        if rc:
+            raise RuntimeError(f"oracle_apply_bcond failed: {rc}")
+
     def steps(self, nsteps: int):
         s = self.ps.soa()
         n = C.c_size_t(self.ps.n)
         dts = (C.c_double * max(nsteps, 1))()
-        rc = lib().oracle_steps(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
-                                C.byref(self.t), nsteps, dts, self.nthreads)
+        if getattr(self, "img_key", None) is not None:
+            rc = lib().oracle_steps_bc(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
+                                       C.byref(self.t), nsteps, dts, self.nthreads,
+                                       self.img_key.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                       self.img_xyz.ctypes.data_as(C.POINTER(C.c_double)),
+                                       len(self.img_key))
+        else:
+            rc = lib().oracle_steps(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
+                                    C.byref(self.t), nsteps, dts, self.nthreads)
         if rc:
             raise RuntimeError(f"oracle_steps failed: {rc}")
         if n.value != self.ps.n:

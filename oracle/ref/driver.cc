@@ -45,6 +45,11 @@
 #include "constant.h"
 #include "sph_header.h"
 #include "plume_gpu.h"
+#if CODE_DIMENSION == 3
+#include <list>
+#include <map>
+#include <bnd_image.h>
+#endif
 
 static const int NF = 19;
 
@@ -59,6 +64,9 @@ struct Case {
   std::vector<uint64_t> key;
   std::vector<double> f[NF];
   std::vector<uint8_t> phase, bc, inv;
+  // optional wall images (3D): ghost key and image point of each
+  std::vector<uint64_t> img_key;
+  std::vector<double> img_xyz;
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -107,6 +115,13 @@ static void read_case(const char *path, Case &c) {
   rd(fp, c.phase.data(), 1, c.n);
   rd(fp, c.bc.data(), 1, c.n);
   rd(fp, c.inv.data(), 1, c.n);
+  int64_t nimg = 0;
+  if (fread(&nimg, 8, 1, fp) == 1 && nimg > 0) {
+    c.img_key.resize((size_t)nimg);
+    c.img_xyz.resize(3 * (size_t)nimg);
+    rd(fp, c.img_key.data(), 8, (size_t)nimg);
+    rd(fp, c.img_xyz.data(), 8, 3 * (size_t)nimg);
+  }
   fclose(fp);
 }
 
@@ -371,6 +386,34 @@ int main(int argc, char **argv) {
     }
   }
   for (size_t b = 0; b < bucks.size(); b++) bucks[b]->put_plist(plists[b]);
+  // wall images (the table search_bnd_images builds, bnd_image.cc:35-245):
+  // the ghost's key and the image point come from the case, the bucket
+  // is the one containing the image
+  std::list<BndImage> Image_table;
+  {
+    std::map<uint64_t, int> row;
+    for (int i = 0; i < c.n; i++) row[c.key[i]] = i;
+    for (size_t q = 0; q < c.img_key.size(); q++) {
+      auto it = row.find(c.img_key[q]);
+      if (it == row.end()) continue;
+      double refc[3] = { c.img_xyz[3 * q], c.img_xyz[3 * q + 1], c.img_xyz[3 * q + 2] };
+      int b3[3];
+      for (int a = 0; a < 3; a++) {
+        int b = (int)floor((refc[a] - c.mindom[a]) / c.del);
+        if (b < 0) b = 0;
+        if (b > c.nb[a] - 1) b = c.nb[a] - 1;
+        while (b > 0 && refc[a] < c.mindom[a] + b * c.del) b--;
+        while (b < c.nb[a] - 1 && refc[a] >= c.mindom[a] + (b + 1) * c.del) b++;
+        b3[a] = b;
+      }
+      unsigned bk2[KEYLENGTH], gk[TKEYLENGTH];
+      bkey(b3[0], b3[1], b3[2], bk2);
+      pkey((unsigned)it->second, gk);
+      Image_table.push_back(BndImage(0, 0, bk2, gk, refc));
+    }
+  }
+  // boundary condition before the loop (main.cc:196)
+  if (!Image_table.empty()) apply_bcond(0, P, BG, matprops, Image_table);
 #endif
 
   FILE *fo = fopen(argv[2], "wb");
@@ -405,6 +448,7 @@ int main(int argc, char **argv) {
 #endif
     update_pos(P, tp, matprops);
     update_particles_in_bucket(0, P, BG, &lost);
+    if (!Image_table.empty()) apply_bcond(0, P, BG, matprops, Image_table);  // main.cc:468
 #endif
     tp->ifoutput();
     bool last = (c.nsteps < 0) ? tp->ifend() : (st == c.nsteps - 1);

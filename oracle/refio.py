@@ -18,7 +18,9 @@ def build_ref(ref_root: str = "/root/reference"):
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
 
 
-def write_case(path, case, nsteps, dump_last=False):
+def write_case(path, case, nsteps, dump_last=False, images=None):
+    """images: optional (ghost keys, image points (n, 3)) of the wall
+    boundary (3D)"""
     o, g, ps = case.options, case.grid, case.particles
     with open(path, "wb") as fp:
         fp.write(b"PLSPHIN1")
@@ -39,6 +41,11 @@ def write_case(path, case, nsteps, dump_last=False):
             fp.write(getattr(ps, f).astype("<f8").tobytes())
         for f in BYTE_FIELDS:
             fp.write(getattr(ps, f).astype(np.uint8).tobytes())
+        if images is not None:
+            keys, xyz = images
+            fp.write(struct.pack("<q", len(keys)))
+            fp.write(np.ascontiguousarray(keys, dtype="<u8").tobytes())
+            fp.write(np.ascontiguousarray(xyz, dtype="<f8").reshape(-1).tobytes())
 
 
 def read_result(path):
@@ -77,11 +84,11 @@ def read_result(path):
     return steps, lists
 
 
-def run_ref(variant, case, nsteps, workdir, dump_last=False):
+def run_ref(variant, case, nsteps, workdir, dump_last=False, images=None):
     os.makedirs(workdir, exist_ok=True)
     cin = os.path.join(workdir, f"{case.name}.case")
     cout = os.path.join(workdir, f"{case.name}.out")
-    write_case(cin, case, nsteps, dump_last)
+    write_case(cin, case, nsteps, dump_last, images)
     exe = os.path.join(HERE, "_ref", variant, "driver")
     subprocess.run([exe, cin, cout], check=True)
     return read_result(cout)

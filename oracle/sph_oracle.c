@@ -779,6 +779,117 @@ static void compact(PlumeSoA *s, size_t *n, const char *del)
 }
 #undef SOA_D
 
+/* ------------------------------------------------------------------ */
+/* wall boundary, apply_bcond (bcond.cc:24-249) with BC_FOR_KX 1        */
+/* ------------------------------------------------------------------ */
+typedef struct Images {
+    const uint64_t *key;   /* wall ghost of each image */
+    const double   *xyz;   /* image point (3 per image) */
+    size_t          n;
+} Images;
+
+static int cmp_u64pair(const void *a, const void *b)
+{
+    const uint64_t *x = (const uint64_t *)a, *y = (const uint64_t *)b;
+    return (x[0] > y[0]) - (x[0] < y[0]);
+}
+
+/* For every image: the Shepard-normalised SPH averages of rho, v, e (and Y,
+ * whose sum the reference accumulates over the neighbour buckets only) of
+ * the real and pressure-ghost particles (contr_image, particle.h:562-565)
+ * inside CUTOFF2 h_j of the image, over the image's bucket then its 26
+ * neighbours in x-major order; the velocity reflected in the wall
+ * (reflect, sph_lib.cc:76-83) along the ghost-to-image direction; written
+ * to the ghost with its EOS. */
+static int apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, size_t n, const Images *im)
+{
+    if (!im || im->n == 0) return PLUME_OK;
+    long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
+    long *bk = (long *)malloc(sizeof(long) * (n ? n : 1));
+    size_t *bstart = (size_t *)calloc((size_t)nbk + 1, sizeof(size_t));
+    int32_t *bidx = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    uint64_t *kr = (uint64_t *)malloc(sizeof(uint64_t) * 2 * (n ? n : 1));
+    if (!bk || !bstart || !bidx || !kr) { free(bk); free(bstart); free(bidx); free(kr); return PLUME_E_INVALID; }
+    for (size_t i = 0; i < n; i++) {
+        bk[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
+        if (bk[i] >= 0) bstart[bk[i] + 1]++;
+        kr[2 * i] = s->key[i];
+        kr[2 * i + 1] = i;
+    }
+    for (long b = 0; b < nbk; b++) bstart[b + 1] += bstart[b];
+    {
+        size_t *fill = (size_t *)malloc(sizeof(size_t) * (size_t)(nbk ? nbk : 1));
+        memcpy(fill, bstart, sizeof(size_t) * (size_t)nbk);
+        for (size_t i = 0; i < n; i++)
+            if (bk[i] >= 0) bidx[fill[bk[i]]++] = (int32_t)i;
+        free(fill);
+    }
+    qsort(kr, n, 2 * sizeof(uint64_t), cmp_u64pair);
+    int nbx = g->nb[0], nby = g->nb[1], nbz = g->nb[2];
+    int rc = PLUME_OK;
+    for (size_t q = 0; q < im->n; q++) {
+        uint64_t want[2] = { im->key[q], 0 };
+        uint64_t *hit = (uint64_t *)bsearch(want, kr, n, 2 * sizeof(uint64_t), cmp_u64pair);
+        if (!hit) continue;  /* ghost deleted */
+        size_t gi = (size_t)hit[1];
+        const double *refc = im->xyz + 3 * q;
+        double normal[3], d = 0;
+        const double pc[3] = { s->x[gi], s->y[gi], s->z[gi] };
+        for (int a = 0; a < 3; a++) { normal[a] = refc[a] - pc[a]; d += normal[a] * normal[a]; }
+        for (int a = 0; a < 3; a++) normal[a] /= sqrt(d);
+        long b = bucket_of(g, refc[0], refc[1], refc[2]);
+        if (b < 0) { rc = PLUME_E_OUTSIDE_GRID; break; }
+        double uvec[5] = { 0, 0, 0, 0, 0 }, wnorm = 0, ks = 0;
+        int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long)nbx * nby));
+        for (int pass = 0; pass < 2; pass++)
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        int own = !dx && !dy && !dz;
+                        if (own != (pass == 0)) continue;   /* own bucket first */
+                        int cx = bx + dx, cy = by + dy, cz = bz + dz;
+                        if (cx < 0 || cx >= nbx || cy < 0 || cy >= nby || cz < 0 || cz >= nbz) continue;
+                        long nb_ = ((long)cz * nby + cy) * nbx + cx;
+                        for (size_t r = bstart[nb_]; r < bstart[nb_ + 1]; r++) {
+                            size_t j = (size_t)bidx[r];
+                            uint8_t bc = s->bc_type[j];
+                            if (!(bc == 100 || bc == 99 || bc == 1)) continue;
+                            double h = s->h[j];
+                            double ds[3] = { refc[0] - s->x[j], refc[1] - s->y[j], refc[2] - s->z[j] };
+                            if (!in_support(ds, o->cutoff2 * h, 3)) continue;
+                            double sv[3] = { ds[0] / h, ds[1] / h, ds[2] / h };
+                            double w = weight_gauss(sv, h, 3);
+                            double mj = s->mass[j], rj = s->rho[j];
+                            uvec[0] += mj * w;
+                            uvec[1] += mj * w * s->vx[j] / rj;
+                            uvec[2] += mj * w * s->vy[j] / rj;
+                            uvec[3] += mj * w * s->vz[j] / rj;
+                            uvec[4] += mj * w * s->e[j] / rj;
+                            if (!own) ks += mj * w * s->Y[j] / rj;
+                            wnorm += mj * w / rj;
+                        }
+                    }
+        if (wnorm > 0.) {
+            for (int a = 0; a < 5; a++) uvec[a] /= wnorm;
+            ks = ks / wnorm;
+        } else {
+            uvec[0] = 1.;
+            for (int a = 1; a < 5; a++) uvec[a] = 0.;
+            ks = 0.0;
+        }
+        double vdotn = uvec[1] * normal[0] + uvec[2] * normal[1] + uvec[3] * normal[2];
+        double vr[3];
+        for (int a = 0; a < 3; a++) vr[a] = uvec[1 + a] - 2 * vdotn * normal[a];
+        s->rho[gi] = uvec[0];
+        s->vx[gi] = vr[0]; s->vy[gi] = vr[1]; s->vz[gi] = vr[2];
+        s->e[gi] = uvec[4];
+        s->Y[gi] = ks;
+        eos(o, s, gi);
+    }
+    free(bk); free(bstart); free(bidx); free(kr);
+    return rc;
+}
+
 static int alloc_work(Work *w, size_t n)
 {
     size_t m = n ? n : 1;
@@ -833,9 +944,36 @@ int oracle_adaptive(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
 }
 
 /* One step of the hot loop: 3D main.cc:217-471, 1D main.cc:676-750. */
+static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                      size_t *n, OracleTime *t, int nsteps, double *dt_log,
+                      int nthreads, const Images *im);
+
 int oracle_steps(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                  size_t *n, OracleTime *t, int nsteps, double *dt_log,
                  int nthreads)
+{
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL);
+}
+
+int oracle_steps_bc(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                    size_t *n, OracleTime *t, int nsteps, double *dt_log,
+                    int nthreads, const uint64_t *img_key, const double *img_xyz,
+                    size_t nimg)
+{
+    Images im = { img_key, img_xyz, nimg };
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im);
+}
+
+int oracle_apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, size_t n,
+                       const uint64_t *img_key, const double *img_xyz, size_t nimg)
+{
+    Images im = { img_key, img_xyz, nimg };
+    return apply_bcond(o, g, s, n, &im);
+}
+
+static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                      size_t *n, OracleTime *t, int nsteps, double *dt_log,
+                      int nthreads, const Images *im)
 {
     int rc = check_opts(o, g, s);
     if (rc) return rc;
@@ -872,6 +1010,9 @@ int oracle_steps(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
             size_t lost = 0;
             rc = rebucket(o, g, s, n, oldb, &lost);
             free(oldb);
+            if (rc) return rc;
+            /* main.cc:468, after the inlet and before the output */
+            rc = apply_bcond(o, g, s, *n, im);
             if (rc) return rc;
         }
         ifoutput(o, t);

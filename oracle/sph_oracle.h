@@ -40,6 +40,14 @@ int oracle_adaptive(const PlumeOptions *opt, const PlumeGrid *grid,
 /* nsteps steps of the hot loop.  *n is updated when particles are deleted
  * (arrays are compacted in order).  dt_log (may be NULL) receives the
  * clipped dt of each step.  Returns PLUME_OK or a PLUME_E_* code. */
+/* Wall boundary (apply_bcond, bcond.cc:24-249): every image (ghost key,
+ * image point) sets its wall ghost's state.  oracle_steps_bc applies it at
+ * the end of every 3D step (main.cc:468). */
+int oracle_apply_bcond(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s, size_t n,
+                       const uint64_t *img_key, const double *img_xyz, size_t nimg);
+int oracle_steps_bc(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s, size_t *n,
+                    OracleTime *t, int nsteps, double *dt_log, int nthreads,
+                    const uint64_t *img_key, const double *img_xyz, size_t nimg);
 int oracle_steps(const PlumeOptions *opt, const PlumeGrid *grid,
                  PlumeSoA *s, size_t *n, OracleTime *t, int nsteps,
                  double *dt_log, int nthreads);

@@ -410,6 +410,125 @@ __global__ void k_set_ghost(const Opt* __restrict__ mopt, Dev A, const int* __re
   A.gam[i] = gam; A.p[i] = p; A.c[i] = c; A.T[i] = T; A.cp[i] = cp;
 }
 
+// ---- wall boundary (apply_bcond, bcond.cc:24-249, BC_FOR_KX 1) ------------
+// One thread per wall ghost with an image: the Shepard-normalised SPH
+// averages of rho, v, e of the real and pressure-ghost particles
+// (contr_image, particle.h:562-565) inside CUTOFF2 h_j of the image point,
+// over the image's bucket and its 26 neighbours (Y over the neighbours only,
+// as the reference accumulates it), the velocity reflected in the wall
+// along the ghost-to-image direction (reflect, sph_lib.cc:76-83), written
+// to the ghost with its EOS.  Runs after the step's sort, where the
+// reference runs it at the end of the previous step (main.cc:196, 468):
+// nothing in between reads ghost states.  T = double: the reference's FP64
+// arithmetic; T = float (mixed path): FP32 weights on bucket-relative
+// coordinates with compensated FP32 sums, like the pair sweeps.
+template <typename T>
+__global__ void k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restrict__ geo, Dev A, Work W,
+                              const uint32_t* __restrict__ cs_all, const double* __restrict__ h27_all,
+                              const int* __restrict__ d_count, const uint64_t* __restrict__ ikey,
+                              const double* __restrict__ ixyz, int nimg, TimeState* ts_all) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count || A.bc[i] != 2) return;
+  const uint64_t k = A.key[i];
+  int lo = 0, hi = nimg;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ikey[mid] < k) lo = mid + 1; else hi = mid;
+  }
+  if (lo >= nimg || ikey[lo] != k) return;
+  const int m = A.mem[i];
+  const Geo& g = geo[m];
+  const Opt& o = mopt[m];
+  TimeState* ts = ts_all + m;
+  const uint32_t* cs = cs_all + g.cell_base;
+  const double refc[3] = {ixyz[3 * lo], ixyz[3 * lo + 1], ixyz[3 * lo + 2]};
+  double normal[3] = {refc[0] - A.x[i], refc[1] - A.y[i], refc[2] - A.z[i]};
+  const double d = sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
+#pragma unroll
+  for (int a = 0; a < 3; a++) normal[a] /= d;
+  bool o1, o2, o3;
+  int bi[3];
+  bi[0] = bucket_axis(refc[0], g.mind[0], g.del, g.idel, g.nb[0], &o1);
+  bi[1] = bucket_axis(refc[1], g.mind[1], g.del, g.idel, g.nb[1], &o2);
+  bi[2] = bucket_axis(refc[2], g.mind[2], g.del, g.idel, g.nb[2], &o3);
+  if (o1 || o2 || o3) {
+    set_status(ts, 6);
+    return;
+  }
+  const int b = (bi[2] * g.nb[1] + bi[1]) * g.nb[0] + bi[0];
+  const double R = o.ksupport * h27_all[g.bucket_base + b] * (1.0 + 1e-10);
+  double u0 = 0, u1 = 0, u2 = 0, u3 = 0, u4 = 0, wn = 0, ks = 0;
+  if constexpr (sizeof(T) == 8) {
+    for_segments<3, double>(g, cs, refc, bi, R, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+      for (uint32_t j = j0; j < j1; j++) {
+        const uint8_t bc = A.bc[j];
+        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
+        const double h = A.h[j];
+        const double ds[3] = {refc[0] - A.x[j], refc[1] - A.y[j], refc[2] - A.z[j]};
+        if (!in_box<3, double>(ds, o.cutoff2 * h)) continue;
+        const double sv[3] = {ds[0] / h, ds[1] / h, ds[2] / h};
+        const double w = w_gauss<3, double>(sv, h);
+        const double mj = A.mass[j], rj = A.rho[j];
+        u0 += mj * w;
+        u1 += mj * w * A.vx[j] / rj;
+        u2 += mj * w * A.vy[j] / rj;
+        u3 += mj * w * A.vz[j] / rj;
+        u4 += mj * w * A.e[j] / rj;
+        if (!own) ks += mj * w * A.Y[j] / rj;
+        wn += mj * w / rj;
+      }
+    });
+  } else {
+    // the image point relative to its bucket, candidates relative to theirs
+    const float ir[3] = {(float)(refc[0] - (g.mind[0] + bi[0] * g.del)),
+                         (float)(refc[1] - (g.mind[1] + bi[1] * g.del)),
+                         (float)(refc[2] - (g.mind[2] + bi[2] * g.del))};
+    const float c2 = (float)o.cutoff2;
+    Acc<float> a0, a1, a2, a3, a4, aw, ak;
+    for_segments<3, float>(g, cs, refc, bi, R, [&](uint32_t j0, uint32_t j1, bool own, float ox, float oy, float oz) {
+      const float xsh[3] = {ir[0] + ox, ir[1] + oy, ir[2] + oz};
+      for (uint32_t j = j0; j < j1; j++) {
+        const uint8_t bc = A.bc[j];
+        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
+        const float h = (float)A.h[j];
+        const float ds[3] = {xsh[0] - W.xr[j], xsh[1] - W.yr[j], xsh[2] - W.zr[j]};
+        if (!in_box<3, float>(ds, c2 * h)) continue;
+        const float ih = __fdividef(1.0f, h);
+        const float sv[3] = {ds[0] * ih, ds[1] * ih, ds[2] * ih};
+        const float w = w_gauss<3, float>(sv, h);
+        const float mw = (float)A.mass[j] * w;
+        const float mwr = mw * __fdividef(1.0f, (float)A.rho[j]);
+        a0.add(mw);
+        a1.add(mwr * (float)A.vx[j]);
+        a2.add(mwr * (float)A.vy[j]);
+        a3.add(mwr * (float)A.vz[j]);
+        a4.add(mwr * (float)A.e[j]);
+        if (!own) ak.add(mwr * (float)A.Y[j]);
+        aw.add(mwr);
+      }
+    });
+    u0 = a0.get(); u1 = a1.get(); u2 = a2.get(); u3 = a3.get(); u4 = a4.get();
+    ks = ak.get(); wn = aw.get();
+  }
+  if (wn > 0.) {
+    u0 /= wn; u1 /= wn; u2 /= wn; u3 /= wn; u4 /= wn;
+    ks = ks / wn;
+  } else {
+    u0 = 1.; u1 = u2 = u3 = u4 = 0.;
+    ks = 0.0;
+  }
+  const double vdotn = u1 * normal[0] + u2 * normal[1] + u3 * normal[2];
+  A.rho[i] = u0;
+  A.vx[i] = u1 - 2 * vdotn * normal[0];
+  A.vy[i] = u2 - 2 * vdotn * normal[1];
+  A.vz[i] = u3 - 2 * vdotn * normal[2];
+  A.e[i] = u4;
+  A.Y[i] = ks;
+  double gam, p, c, temp, cp = A.cp[i];
+  eos(o, u0, ks, u4, gam, p, c, temp, cp, o.lans != 0);
+  A.gam[i] = gam; A.p[i] = p; A.c[i] = c; A.T[i] = temp; A.cp[i] = cp;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -513,6 +632,10 @@ struct plume_ctx {
   std::vector<void*> adj_allocs;
   int adj_every = 0, adj_steps = 0;
   size_t adj_rows = 0;
+  // wall images (plume_set_wall_images), sorted by ghost key
+  uint64_t* img_key = nullptr;
+  double* img_xyz = nullptr;
+  int nimg = 0;
 };
 
 #define CK(call)                                                                      \
@@ -775,6 +898,24 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   record_ev(ctx, 9);
 }
 
+// wall boundary on the sorted state (per-bucket maximum h bounds its walk)
+static void apply_bc(plume_ctx* ctx) {
+  cudaStream_t st = ctx->st;
+  const int n = (int)ctx->n_alloc;
+  k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
+  k_hmax<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->hb, ctx->o.dim);
+  k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->nbk, ctx->hb, ctx->h27);
+  if (ctx->opt.precision == PLUME_PREC_MIXED)
+    k_apply_bcond<float><<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(
+        ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->img_key, ctx->img_xyz,
+        ctx->nimg, ctx->ts);
+  else
+    k_apply_bcond<double><<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(
+        ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->img_key, ctx->img_xyz,
+        ctx->nimg, ctx->ts);
+  ctx->launches += 4;
+}
+
 // one step, no host synchronisation
 static int step_async(plume_ctx* ctx) {
   cudaStream_t st = ctx->st;
@@ -788,6 +929,7 @@ static int step_async(plume_ctx* ctx) {
   record_ev(ctx, 1);
   int rc = search(ctx);
   if (rc) return rc;
+  if (ctx->nimg) apply_bc(ctx);
   record_ev(ctx, 2);
   ctx->host_step++;
   bool adaptive_now = ctx->o.adaptive && (ctx->host_step % ctx->o.interval) == 0;
@@ -1090,6 +1232,8 @@ int plume_destroy(plume_ctx* ctx) {
   if (!ctx) return PLUME_OK;
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->img_key) cudaFree(ctx->img_key);
+  if (ctx->img_xyz) cudaFree(ctx->img_xyz);
   for (void* p : ctx->adj_allocs) cudaFree(p);
   for (auto e : ctx->run_ev)
     if (e) cudaEventDestroy(e);
@@ -1763,6 +1907,10 @@ int plume_adjoint_record(plume_ctx* ctx, int nsteps, int checkpoint_every) {
     ctx->err = "adjoint: one 3D FP64 run with the Gaussian kernel and neighbour lists";
     return PLUME_E_INVALID;
   }
+  if (ctx->nimg) {
+    ctx->err = "adjoint: the wall boundary is not differentiated (clear the wall images)";
+    return PLUME_E_INVALID;
+  }
   for (void* p : ctx->adj_allocs) cudaFree(p);
   ctx->adj_allocs.clear();
   ctx->ckpts.clear();
@@ -1922,6 +2070,49 @@ int plume_adjoint_backward(plume_ctx* ctx, const PlumeSoA* final_bar, size_t n_f
   // the context continues from the window's final state
   int rc = restore_ckpt(ctx, ctx->ckpts.back());
   if (rc) return rc;
+  return finish_steps(ctx);
+}
+
+// ---------------------------------------------------------------- wall boundary
+int plume_set_wall_images(plume_ctx* ctx, const uint64_t* ghost_keys, const double* image_xyz, size_t n) {
+  if (!ctx || (n && (!ghost_keys || !image_xyz))) return PLUME_E_INVALID;
+  if (ctx->o.dim != 3) {
+    ctx->err = "wall images: 3D only";
+    return PLUME_E_INVALID;
+  }
+  if (n > (size_t)0x7fffffff) return PLUME_E_CAPACITY;
+  if (ctx->img_key) { cudaFree(ctx->img_key); ctx->img_key = nullptr; }
+  if (ctx->img_xyz) { cudaFree(ctx->img_xyz); ctx->img_xyz = nullptr; }
+  ctx->nimg = 0;
+  if (n == 0) return PLUME_OK;
+  std::vector<size_t> ord(n);
+  for (size_t i = 0; i < n; i++) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return ghost_keys[a] < ghost_keys[b]; });
+  std::vector<uint64_t> k(n);
+  std::vector<double> x(3 * n);
+  for (size_t r = 0; r < n; r++) {
+    k[r] = ghost_keys[ord[r]];
+    for (int a = 0; a < 3; a++) x[3 * r + a] = image_xyz[3 * ord[r] + a];
+    if (r && k[r] == k[r - 1]) {
+      ctx->err = "wall images: a ghost key twice";
+      return PLUME_E_INVALID;
+    }
+  }
+  CK(cudaMalloc(&ctx->img_key, 8 * n));
+  CK(cudaMalloc(&ctx->img_xyz, 24 * n));
+  CK(cudaMemcpy(ctx->img_key, k.data(), 8 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->img_xyz, x.data(), 24 * n, cudaMemcpyHostToDevice));
+  ctx->nimg = (int)n;
+  return PLUME_OK;
+}
+
+int plume_apply_bcond(plume_ctx* ctx) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (!ctx->nimg) return PLUME_OK;
+  int rc = search(ctx);
+  if (rc) return rc;
+  apply_bc(ctx);
+  CK(cudaGetLastError());
   return finish_steps(ctx);
 }
 

@@ -87,6 +87,8 @@ def lib():
         L.plume_batch_time.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int), P(C.c_int)]
         L.plume_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_int)]
         L.plume_adjoint_record.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.plume_set_wall_images.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_double), C.c_size_t]
+        L.plume_apply_bcond.argtypes = [C.c_void_p]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
                                              P(C.c_size_t), P(C.c_double)]
         _LIB = L

@@ -292,6 +292,43 @@ def plume_grid(lo, hi, h0, subcells=4) -> Grid:
                 flags=flags, face_index=face, domain_lo=tuple(lo), domain_hi=tuple(hi))
 
 
+def wall_images(case):
+    """The image table of search_bnd_images (bnd_image.cc:35-245) for a flat
+    ground at the domain's lower z: a wall ghost whose bucket is MIXED and
+    has an on-ground MIXED bucket (bottom face below ground, top face inside,
+    bucket.h:524-527) among itself and its 26 neighbours gets the image
+    2 intsct - x, intsct = (x, y, z_ground) (bucket.cc:294-360 for flat
+    ground).  Returns (ghost keys, (n, 3) image points)."""
+    g, ps = case.grid, case.particles
+    nb = np.array(g.nb)
+    mind = np.array(g.mindom)
+    zg = g.domain_lo[2]
+    wall = np.nonzero(ps.bc_type == BC_WALL)[0]
+    pos = np.stack([ps.x[wall], ps.y[wall], ps.z[wall]], axis=1)
+    b3 = np.clip(np.floor((pos - mind) / g.del_).astype(np.int64), 0, nb - 1)
+    flags = np.asarray(g.flags)
+    face = np.asarray(g.face_index).reshape(-1, 6)
+    mixed = (flags & BUCKET_MIXED) != 0
+    onground = mixed & (face[:, 4] == -1) & (face[:, 5] == 0)
+
+    def lin(b):
+        return (b[:, 2] * nb[1] + b[:, 1]) * nb[0] + b[:, 0]
+    sel = mixed[lin(b3)]
+    near = np.zeros(len(wall), dtype=bool)
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                q = b3 + np.array([dx, dy, dz])
+                ok = np.all((q >= 0) & (q < nb), axis=1)
+                qq = np.where(ok[:, None], q, 0)
+                near |= ok & onground[lin(qq)]
+    sel &= near
+    keys = ps.key[wall[sel]]
+    img = pos[sel].copy()
+    img[:, 2] = 2 * zg - img[:, 2]
+    return keys, img
+
+
 def options_3d(precision=PREC_FP64, h0=150.0, cva=711.0) -> Options:
     """3D plume switches (options.h:416-837 with ATMOSPHERE_TYPE 1, USE_GSPH 0)
     and constants (parameters.h:862-1041 with cp = 998, ash 0.95)."""

@@ -125,6 +125,19 @@ class Solver:
         self._check(self.L.plume_steps(self.ctx, n, None), "plume_steps")
         return None
 
+    # -- wall boundary -------------------------------------------------------
+    def set_wall_images(self, keys, xyz):
+        """image table of the wall boundary (keys of wall ghosts, (n, 3)
+        image points); empty arrays clear it"""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        self._check(self.L.plume_set_wall_images(self.ctx, keys.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                 xyz.ctypes.data_as(C.POINTER(C.c_double)), len(keys)),
+                    "plume_set_wall_images")
+
+    def apply_bcond(self):
+        self._check(self.L.plume_apply_bcond(self.ctx), "plume_apply_bcond")
+
     # -- adjoint --------------------------------------------------------------
     def adjoint_record(self, nsteps: int, checkpoint_every: int = 25):
         """nsteps steps keeping checkpoints for adjoint_backward"""

@@ -50,6 +50,9 @@ def golden_case(name):
     elif name == "plume_3d_small":
         c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
                            vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")
+    elif name == "plume_3d_bc":
+        c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                           vent_dx=25.0, duct_depth=300.0, seed=4, name="plume_3d_bc")
     else:
         raise KeyError(name)
     c.particles = unpack(d, "in_")

@@ -17,6 +17,10 @@ state and a summary of the reference's neighbour lists:
   plume_3d_small.npz   3D plume, 600 m cube at 50 m spacing with pressure,
                        wall and erupt ghosts, LANS + energy smoothing, steps
                        49..51 (step 50 runs adaptive_sml)
+  plume_3d_bc.npz      the same plume (seed 4) with the wall boundary: the
+                       flat-ground image table of cases.wall_images, the
+                       reference's apply_bcond before the loop and after each
+                       of steps 49..51
 
 Usage (in a container that has the reference tree):
   python tests/golden/make_golden.py [--ref /root/reference]
@@ -68,8 +72,8 @@ def pack(prefix, ps):
     return out
 
 
-def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_key=None):
-    steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden", dump_last)
+def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_key=None, images=None):
+    steps, lists = refio.run_ref(variant, case, nsteps, "/tmp/plume_golden", dump_last, images)
     extra = {}
     if perturb_key is not None:
         pc = case.__class__(**{**case.__dict__, "particles": case.particles.copy()})
@@ -105,6 +109,9 @@ def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_
         # the lists of the last step were built from the state before it
         d.update(pack("pre_", steps[-2]["particles"].sorted_by_key()))
     d.update(extra)
+    if images is not None:
+        d["img_key"] = np.asarray(images[0], dtype=np.uint64)
+        d["img_xyz"] = np.asarray(images[1], dtype=np.float64)
     np.savez_compressed(path, **d)
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
@@ -125,6 +132,14 @@ def main():
                        vent_dx=25.0, duct_depth=300.0, seed=3, name="plume_3d_small")
     c.step0 = 48
     make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_small.npz"))
+    make_bc()
+
+
+def make_bc():
+    c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                       vent_dx=25.0, duct_depth=300.0, seed=4, name="plume_3d_bc")
+    c.step0 = 48
+    make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_bc.npz"), images=cases.wall_images(c))
 
 
 if __name__ == "__main__":

@@ -225,3 +225,35 @@ def test_autotuner_returns_a_measured_candidate():
     best, table = tune_subcells(cases.plume_small(seed=0, precision=PREC_MIXED),
                                 candidates=(2, 4), steps=2, warmup=1)
     assert set(table) == {2, 4} and best in table and all(v > 0 for v in table.values())
+
+
+def test_wall_boundary_matches_oracle():
+    case, d = golden_case("plume_3d_bc")
+    s = Solver(case)
+    s.set_wall_images(d["img_key"], d["img_xyz"])
+    n = int(d["nsteps"])
+    s.steps(n)
+    s.apply_bcond()  # the reference applies it at the end of the last step
+    o = OracleRun(case)
+    o.set_images(d["img_key"], d["img_xyz"])
+    o.apply_bcond()
+    o.steps(n)
+    _check_fields(s.download(), o.ps, FP64_TOL)
+    _check_fields(s.download(), unpack(d, "out_"), FP64_TOL)
+
+
+def test_mixed_wall_boundary_density_error():
+    case, d = golden_case("plume_3d_bc")
+    out = {}
+    for prec in (0, PREC_MIXED):
+        c = case.__class__(**{**case.__dict__, "particles": case.particles.copy()})
+        c.options = case.options.__class__(**{**case.options.__dict__, "precision": prec})
+        s = Solver(c)
+        s.set_wall_images(d["img_key"], d["img_xyz"])
+        s.steps(3)
+        s.apply_bcond()
+        out[prec] = s.download().sorted_by_key()
+    a, b = out[0], out[PREC_MIXED]
+    for sel in (a.need_neigh(), a.bc_type == 2):
+        err = np.abs(b.rho[sel] - a.rho[sel]).sum() / np.abs(a.rho[sel]).sum()
+        assert err <= 1e-4, err

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from oracle.binding import OracleRun
+from plume_gpu import cases
 from plume_gpu.abi import BYTE_FIELDS
 from _util import field_errors, golden_case, set_summary, unpack
 
@@ -99,3 +100,32 @@ def test_oracle_3d_neighbour_sets_match_reference():
         want = np.sort(d["sample_flat"][offs[r]:offs[r + 1]])
         got = np.sort(kj[ki == k])
         np.testing.assert_array_equal(got, want)
+
+
+def test_oracle_wall_boundary_matches_reference():
+    # apply_bcond of the reference (bcond.cc) before the loop and after each
+    # of steps 49..51, flat-ground images
+    case, d = golden_case("plume_3d_bc")
+    o = OracleRun(case)
+    o.set_images(d["img_key"], d["img_xyz"])
+    o.apply_bcond()
+    dts = o.steps(int(d["nsteps"]))
+    np.testing.assert_allclose(dts, d["dt"], rtol=1e-12, atol=0)
+    ref = unpack(d, "out_")
+    err = field_errors(o.ps, ref)
+    assert max(err.values()) < 1e-12, err
+    walls = ref.sorted_by_key().bc_type == 2
+    moved = ref.sorted_by_key().rho[walls] != case.particles.sorted_by_key().rho[walls]
+    assert moved.sum() > 1000  # the boundary did set ghost states
+
+
+def test_wall_image_table_restates_search_bnd_images():
+    case, d = golden_case("plume_3d_bc")
+    k, x = cases.wall_images(case)
+    np.testing.assert_array_equal(k, d["img_key"])
+    np.testing.assert_array_equal(x, d["img_xyz"])
+    ps = case.particles
+    row = {int(kk): i for i, kk in enumerate(ps.key)}
+    g = np.array([[ps.x[row[int(kk)]], ps.y[row[int(kk)]], ps.z[row[int(kk)]]] for kk in k])
+    np.testing.assert_array_equal(x[:, :2], g[:, :2])
+    np.testing.assert_allclose(x[:, 2], -g[:, 2], rtol=0, atol=0)  # mirrored in z = 0
