@@ -311,6 +311,33 @@ int plume_batch_run(plume_ctx *ctx, int max_steps, int graph_steps, int *steps_d
 int plume_set_wall_images(plume_ctx *ctx, const uint64_t *ghost_keys, const double *image_xyz, size_t n);
 int plume_apply_bcond(plume_ctx *ctx);
 
+/* ---------------------------------------------------------------- eruption inlet
+ * add_new_erupt (src/plume/setup_erupt.cc:389-673) on the device.  While
+ * TimeProps::iferupt, every step ends by adding, for each duct column, the
+ * particles the inflow has made room for since the previous step:
+ * n = floor((fmod(t - dt, t_each) + dt) / t_each), t_each = spacing / vel,
+ * at z = bot + (t_add + i t_each) vel, with the vent state (Particle
+ * constructor, datstr/particle.cc:210-316: v = (0, 0, vel), Y, phase 2,
+ * bc_type 0, T and cp from the EOS, p, c and gamma the given values).  The
+ * key of a column's k-th particle is key_base + k ncol + column (col_count:
+ * particles already added per column, NULL = 0).  New particles take rows
+ * after the live ones; reserve_per_step bounds how many one step adds
+ * (more: PLUME_E_CAPACITY), and every step's sort covers that many extra
+ * rows.  NULL or ncol = 0 clears the inlet.  One 3D run; the adjoint entry
+ * points reject a context with an inlet. */
+typedef struct PlumeInlet {
+    size_t ncol;
+    const double *col_xy;               /* 2 per column                         */
+    const double *col_vel;              /* inflow velocity per column (> 0)      */
+    const unsigned long long *col_count;
+    double bot;                         /* simprops bot: duct bottom             */
+    double spacing;                     /* sml_of_phase2: particle spacing       */
+    double mass, h;                     /* mass_of_phase2, RATIO_SML_DX * spacing */
+    double rho, e, p, gamma, c, Y;      /* rhov_P, ev0_P, pv0_P, gamma_v_P, 340, 1 */
+    uint64_t key_base;
+} PlumeInlet;
+int plume_set_inlet(plume_ctx *ctx, const PlumeInlet *inlet, int reserve_per_step);
+
 /* ---------------------------------------------------------------- adjoint
  * Reverse-mode derivatives of a window of particle steps (one 3D run, FP64,
  * Gaussian kernel).  No counterpart in the reference.

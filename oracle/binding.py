@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 sys.path.insert(0, os.path.join(ROOT, "plume-sph_gb300"))
 
-from plume_gpu.abi import PlumeGrid, PlumeOptions, PlumeSoA, ParticleSet  # noqa: E402
+from plume_gpu.abi import (BYTE_FIELDS, DOUBLE_FIELDS, PlumeGrid, PlumeOptions, PlumeSoA,  # noqa: E402
+                           ParticleSet)
 
 _LIB = None
 
@@ -53,6 +54,13 @@ def lib():
         L.oracle_apply_bcond.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
                                          C.POINTER(PlumeSoA), C.c_size_t, C.POINTER(C.c_uint64),
                                          C.POINTER(C.c_double), C.c_size_t]
+        L.oracle_steps_inlet.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                         C.POINTER(PlumeSoA), C.POINTER(C.c_size_t), C.c_size_t,
+                                         C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
+                                         C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_size_t,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_double),
+                                         C.c_uint64]
         L.oracle_steps_bc.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
                                       C.POINTER(PlumeSoA), C.POINTER(C.c_size_t),
                                       C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
@@ -92,10 +100,44 @@ class OracleRun:
         if rc:
             raise RuntimeError(f"oracle_apply_bcond failed: {rc}")
 
+    def set_inlet(self, inlet: dict):
+        """eruption inlet (plume_gpu.cases.inlet), applied in every step"""
+        self.inlet = inlet
+        self.inlet_count = np.zeros(len(inlet["col_vel"]), dtype=np.uint64)
+
+    def _steps_inlet(self, nsteps, dts):
+        inl = self.inlet
+        cap = self.ps.n + nsteps * 8 * len(inl["col_vel"])
+        big = ParticleSet(cap)
+        for f in ["key"] + list(DOUBLE_FIELDS) + list(BYTE_FIELDS):
+            getattr(big, f)[:self.ps.n] = getattr(self.ps, f)
+        s = big.soa()
+        n = C.c_size_t(self.ps.n)
+        keys = getattr(self, "img_key", None)
+        ik = keys if keys is not None else np.zeros(0, np.uint64)
+        ix = self.img_xyz if keys is not None else np.zeros(0)
+        xy = np.ascontiguousarray(inl["col_xy"], dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(inl["col_vel"], dtype=np.float64)
+        par = np.array([inl[k] for k in ("bot", "spacing", "mass", "h", "rho", "e", "p", "gamma", "c", "Y")],
+                       dtype=np.float64)
+        D = C.POINTER(C.c_double)
+        rc = lib().oracle_steps_inlet(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n), cap,
+                                      C.byref(self.t), nsteps, dts, self.nthreads,
+                                      ik.ctypes.data_as(C.POINTER(C.c_uint64)), ix.ctypes.data_as(D), len(ik),
+                                      xy.ctypes.data_as(D), vel.ctypes.data_as(D),
+                                      self.inlet_count.ctypes.data_as(C.POINTER(C.c_uint64)), len(vel),
+                                      par.ctypes.data_as(D), int(inl["key_base"]))
+        if rc:
+            raise RuntimeError(f"oracle_steps_inlet failed: {rc}")
+        self.ps = big.take(np.arange(n.value))
+        return np.array(dts[:nsteps])
+
     def steps(self, nsteps: int):
         s = self.ps.soa()
         n = C.c_size_t(self.ps.n)
         dts = (C.c_double * max(nsteps, 1))()
+        if getattr(self, "inlet", None) is not None:
+            return self._steps_inlet(nsteps, dts)
         if getattr(self, "img_key", None) is not None:
             rc = lib().oracle_steps_bc(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
                                        C.byref(self.t), nsteps, dts, self.nthreads,

@@ -890,6 +890,58 @@ static int apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, s
     return rc;
 }
 
+/* ------------------------------------------------------------------ */
+/* eruption inlet, add_new_erupt (setup_erupt.cc:389-673)               */
+/* ------------------------------------------------------------------ */
+typedef struct Inlet {
+    const double *xy, *vel;     /* columns */
+    uint64_t     *count;        /* particles added per column so far */
+    size_t        ncol, cap;    /* cap: rows the particle arrays hold */
+    double bot, spacing, mass, h, rho, e, p, gamma, c, Y;
+    uint64_t key_base;
+} Inlet;
+
+/* Per column, the particles the inflow made room for since the previous
+ * step, with the vent state of the Particle constructor (particle.cc:
+ * 210-316); key of a column's k-th particle: key_base + k ncol + column. */
+static int add_new_erupt(const PlumeOptions *o, PlumeSoA *s, size_t *n, const OracleTime *t,
+                         const Inlet *in)
+{
+    double dt = t->dtime;
+    double t_total = t->time - dt;
+    for (size_t col = 0; col < in->ncol; col++) {
+        double vel = in->vel[col];
+        double t_each = in->spacing / vel;
+        double t_add = fmod(t_total, t_each) + dt;
+        int nn = (int)floor(t_add / t_each);
+        t_add = t_add - nn * t_each;
+        for (int i = 0; i < nn; i++) {
+            if (*n >= in->cap) return PLUME_E_CAPACITY;
+            size_t r = (*n)++;
+            s->key[r] = in->key_base + in->count[col]++ * (uint64_t)in->ncol + col;
+            s->x[r] = in->xy[2 * col];
+            s->y[r] = in->xy[2 * col + 1];
+            s->z[r] = in->bot + (t_add + i * t_each) * vel;
+            s->vx[r] = 0; s->vy[r] = 0; s->vz[r] = vel;
+            if (s->vsx) { s->vsx[r] = 0; s->vsy[r] = 0; s->vsz[r] = 0; }
+            s->mass[r] = in->mass;
+            s->h[r] = in->h;
+            s->rho[r] = in->rho;
+            s->e[r] = in->e;
+            s->Y[r] = in->Y;
+            s->phase[r] = 2;
+            s->bc_type[r] = 0;
+            s->involved[r] = 0;
+            s->cp[r] = 0.;
+            eos(o, s, r);
+            s->p[r] = in->p;
+            s->c[r] = in->c;
+            s->gamma[r] = in->gamma;
+        }
+    }
+    return PLUME_OK;
+}
+
 static int alloc_work(Work *w, size_t n)
 {
     size_t m = n ? n : 1;
@@ -946,13 +998,13 @@ int oracle_adaptive(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
 /* One step of the hot loop: 3D main.cc:217-471, 1D main.cc:676-750. */
 static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                       size_t *n, OracleTime *t, int nsteps, double *dt_log,
-                      int nthreads, const Images *im);
+                      int nthreads, const Images *im, const Inlet *inl);
 
 int oracle_steps(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                  size_t *n, OracleTime *t, int nsteps, double *dt_log,
                  int nthreads)
 {
-    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL);
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL, NULL);
 }
 
 int oracle_steps_bc(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
@@ -961,7 +1013,20 @@ int oracle_steps_bc(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                     size_t nimg)
 {
     Images im = { img_key, img_xyz, nimg };
-    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im);
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, NULL);
+}
+
+int oracle_steps_inlet(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                       size_t *n, size_t cap, OracleTime *t, int nsteps, double *dt_log,
+                       int nthreads, const uint64_t *img_key, const double *img_xyz,
+                       size_t nimg, const double *col_xy, const double *col_vel,
+                       uint64_t *col_count, size_t ncol, const double *par,
+                       uint64_t key_base)
+{
+    Images im = { img_key, img_xyz, nimg };
+    Inlet in = { col_xy, col_vel, col_count, ncol, cap, par[0], par[1], par[2], par[3], par[4],
+                 par[5], par[6], par[7], par[8], par[9], key_base };
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, &in);
 }
 
 int oracle_apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, size_t n,
@@ -973,7 +1038,7 @@ int oracle_apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, s
 
 static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                       size_t *n, OracleTime *t, int nsteps, double *dt_log,
-                      int nthreads, const Images *im)
+                      int nthreads, const Images *im, const Inlet *inl)
 {
     int rc = check_opts(o, g, s);
     if (rc) return rc;
@@ -1011,6 +1076,11 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
             rc = rebucket(o, g, s, n, oldb, &lost);
             free(oldb);
             if (rc) return rc;
+            /* main.cc:416-417 */
+            if (inl && inl->ncol && iferupt(o, t)) {
+                rc = add_new_erupt(o, s, n, t, inl);
+                if (rc) return rc;
+            }
             /* main.cc:468, after the inlet and before the output */
             rc = apply_bcond(o, g, s, *n, im);
             if (rc) return rc;

@@ -48,6 +48,16 @@ int oracle_apply_bcond(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA 
 int oracle_steps_bc(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s, size_t *n,
                     OracleTime *t, int nsteps, double *dt_log, int nthreads,
                     const uint64_t *img_key, const double *img_xyz, size_t nimg);
+/* oracle_steps_bc plus the eruption inlet (add_new_erupt,
+ * setup_erupt.cc:389-673) after the re-bucketing of every 3D step; the
+ * particle arrays hold cap rows; par = bot, spacing, mass, h, rho, e, p,
+ * gamma, c, Y of the vent; col_count is updated. */
+int oracle_steps_inlet(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s,
+                       size_t *n, size_t cap, OracleTime *t, int nsteps, double *dt_log,
+                       int nthreads, const uint64_t *img_key, const double *img_xyz,
+                       size_t nimg, const double *col_xy, const double *col_vel,
+                       uint64_t *col_count, size_t ncol, const double *par,
+                       uint64_t key_base);
 int oracle_steps(const PlumeOptions *opt, const PlumeGrid *grid,
                  PlumeSoA *s, size_t *n, OracleTime *t, int nsteps,
                  double *dt_log, int nthreads);

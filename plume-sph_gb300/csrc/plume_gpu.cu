@@ -529,6 +529,76 @@ __global__ void k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restric
   A.gam[i] = gam; A.p[i] = p; A.c[i] = c; A.T[i] = temp; A.cp[i] = cp;
 }
 
+// ---- eruption inlet (add_new_erupt, setup_erupt.cc:389-673) ---------------
+struct Inlet {
+  const double* xy;   // column positions (2 per column)
+  const double* vel;  // column inflow velocity
+  int ncol;
+  double bot, spacing, mass, h, rho, e, p, gam, c, Y;
+  uint64_t key_base;
+};
+// One thread per duct column, while iferupt: the particles the flow has made
+// room for since the previous step enter at the duct bottom, spaced by
+// `spacing` along the column, with the vent state (the Particle constructor
+// of particle.cc:210-316: v = (0, 0, vel), Y = 1, phase 2, EOS for T and
+// cp, then p, c and gamma set to the vent values).  New particles take the
+// dead rows after the live ones (row counter, at most `reserve` a step);
+// the key of a column's k-th particle is key_base + k ncol + column.
+__global__ void k_inject(Inlet in, const Opt* __restrict__ mopt, Dev A, const int* __restrict__ d_count,
+                         TimeState* ts, unsigned long long* __restrict__ colcnt, int* __restrict__ rowctr,
+                         int reserve, int cap_rows) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= in.ncol || !ts->erupt) return;
+  const Opt& o = mopt[0];
+  const double dt = ts->dtime;
+  const double t_total = ts->time - dt;
+  const double vel = in.vel[col];
+  const double t_each = in.spacing / vel;
+  double t_add = fmod(t_total, t_each) + dt;
+  const int nn = (int)floor(t_add / t_each);
+  t_add = t_add - nn * t_each;
+  for (int i = 0; i < nn; i++) {
+    const int r = atomicAdd(rowctr, 1);
+    const int row = *d_count + r;
+    if (r >= reserve || row >= cap_rows) {
+      set_status(ts, 5);
+      return;
+    }
+    const unsigned long long k = colcnt[col]++;
+    A.key[row] = in.key_base + k * (unsigned long long)in.ncol + (unsigned long long)col;
+    A.x[row] = in.xy[2 * col];
+    A.y[row] = in.xy[2 * col + 1];
+    A.z[row] = in.bot + (t_add + i * t_each) * vel;
+    A.vx[row] = 0; A.vy[row] = 0; A.vz[row] = vel;
+    A.vsx[row] = 0; A.vsy[row] = 0; A.vsz[row] = 0;
+    A.mass[row] = in.mass;
+    A.h[row] = in.h;
+    A.rho[row] = in.rho;
+    A.e[row] = in.e;
+    A.Y[row] = in.Y;
+    A.phase[row] = 2;
+    A.bc[row] = 0;
+    A.inv[row] = 0;
+    A.bkt[row] = 0;
+    A.mem[row] = 0;
+    double gam, p, c, temp, cp = 0.;
+    eos(o, in.rho, in.Y, in.e, gam, p, c, temp, cp, o.lans != 0);
+    A.T[row] = temp;
+    A.cp[row] = cp;
+    A.p[row] = in.p;
+    A.c[row] = in.c;
+    A.gam[row] = in.gam;
+  }
+}
+// the injected rows join the counted rows
+__global__ void k_inject_count(int* d_count, const int* __restrict__ rowctr, int reserve) {
+  *d_count += min(*rowctr, reserve);
+}
+__global__ void k_mark_dead(uint8_t* bc, size_t from, size_t to) {
+  const size_t r = from + blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r < to) bc[r] = BC_DEAD;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -636,6 +706,12 @@ struct plume_ctx {
   uint64_t* img_key = nullptr;
   double* img_xyz = nullptr;
   int nimg = 0;
+  // eruption inlet (plume_set_inlet)
+  Inlet inlet{};
+  double* inlet_buf = nullptr;              // column xy + vel
+  unsigned long long* inlet_colcnt = nullptr;
+  int* inlet_rowctr = nullptr;
+  int inlet_reserve = 0;
 };
 
 #define CK(call)                                                                      \
@@ -767,6 +843,12 @@ static int search(plume_ctx* ctx) {
   ctx->launches += 2;
   ctx->pending_dead = false;
   if (ctx->rec) snap_search(ctx);
+  if (ctx->inlet_reserve) {
+    // rows the inlet may fill this step: dead until it does
+    const size_t to = std::min(ctx->cap, (size_t)n + (size_t)ctx->inlet_reserve);
+    if (to > (size_t)n)
+      k_mark_dead<<<nblocks(to - (size_t)n, 256), 256, 0, st>>>(ctx->A.bc, (size_t)n, to);
+  }
   CK(cudaGetLastError());
   return PLUME_OK;
 }
@@ -944,6 +1026,16 @@ static int step_async(plume_ctx* ctx) {
   } else {
     if (mixed) launch_sweeps<1, float, true>(ctx, adaptive_now); else launch_sweeps<1, double, true>(ctx, adaptive_now);
     k_update_pos<1><<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
+  }
+  if (ctx->inlet_reserve) {  // add_new_erupt (main.cc:416-417)
+    cudaMemsetAsync(ctx->inlet_rowctr, 0, sizeof(int), st);
+    k_inject<<<nblocks(ctx->inlet.ncol), NTHREADS, 0, st>>>(ctx->inlet, ctx->d_opt, ctx->A, ctx->d_count, ctx->ts,
+                                                             ctx->inlet_colcnt, ctx->inlet_rowctr,
+                                                             ctx->inlet_reserve, (int)ctx->cap);
+    k_inject_count<<<1, 1, 0, st>>>(ctx->d_count, ctx->inlet_rowctr, ctx->inlet_reserve);
+    ctx->launches += 2;
+    // the next sort covers the rows the inlet may have filled
+    ctx->n_alloc = std::min(ctx->cap, ctx->n_alloc + (size_t)ctx->inlet_reserve);
   }
   k_end_step<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem);
   ctx->launches += 2;
@@ -1234,6 +1326,9 @@ int plume_destroy(plume_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->img_key) cudaFree(ctx->img_key);
   if (ctx->img_xyz) cudaFree(ctx->img_xyz);
+  if (ctx->inlet_buf) cudaFree(ctx->inlet_buf);
+  if (ctx->inlet_colcnt) cudaFree(ctx->inlet_colcnt);
+  if (ctx->inlet_rowctr) cudaFree(ctx->inlet_rowctr);
   for (void* p : ctx->adj_allocs) cudaFree(p);
   for (auto e : ctx->run_ev)
     if (e) cudaEventDestroy(e);
@@ -1911,6 +2006,10 @@ int plume_adjoint_record(plume_ctx* ctx, int nsteps, int checkpoint_every) {
     ctx->err = "adjoint: the wall boundary is not differentiated (clear the wall images)";
     return PLUME_E_INVALID;
   }
+  if (ctx->inlet_reserve) {
+    ctx->err = "adjoint: the inlet is not differentiated (clear it)";
+    return PLUME_E_INVALID;
+  }
   for (void* p : ctx->adj_allocs) cudaFree(p);
   ctx->adj_allocs.clear();
   ctx->ckpts.clear();
@@ -2114,6 +2213,56 @@ int plume_apply_bcond(plume_ctx* ctx) {
   apply_bc(ctx);
   CK(cudaGetLastError());
   return finish_steps(ctx);
+}
+
+// ---------------------------------------------------------------- eruption inlet
+int plume_set_inlet(plume_ctx* ctx, const PlumeInlet* in, int reserve_per_step) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (ctx->inlet_buf) { cudaFree(ctx->inlet_buf); ctx->inlet_buf = nullptr; }
+  if (ctx->inlet_colcnt) { cudaFree(ctx->inlet_colcnt); ctx->inlet_colcnt = nullptr; }
+  if (ctx->inlet_rowctr) { cudaFree(ctx->inlet_rowctr); ctx->inlet_rowctr = nullptr; }
+  ctx->inlet = Inlet{};
+  ctx->inlet_reserve = 0;
+  if (!in || in->ncol == 0) return PLUME_OK;
+  if (ctx->o.dim != 3 || ctx->nmem != 1 || !in->col_xy || !in->col_vel || reserve_per_step < 1 ||
+      !(in->spacing > 0)) {
+    ctx->err = "inlet: one 3D run, columns with velocities, spacing > 0, reserve >= 1";
+    return PLUME_E_INVALID;
+  }
+  for (size_t c = 0; c < in->ncol; c++)
+    if (!(in->col_vel[c] > 0)) {
+      ctx->err = "inlet: column velocity must be > 0";
+      return PLUME_E_INVALID;
+    }
+  const size_t nc = in->ncol;
+  std::vector<double> h(3 * nc);
+  for (size_t c = 0; c < nc; c++) {
+    h[2 * c] = in->col_xy[2 * c];
+    h[2 * c + 1] = in->col_xy[2 * c + 1];
+    h[2 * nc + c] = in->col_vel[c];
+  }
+  CK(cudaMalloc(&ctx->inlet_buf, 8 * 3 * nc));
+  CK(cudaMalloc(&ctx->inlet_colcnt, 8 * nc));
+  CK(cudaMalloc(&ctx->inlet_rowctr, sizeof(int)));
+  CK(cudaMemcpy(ctx->inlet_buf, h.data(), 8 * 3 * nc, cudaMemcpyHostToDevice));
+  std::vector<unsigned long long> cc(nc);
+  for (size_t c = 0; c < nc; c++) cc[c] = in->col_count ? in->col_count[c] : 0ull;
+  CK(cudaMemcpy(ctx->inlet_colcnt, cc.data(), 8 * nc, cudaMemcpyHostToDevice));
+  Inlet& d = ctx->inlet;
+  d.xy = ctx->inlet_buf;
+  d.vel = ctx->inlet_buf + 2 * nc;
+  d.ncol = (int)nc;
+  d.bot = in->bot; d.spacing = in->spacing; d.mass = in->mass; d.h = in->h; d.rho = in->rho;
+  d.e = in->e; d.p = in->p; d.gam = in->gamma; d.c = in->c; d.Y = in->Y;
+  d.key_base = in->key_base;
+  ctx->inlet_reserve = reserve_per_step;
+  // rows past the live ones are dead (the sort of the next step covers
+  // `reserve` of them)
+  const size_t from = ctx->n_alloc, to = std::min(ctx->cap, ctx->n_alloc + (size_t)reserve_per_step);
+  if (to > from) k_mark_dead<<<nblocks(to - from, 256), 256, 0, ctx->st>>>(ctx->A.bc, from, to);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->st));
+  return PLUME_OK;
 }
 
 int plume_phase_times(plume_ctx* ctx, float* ms, int n) {

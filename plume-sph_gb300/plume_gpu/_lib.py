@@ -10,7 +10,7 @@ import os
 import subprocess
 import threading
 
-from .abi import PlumeGrid, PlumeOptions, PlumeSoA, PlumeStepLog
+from .abi import PlumeGrid, PlumeInlet, PlumeOptions, PlumeSoA, PlumeStepLog
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
@@ -89,6 +89,7 @@ def lib():
         L.plume_adjoint_record.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.plume_set_wall_images.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_double), C.c_size_t]
         L.plume_apply_bcond.argtypes = [C.c_void_p]
+        L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
                                              P(C.c_size_t), P(C.c_double)]
         _LIB = L

@@ -79,6 +79,14 @@ class PlumeSoA(C.Structure):
                [(f, _BP) for f in BYTE_FIELDS]
 
 
+class PlumeInlet(C.Structure):
+    _fields_ = [("ncol", C.c_size_t), ("col_xy", C.POINTER(C.c_double)), ("col_vel", C.POINTER(C.c_double)),
+                ("col_count", C.POINTER(C.c_ulonglong)), ("bot", C.c_double), ("spacing", C.c_double),
+                ("mass", C.c_double), ("h", C.c_double), ("rho", C.c_double), ("e", C.c_double),
+                ("p", C.c_double), ("gamma", C.c_double), ("c", C.c_double), ("Y", C.c_double),
+                ("key_base", C.c_uint64)]
+
+
 class PlumeStepLog(C.Structure):
     _fields_ = [("dt", C.c_double), ("time", C.c_double), ("step", C.c_int),
                 ("status", C.c_int), ("n_total", C.c_uint64), ("n_real", C.c_uint64),

@@ -329,6 +329,28 @@ def wall_images(case):
     return keys, img
 
 
+def inlet(case):
+    """The eruption inlet of add_new_erupt (setup_erupt.cc:389-673) for a
+    plume built by plume_3d: the duct's particle columns (spacing vent_dx,
+    inside the vent radius), bottom = the duct's lowest particle, the vent
+    state of the Particle constructor (particle.cc:210-316: p = the vent
+    pressure, c = 340 m/s, gamma of the vent mixture) and uniform inflow at
+    the vent velocity (ERUPT_VELOCITY_PROF 0).  Keys continue after the
+    case's largest key."""
+    ps, info, opt = case.particles, case.info, case.options
+    vent = (ps.bc_type == BC_ERUPT) & (ps.phase == 2)
+    vdx = info["vent_dx"]
+    cols = np.unique(np.round(np.stack([ps.x[vent], ps.y[vent]], axis=1) / (0.5 * vdx)).astype(np.int64),
+                     axis=0) * (0.5 * vdx)
+    v0 = float(ps.vz[vent].max())
+    i0 = int(np.nonzero(vent)[0][0])
+    return {"col_xy": cols.astype(np.float64), "col_vel": np.full(len(cols), v0),
+            "bot": float(ps.z[vent].min()), "spacing": vdx, "mass": float(ps.mass[i0]), "h": vdx,
+            "rho": float(ps.rho[i0]), "e": float(ps.e[i0]), "p": info.get("p0", 101325.0),
+            "gamma": float(ps.gamma[i0]), "c": 340.0, "Y": 1.0,
+            "key_base": int(ps.key.max()) + 1}
+
+
 def options_3d(precision=PREC_FP64, h0=150.0, cva=711.0) -> Options:
     """3D plume switches (options.h:416-837 with ATMOSPHERE_TYPE 1, USE_GSPH 0)
     and constants (parameters.h:862-1041 with cp = 998, ash 0.95)."""

@@ -135,6 +135,23 @@ class Solver:
                                                  xyz.ctypes.data_as(C.POINTER(C.c_double)), len(keys)),
                     "plume_set_wall_images")
 
+    def set_inlet(self, inlet: dict | None, reserve_per_step: int = 0):
+        """eruption inlet (cases.inlet); None clears it; the reserve defaults
+        to 4 particles per column"""
+        from .abi import PlumeInlet
+        if inlet is None:
+            self._check(self.L.plume_set_inlet(self.ctx, None, 0), "plume_set_inlet")
+            return
+        xy = np.ascontiguousarray(inlet["col_xy"], dtype=np.float64).reshape(-1)
+        vel = np.ascontiguousarray(inlet["col_vel"], dtype=np.float64)
+        self._inlet_keep = (xy, vel)
+        s = PlumeInlet(len(vel), xy.ctypes.data_as(C.POINTER(C.c_double)),
+                       vel.ctypes.data_as(C.POINTER(C.c_double)), None, inlet["bot"], inlet["spacing"],
+                       inlet["mass"], inlet["h"], inlet["rho"], inlet["e"], inlet["p"], inlet["gamma"],
+                       inlet["c"], inlet["Y"], inlet["key_base"])
+        res = reserve_per_step or 4 * len(vel)
+        self._check(self.L.plume_set_inlet(self.ctx, C.byref(s), res), "plume_set_inlet")
+
     def apply_bcond(self):
         self._check(self.L.plume_apply_bcond(self.ctx), "plume_apply_bcond")
 

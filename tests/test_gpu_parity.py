@@ -257,3 +257,24 @@ def test_mixed_wall_boundary_density_error():
     for sel in (a.need_neigh(), a.bc_type == 2):
         err = np.abs(b.rho[sel] - a.rho[sel]).sum() / np.abs(a.rho[sel]).sum()
         assert err <= 1e-4, err
+
+
+def test_inlet_and_wall_boundary_match_oracle():
+    # add_new_erupt and apply_bcond on the device over six steps that add
+    # two particle layers to every duct column
+    case = cases.plume_small(seed=0)
+    inl = cases.inlet(case)
+    keys, xyz = cases.wall_images(case)
+    s = Solver(case)
+    s.set_wall_images(keys, xyz)
+    s.set_inlet(inl)
+    s.steps(6)
+    s.apply_bcond()
+    o = OracleRun(case)
+    o.set_images(keys, xyz)
+    o.set_inlet(inl)
+    o.apply_bcond()
+    o.steps(6)
+    g = s.download()
+    assert g.n == o.ps.n and (g.key >= inl["key_base"]).sum() == 24
+    _check_fields(g, o.ps, FP64_TOL)
