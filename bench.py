@@ -380,6 +380,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="test-size workload")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     ap.add_argument("--no-tune", action="store_true", help="fixed cell tiles (4^3 per bucket)")
+    ap.add_argument("--subcells", type=int, default=0, help="fixed cell tiles (N^3 per bucket), no tuning")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-wall-bc", action="store_true",
                     help="leave the wall ghosts' states fixed (no apply_bcond in the step)")
@@ -410,7 +411,9 @@ def main():
     case = make(PREC_MIXED)
     tuning = None
     from plume_gpu.autotune import tune_subcells, with_subcells
-    if not args.no_tune:
+    if args.subcells:
+        case = with_subcells(case, args.subcells)
+    elif not args.no_tune:
         t0 = time.perf_counter()
         best, table = tune_subcells(case, candidates=(3, 4, 5, 6), steps=3, warmup=2)
         tuning = {"subcells": best, "ms_per_step": {str(k): round(v, 3) for k, v in table.items()},
