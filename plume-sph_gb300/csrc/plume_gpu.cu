@@ -411,105 +411,174 @@ __global__ void k_set_ghost(const Opt* __restrict__ mopt, Dev A, const int* __re
 }
 
 // ---- wall boundary (apply_bcond, bcond.cc:24-249, BC_FOR_KX 1) ------------
-// One thread per wall ghost with an image: the Shepard-normalised SPH
-// averages of rho, v, e of the real and pressure-ghost particles
-// (contr_image, particle.h:562-565) inside CUTOFF2 h_j of the image point,
-// over the image's bucket and its 26 neighbours (Y over the neighbours only,
-// as the reference accumulates it), the velocity reflected in the wall
-// along the ghost-to-image direction (reflect, sph_lib.cc:76-83), written
-// to the ghost with its EOS.  Runs after the step's sort, where the
-// reference runs it at the end of the previous step (main.cc:196, 468):
-// nothing in between reads ghost states.  T = double: the reference's FP64
-// arithmetic; T = float (mixed path): FP32 weights on bucket-relative
-// coordinates with compensated FP32 sums, like the pair sweeps.
-template <typename T>
-__global__ void k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restrict__ geo, Dev A, Work W,
-                              const uint32_t* __restrict__ cs_all, const double* __restrict__ h27_all,
-                              const int* __restrict__ d_count, const uint64_t* __restrict__ ikey,
-                              const double* __restrict__ ixyz, int nimg, TimeState* ts_all) {
+// Maps every live wall ghost (bc 2) to its image by key (binary search of
+// the key-sorted image table): map[member * nimg + image] = row.  A ghost
+// without an image is left alone, as in the reference.
+__global__ void k_bc_map(Dev A, const int* __restrict__ d_count, const uint64_t* __restrict__ ikey, int nimg,
+                         int* __restrict__ map) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *d_count || A.bc[i] != 2) return;
   const uint64_t k = A.key[i];
-  int lo = 0, hi = nimg;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (ikey[mid] < k) lo = mid + 1; else hi = mid;
+  int l = 0, h = nimg;
+  while (l < h) {
+    const int mid = (l + h) >> 1;
+    if (ikey[mid] < k) l = mid + 1; else h = mid;
   }
-  if (lo >= nimg || ikey[lo] != k) return;
+  if (l < nimg && ikey[l] == k) map[(size_t)A.mem[i] * nimg + l] = i;
+}
+
+// binary64 -> binary32 rounding toward zero on the integer pipe (the
+// exponent rebiased, the top 23 fraction bits kept): the FP64 pipe, which
+// executes F2F, is narrow on this part.  Below the binary32 normal range the
+// result is a signed zero, above it a signed infinity; NaN stays NaN.
+__device__ __forceinline__ float f32_rz(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int ex = (int)((hi >> 20) & 0x7ffu);
+  const int e = ex - 1023 + 127;
+  unsigned r = sign | ((unsigned)e << 23) | ((unsigned)(b >> 29) & 0x7fffffu);
+  if (e <= 0) r = sign;
+  if (e >= 255) r = sign | 0x7f800000u;
+  if (ex == 0x7ff && (b & 0xfffffffffffffull)) r = 0x7fc00000u;
+  return __uint_as_float(r);
+}
+
+// BCG threads per (member, image) slot, slots in image-key order, so that
+// the threads of a warp walk overlapping candidate sets together: the
+// Shepard-normalised SPH averages of rho, v, e of the real and
+// pressure-ghost particles (contr_image, particle.h:562-565) inside CUTOFF2
+// h_j of the image point, over the image's bucket and its 26 neighbours (Y
+// over the neighbours only, as the reference accumulates it); the velocity
+// reflected in the wall along the ghost-to-image direction (reflect,
+// sph_lib.cc:76-83), written to the ghost with its EOS.  Runs after the
+// step's sort, where the reference runs it at the end of the previous step
+// (main.cc:196, 468): nothing in between reads ghost states.
+// The walk goes over rows of fine cells, dealt round-robin to the slot's
+// threads (partial sums combined by shuffles): the x-run of a row is
+// contiguous in the sorted order across bucket boundaries, so one loop takes
+// the whole run and finds a candidate's bucket (at most three along x) from
+// the two boundary rows.  T = double: the reference's FP64 arithmetic on absolute
+// coordinates; T = float (mixed path): FP32 weights on bucket-relative
+// coordinates, fields narrowed on the integer pipe, compensated FP32 sums.
+constexpr int BCG = 8;  // threads per image slot (a power of two dividing 32)
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restrict__ geo,
+                                                          Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                                                          const double* __restrict__ h27_all,
+                                                          const int* __restrict__ map, int nslots, int nimg,
+                                                          const double* __restrict__ ixyz, TimeState* ts_all) {
+  constexpr bool MIXED = sizeof(T) == 4;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / BCG, sub = gt % BCG;
+  if (t >= nslots) return;
+  // the slot's threads are BCG consecutive lanes; they leave together
+  const unsigned gmask = ((1u << BCG) - 1u) << ((threadIdx.x & 31) & ~(BCG - 1));
+  const int i = map[t];
+  if (i < 0) return;
+  const int lo = t % nimg;
   const int m = A.mem[i];
   const Geo& g = geo[m];
   const Opt& o = mopt[m];
   TimeState* ts = ts_all + m;
   const uint32_t* cs = cs_all + g.cell_base;
   const double refc[3] = {ixyz[3 * lo], ixyz[3 * lo + 1], ixyz[3 * lo + 2]};
-  double normal[3] = {refc[0] - A.x[i], refc[1] - A.y[i], refc[2] - A.z[i]};
-  const double d = sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
-#pragma unroll
-  for (int a = 0; a < 3; a++) normal[a] /= d;
   bool o1, o2, o3;
   int bi[3];
   bi[0] = bucket_axis(refc[0], g.mind[0], g.del, g.idel, g.nb[0], &o1);
   bi[1] = bucket_axis(refc[1], g.mind[1], g.del, g.idel, g.nb[1], &o2);
   bi[2] = bucket_axis(refc[2], g.mind[2], g.del, g.idel, g.nb[2], &o3);
   if (o1 || o2 || o3) {
-    set_status(ts, 6);
+    if (!sub) set_status(ts, 6);
     return;
   }
   const int b = (bi[2] * g.nb[1] + bi[1]) * g.nb[0] + bi[0];
   const double R = o.ksupport * h27_all[g.bucket_base + b] * (1.0 + 1e-10);
-  double u0 = 0, u1 = 0, u2 = 0, u3 = 0, u4 = 0, wn = 0, ks = 0;
-  if constexpr (sizeof(T) == 8) {
-    for_segments<3, double>(g, cs, refc, bi, R, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
-      for (uint32_t j = j0; j < j1; j++) {
-        const uint8_t bc = A.bc[j];
-        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
-        const double h = A.h[j];
-        const double ds[3] = {refc[0] - A.x[j], refc[1] - A.y[j], refc[2] - A.z[j]};
-        if (!in_box<3, double>(ds, o.cutoff2 * h)) continue;
-        const double sv[3] = {ds[0] / h, ds[1] / h, ds[2] / h};
-        const double w = w_gauss<3, double>(sv, h);
-        const double mj = A.mass[j], rj = A.rho[j];
-        u0 += mj * w;
-        u1 += mj * w * A.vx[j] / rj;
-        u2 += mj * w * A.vy[j] / rj;
-        u3 += mj * w * A.vz[j] / rj;
-        u4 += mj * w * A.e[j] / rj;
-        if (!own) ks += mj * w * A.Y[j] / rj;
-        wn += mj * w / rj;
-      }
-    });
-  } else {
-    // the image point relative to its bucket, candidates relative to theirs
-    const float ir[3] = {(float)(refc[0] - (g.mind[0] + bi[0] * g.del)),
-                         (float)(refc[1] - (g.mind[1] + bi[1] * g.del)),
-                         (float)(refc[2] - (g.mind[2] + bi[2] * g.del))};
-    const float c2 = (float)o.cutoff2;
-    Acc<float> a0, a1, a2, a3, a4, aw, ak;
-    for_segments<3, float>(g, cs, refc, bi, R, [&](uint32_t j0, uint32_t j1, bool own, float ox, float oy, float oz) {
-      const float xsh[3] = {ir[0] + ox, ir[1] + oy, ir[2] + oz};
-      for (uint32_t j = j0; j < j1; j++) {
-        const uint8_t bc = A.bc[j];
-        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
-        const float h = (float)A.h[j];
-        const float ds[3] = {xsh[0] - W.xr[j], xsh[1] - W.yr[j], xsh[2] - W.zr[j]};
-        if (!in_box<3, float>(ds, c2 * h)) continue;
-        const float ih = __fdividef(1.0f, h);
-        const float sv[3] = {ds[0] * ih, ds[1] * ih, ds[2] * ih};
-        const float w = w_gauss<3, float>(sv, h);
-        const float mw = (float)A.mass[j] * w;
-        const float mwr = mw * __fdividef(1.0f, (float)A.rho[j]);
-        a0.add(mw);
-        a1.add(mwr * (float)A.vx[j]);
-        a2.add(mwr * (float)A.vy[j]);
-        a3.add(mwr * (float)A.vz[j]);
-        a4.add(mwr * (float)A.e[j]);
-        if (!own) ak.add(mwr * (float)A.Y[j]);
-        aw.add(mwr);
-      }
-    });
-    u0 = a0.get(); u1 = a1.get(); u2 = a2.get(); u3 = a3.get(); u4 = a4.get();
-    ks = ak.get(); wn = aw.get();
+  // cell box of the walk: the reach R, clipped to the 27 buckets
+  int clo[3], chi[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const int l = cell_axis(g, a, refc[a] - R, nullptr, nullptr);
+    const int h = cell_axis(g, a, refc[a] + R, nullptr, nullptr);
+    clo[a] = max(l, max((bi[a] - 1) * g.s, 0));
+    chi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
   }
+  // the image point relative to its bucket (mixed path)
+  const float ir[3] = {(float)(refc[0] - (g.mind[0] + bi[0] * g.del)),
+                       (float)(refc[1] - (g.mind[1] + bi[1] * g.del)),
+                       (float)(refc[2] - (g.mind[2] + bi[2] * g.del))};
+  const float delf = (float)g.del;
+  const float c2f = (float)o.cutoff2;
+  Acc<T> a0, a1, a2, a3, a4, aw, ak;
+  const int bx0 = clo[0] / g.s;  // bucket of the first cell of every x-run
+  const int ny = chi[1] - clo[1] + 1, nrow = ny * (chi[2] - clo[2] + 1);
+  for (int r = sub; r < nrow; r += BCG) {
+    const int cz = clo[2] + r / ny, cy = clo[1] + r % ny;
+    const int bz = cz / g.s;
+    {
+      const int by = cy / g.s;
+      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      const uint32_t j0 = cs[rowbase + clo[0]], j1 = cs[rowbase + chi[0] + 1];
+      const int c1 = (bx0 + 1) * g.s, c2 = (bx0 + 2) * g.s;
+      const uint32_t s1 = c1 <= chi[0] ? cs[rowbase + c1] : j1;
+      const uint32_t s2 = c2 <= chi[0] ? cs[rowbase + c2] : j1;
+      const int own_run = (by == bi[1] && bz == bi[2]) ? bi[0] - bx0 : -1;
+      const float oy = (float)(bi[1] - by) * delf, oz = (float)(bi[2] - bz) * delf;
+      const float ox0 = (float)(bi[0] - bx0) * delf;
+      for (uint32_t j = j0; j < j1; j++) {
+        const uint8_t bc = A.bc[j];
+        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
+        const int run = (j >= s1) + (j >= s2);
+        const bool own = run == own_run;
+        if constexpr (MIXED) {
+          const float ox = ox0 - (float)run * delf;
+          const float ds[3] = {ir[0] + ox - W.xr[j], ir[1] + oy - W.yr[j], ir[2] + oz - W.zr[j]};
+          const float h = f32_rz(A.h[j]);
+          if (!in_box<3, float>(ds, c2f * h)) continue;
+          const float ih = __fdividef(1.0f, h);
+          const float sv[3] = {ds[0] * ih, ds[1] * ih, ds[2] * ih};
+          const float w = w_gauss<3, float>(sv, h);
+          const float mw = f32_rz(A.mass[j]) * w;
+          const float mwr = mw * __fdividef(1.0f, f32_rz(A.rho[j]));
+          a0.add(mw);
+          a1.add(mwr * f32_rz(A.vx[j]));
+          a2.add(mwr * f32_rz(A.vy[j]));
+          a3.add(mwr * f32_rz(A.vz[j]));
+          a4.add(mwr * f32_rz(A.e[j]));
+          if (!own) ak.add(mwr * f32_rz(A.Y[j]));
+          aw.add(mwr);
+        } else {
+          const double h = A.h[j];
+          const double ds[3] = {refc[0] - A.x[j], refc[1] - A.y[j], refc[2] - A.z[j]};
+          if (!in_box<3, double>(ds, o.cutoff2 * h)) continue;
+          const double sv[3] = {ds[0] / h, ds[1] / h, ds[2] / h};
+          const double w = w_gauss<3, double>(sv, h);
+          const double mj = A.mass[j], rj = A.rho[j];
+          a0.add(mj * w);
+          a1.add(mj * w * A.vx[j] / rj);
+          a2.add(mj * w * A.vy[j] / rj);
+          a3.add(mj * w * A.vz[j] / rj);
+          a4.add(mj * w * A.e[j] / rj);
+          if (!own) ak.add(mj * w * A.Y[j] / rj);
+          aw.add(mj * w / rj);
+        }
+      }
+    }
+  }
+  double u0 = a0.get(), u1 = a1.get(), u2 = a2.get(), u3 = a3.get(), u4 = a4.get();
+  double wn = aw.get(), ks = ak.get();
+#pragma unroll
+  for (int off = BCG / 2; off > 0; off >>= 1) {
+    u0 += __shfl_xor_sync(gmask, u0, off);
+    u1 += __shfl_xor_sync(gmask, u1, off);
+    u2 += __shfl_xor_sync(gmask, u2, off);
+    u3 += __shfl_xor_sync(gmask, u3, off);
+    u4 += __shfl_xor_sync(gmask, u4, off);
+    wn += __shfl_xor_sync(gmask, wn, off);
+    ks += __shfl_xor_sync(gmask, ks, off);
+  }
+  if (sub) return;
   if (wn > 0.) {
     u0 /= wn; u1 /= wn; u2 /= wn; u3 /= wn; u4 /= wn;
     ks = ks / wn;
@@ -517,6 +586,10 @@ __global__ void k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restric
     u0 = 1.; u1 = u2 = u3 = u4 = 0.;
     ks = 0.0;
   }
+  double normal[3] = {refc[0] - A.x[i], refc[1] - A.y[i], refc[2] - A.z[i]};
+  const double d = sqrt(normal[0] * normal[0] + normal[1] * normal[1] + normal[2] * normal[2]);
+#pragma unroll
+  for (int a = 0; a < 3; a++) normal[a] /= d;
   const double vdotn = u1 * normal[0] + u2 * normal[1] + u3 * normal[2];
   A.rho[i] = u0;
   A.vx[i] = u1 - 2 * vdotn * normal[0];
@@ -706,6 +779,7 @@ struct plume_ctx {
   uint64_t* img_key = nullptr;
   double* img_xyz = nullptr;
   int nimg = 0;
+  int* bc_map = nullptr;  // row of (member, image), -1 when absent
   // eruption inlet (plume_set_inlet)
   Inlet inlet{};
   double* inlet_buf = nullptr;              // column xy + vel
@@ -987,15 +1061,18 @@ static void apply_bc(plume_ctx* ctx) {
   k_hmax_reset<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->hb, ctx->nbk);
   k_hmax<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->hb, ctx->o.dim);
   k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->nbk, ctx->hb, ctx->h27);
+  const int nslots = ctx->nmem * ctx->nimg;
+  cudaMemsetAsync(ctx->bc_map, 0xff, sizeof(int) * (size_t)nslots, st);
+  k_bc_map<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->img_key, ctx->nimg, ctx->bc_map);
   if (ctx->opt.precision == PLUME_PREC_MIXED)
-    k_apply_bcond<float><<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(
-        ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->img_key, ctx->img_xyz,
-        ctx->nimg, ctx->ts);
+    k_apply_bcond<float><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs,
+                                                               ctx->h27, ctx->bc_map, nslots, ctx->nimg,
+                                                               ctx->img_xyz, ctx->ts);
   else
-    k_apply_bcond<double><<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(
-        ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->img_key, ctx->img_xyz,
-        ctx->nimg, ctx->ts);
-  ctx->launches += 4;
+    k_apply_bcond<double><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs,
+                                                                ctx->h27, ctx->bc_map, nslots, ctx->nimg,
+                                                                ctx->img_xyz, ctx->ts);
+  ctx->launches += 5;
 }
 
 // one step, no host synchronisation
@@ -1326,6 +1403,7 @@ int plume_destroy(plume_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->img_key) cudaFree(ctx->img_key);
   if (ctx->img_xyz) cudaFree(ctx->img_xyz);
+  if (ctx->bc_map) cudaFree(ctx->bc_map);
   if (ctx->inlet_buf) cudaFree(ctx->inlet_buf);
   if (ctx->inlet_colcnt) cudaFree(ctx->inlet_colcnt);
   if (ctx->inlet_rowctr) cudaFree(ctx->inlet_rowctr);
@@ -2182,6 +2260,7 @@ int plume_set_wall_images(plume_ctx* ctx, const uint64_t* ghost_keys, const doub
   if (n > (size_t)0x7fffffff) return PLUME_E_CAPACITY;
   if (ctx->img_key) { cudaFree(ctx->img_key); ctx->img_key = nullptr; }
   if (ctx->img_xyz) { cudaFree(ctx->img_xyz); ctx->img_xyz = nullptr; }
+  if (ctx->bc_map) { cudaFree(ctx->bc_map); ctx->bc_map = nullptr; }
   ctx->nimg = 0;
   if (n == 0) return PLUME_OK;
   std::vector<size_t> ord(n);
@@ -2201,6 +2280,9 @@ int plume_set_wall_images(plume_ctx* ctx, const uint64_t* ghost_keys, const doub
   CK(cudaMalloc(&ctx->img_xyz, 24 * n));
   CK(cudaMemcpy(ctx->img_key, k.data(), 8 * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->img_xyz, x.data(), 24 * n, cudaMemcpyHostToDevice));
+  // one slot per (member, image)
+  if ((size_t)ctx->nmem * n > (size_t)0x7fffffff) return PLUME_E_CAPACITY;
+  CK(cudaMalloc(&ctx->bc_map, sizeof(int) * (size_t)ctx->nmem * n));
   ctx->nimg = (int)n;
   return PLUME_OK;
 }
