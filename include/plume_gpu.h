@@ -108,6 +108,29 @@ extern "C" {
 #define PLUME_KERNEL_M4     1 /* cubic B-spline (Monaghan M4), radial support
                                  2h, used by the Sod / ensemble workloads     */
 
+/* ---- momentum/energy discretisation (USE_GSPH, options.h:136-142) ------ */
+#define PLUME_METHOD_SPH   0  /* artificial viscosity (mom_engr_update.cc:29-439) */
+#define PLUME_METHOD_GSPH  1  /* Godunov SPH: a Riemann problem per pair
+                                 (mom_engr_update.cc:441-1146, SHEAR_VEL_APP 2,
+                                 RP_MASS_WEIGHTED 0)                           */
+
+/* ---- GSPH Riemann solver (RIEMANN_SOLVER, options.h:185-192, 586-593) -- */
+#define PLUME_RIEMANN_ROE   0 /* Roe_RP_Solver, sph_lib.cc:1694-1750 (3D default) */
+#define PLUME_RIEMANN_HLLC  1 /* HLLC_RP_Solver, sph_lib.cc:1753-1908,
+                                 HLL_WAVE_SPEED_EVA 0 (1D default)            */
+
+/* ---- GSPH Riemann-problem states (MINI_DERIVATIVE_COND, options.h:156-170,
+ *      559-573): zeroth order (the particles' own states) or linear in the
+ *      calc_gradients gradients, with a fallback where a state turns
+ *      negative --------------------------------------------------------- */
+#define PLUME_RECON_NONE       0   /* linear, no fallback                      */
+#define PLUME_RECON_EACH       1   /* per variable and side                    */
+#define PLUME_RECON_PAIRWISE   2   /* density / pressure on both sides         */
+#define PLUME_RECON_ALL        3   /* every variable on both sides             */
+#define PLUME_RECON_ZEROTH     4   /* zeroth order (1D default)                */
+#define PLUME_RECON_EACH_SHOCK 10  /* EACH, plus zeroth-order velocities where
+                                      3 |u_l - u_r| > min(c_i, c_j) (3D default) */
+
 /* Compile-time switches and physical constants of the reference, as a
  * runtime struct.  Field comments give the reference symbol. */
 typedef struct PlumeOptions {
@@ -138,6 +161,16 @@ typedef struct PlumeOptions {
     int    max_steps;
     int    max_per_bucket;      /* MAX_PARTICLES_PER_BUCKET                    */
     size_t capacity;            /* device particle capacity of the context     */
+    int    method;              /* PLUME_METHOD_* (USE_GSPH)                   */
+    int    gsph_solver;         /* PLUME_RIEMANN_* (RIEMANN_SOLVER)            */
+    int    gsph_recon;          /* PLUME_RECON_* (MINI_DERIVATIVE_COND)        */
+    int    gsph_vol;            /* GSPH_SPECIFIC_VOL_APP: 0 interface at the
+                                   midpoint, 1 linear, 3 cubic specific volume
+                                   (Compute_sij_star, sph_lib.cc:1655-1692)   */
+    int    gsph_mono;           /* GSPH_MODIFIED_MONOTONICITY: 0 or 1 (|u_j-u_i|) */
+    int    gsph_gradients;      /* 1: calc_gradients every GSPH step, as the
+                                   reference does; 0: only when the
+                                   reconstruction reads them                  */
 } PlumeOptions;
 
 /* Bucket grid (the background mesh of src/datstr/bucket.h).  Bucket (i,j,k)
@@ -234,6 +267,17 @@ int plume_set_time(plume_ctx *ctx, double time, int step, int ioutput,
  * the count. */
 int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
                          uint64_t *key_j, size_t cap, size_t *n);
+
+/* Gradients of the last GSPH step (calc_gradients, calculate_gradient.cc:
+ * 22-208: the renormalised SPH gradient of rho, the D velocity components
+ * and p of every particle over its neighbour list, zero when the list holds
+ * 20 particles or fewer inside the CUTOFF2*h box), with the keys of their
+ * rows.  grad receives (D+2)*D doubles per particle: d rho/dx_k, d v_0/dx_k,
+ * ..., d p/dx_k (k fastest).  PLUME_E_INVALID when the last step computed
+ * none (method SPH, or zeroth-order reconstruction with gsph_gradients 0).
+ * If cap is smaller than the particle count nothing is written and *n
+ * receives the count. */
+int plume_gsph_gradients(plume_ctx *ctx, uint64_t *key, double *grad, size_t cap, size_t *n);
 
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):

@@ -65,6 +65,11 @@ def lib():
                                       C.POINTER(PlumeSoA), C.POINTER(C.c_size_t),
                                       C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
                                       C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_size_t]
+        L.oracle_steps_grad.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                        C.POINTER(PlumeSoA), C.POINTER(C.c_size_t),
+                                        C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
+                                        C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t,
+                                        C.POINTER(C.c_size_t)]
         _LIB = L
     return _LIB
 
@@ -149,6 +154,28 @@ class OracleRun:
                                     C.byref(self.t), nsteps, dts, self.nthreads)
         if rc:
             raise RuntimeError(f"oracle_steps failed: {rc}")
+        if n.value != self.ps.n:
+            self.ps = self.ps.take(np.arange(n.value))
+        return np.array(dts[:nsteps])
+
+    def steps_grad(self, nsteps: int):
+        """steps(), keeping the GSPH gradients of the last step in
+        self.grad = (keys, (n, (D+2)*D) array), or None"""
+        s = self.ps.soa()
+        n = C.c_size_t(self.ps.n)
+        dts = (C.c_double * max(nsteps, 1))()
+        D = self.case.options.dim
+        cap = self.ps.n
+        g = np.zeros((cap, (D + 2) * D))
+        gk = np.zeros(cap, dtype=np.uint64)
+        ng = C.c_size_t(0)
+        rc = lib().oracle_steps_grad(C.byref(self.opt), C.byref(self.grid), C.byref(s), C.byref(n),
+                                     C.byref(self.t), nsteps, dts, self.nthreads,
+                                     g.ctypes.data_as(C.POINTER(C.c_double)),
+                                     gk.ctypes.data_as(C.POINTER(C.c_uint64)), cap, C.byref(ng))
+        if rc:
+            raise RuntimeError(f"oracle_steps_grad failed: {rc}")
+        self.grad = (gk[:ng.value], g[:ng.value]) if ng.value else None
         if n.value != self.ps.n:
             self.ps = self.ps.take(np.arange(n.value))
         return np.array(dts[:nsteps])

@@ -9,7 +9,8 @@
 // ghosts, inlet) with the particles of the case file, and calls, in the
 // order of src/plume/main.cc:217-408 (3D) or :676-729 (1D):
 //   timestep, TimeProps::incrtime, search_neighs_consth (3D),
-//   adaptive_sml, mom_engr_update, smooth_density, smooth_velocity (3D LANS),
+//   adaptive_sml, calc_gradients (USE_GSPH builds), mom_engr_update,
+//   smooth_density, smooth_velocity (3D LANS),
 //   update_pos, update_particles_in_bucket (3D), TimeProps::ifoutput.
 //
 // Case file (little endian):
@@ -26,7 +27,8 @@
 //   double dt, time; int32 step, ioutput; int64 n; the same field arrays in
 //   ascending input-index order (key array = input keys); after the last
 //   step: int64 nlists; per need_neigh particle: uint64 key_i, int64 len,
-//   uint64 key_j[len] (list order as stored by the reference).
+//   uint64 key_j[len] (list order as stored by the reference); GSPH builds
+//   (USE_GSPH 1) then append the last step's gradients (dump_gradients).
 
 #include <cstdio>
 #include <cstdlib>
@@ -251,6 +253,38 @@ static void dump_lists(FILE *fo, THashTable *P, const Case &c) {
   }
 }
 
+#if USE_GSPH != 0
+// GSPH builds: the gradients that calc_gradients stored in the last step,
+// char[4] "GRAD"; int64 n; uint64 key[n]; then per particle (D+2)*D doubles
+// (d rho, d v_0 .. d v_D-1, d p; x_k fastest), input-index order.
+static void dump_gradients(FILE *fo, THashTable *P, const Case &c) {
+  std::vector<std::pair<unsigned, Particle *>> rows;
+  THTIterator it(P);
+  Particle *p;
+  while ((p = (Particle *)it.next())) rows.push_back(std::make_pair(p->getKey().key[2], p));
+  std::sort(rows.begin(), rows.end(),
+            [](const std::pair<unsigned, Particle *> &a, const std::pair<unsigned, Particle *> &b) {
+              return a.first < b.first;
+            });
+  fwrite("GRAD", 1, 4, fo);
+  int64_t n = (int64_t)rows.size();
+  fwrite(&n, 8, 1, fo);
+  for (auto &r : rows) {
+    uint64_t k = c.key[r.first];
+    fwrite(&k, 8, 1, fo);
+  }
+  for (auto &r : rows) {
+    Particle *q = r.second;
+    const double *g[5] = { q->get_density_derivative(), q->get_velocity_u_derivative(),
+                           q->get_velocity_v_derivative(), q->get_velocity_w_derivative(),
+                           q->get_pressure_derivative() };
+    const int idx3[5] = { 0, 1, 2, 3, 4 }, idx1[3] = { 0, 1, 4 };
+    const int nq = DIMENSION + 2;
+    for (int a = 0; a < nq; a++) fwrite(g[DIMENSION == 3 ? idx3[a] : idx1[a]], 8, DIMENSION, fo);
+  }
+}
+#endif
+
 int main(int argc, char **argv) {
   if (argc != 3) {
     fprintf(stderr, "usage: %s case.bin out.bin\n", argv[0]);
@@ -433,6 +467,9 @@ int main(int argc, char **argv) {
     double dt = timestep(P, tp);
     tp->incrtime(&dt);
     adaptive_sml(0, P);
+#if USE_GSPH != 0
+    calc_gradients(P);  // main.cc:697-699
+#endif
     mom_engr_update(0, P, tp, simprops);
     smooth_density(P);
     update_pos(P, tp, matprops);
@@ -441,6 +478,9 @@ int main(int argc, char **argv) {
     tp->incrtime(&dt);
     search_neighs_consth(0, P, BG);
     if ((tp->step) % SML_UPDATE_INT == 0) adaptive_sml(0, P);
+#if USE_GSPH != 0
+    calc_gradients(P);  // main.cc:341-343
+#endif
     mom_engr_update(0, P, tp, simprops);
     smooth_density(P);
 #if HAVE_TURBULENCE_LANS != 0
@@ -458,6 +498,9 @@ int main(int argc, char **argv) {
     }
   }
   dump_lists(fo, P, c);
+#if USE_GSPH != 0
+  dump_gradients(fo, P, c);
+#endif
   fseek(fo, 12, SEEK_SET);
   int32_t nd = ndumped;
   fwrite(&nd, 4, 1, fo);

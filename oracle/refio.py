@@ -81,6 +81,14 @@ def read_result(path):
         (ki,) = take("<Q")
         (ln,) = take("<q")
         lists[ki] = np.frombuffer(data, "<u8", ln, off).copy(); off += 8 * ln
+    if data[off:off + 4] == b"GRAD":
+        # GSPH builds: the last step's gradients, (n, (D+2)*D) by key
+        off += 4
+        (ng,) = take("<q")
+        gk = np.frombuffer(data, "<u8", ng, off).copy(); off += 8 * ng
+        nq = (dim + 2) * dim
+        g = np.frombuffer(data, "<f8", ng * nq, off).copy().reshape(ng, nq); off += 8 * ng * nq
+        steps[-1]["grad"] = (gk, g)
     return steps, lists
 
 

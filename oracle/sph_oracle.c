@@ -31,6 +31,7 @@
 #define OR_E_SMOOTH  4.0                 /* E_SMOOTH_RATIO, constant.h:185 */
 #define OR_MSFRC_TH  1.0e-6              /* MSFRC_THRESH, constant.h:80    */
 #define OR_TINY      1.0e-8              /* TINY, constant.h:76            */
+#define OR_C_SHOCK   3.0                 /* C_SHOCK, constant.h:103        */
 /* cubic B-spline normalisations (1D: 2/3, 3D: 1/pi) */
 #define OR_M4_S1     0.66666666666666663
 #define OR_M4_S3     0.31830988618379069
@@ -247,9 +248,21 @@ static void lists_free(Lists *L)
  * (neighs.cc:89-92), then, for the 26 adjacent buckets in x-major order
  * (preprocess.cc:287-313), the particles inside the list_factor*h_i box
  * (neighs.cc:84,117-131).  Particles of one bucket keep index order. */
+static int build_lists_3d_for(const PlumeOptions *o, const PlumeGrid *g,
+                              const PlumeSoA *s, size_t n, size_t ntarget,
+                              Lists *L, int nthreads, int all);
 static int build_lists_3d(const PlumeOptions *o, const PlumeGrid *g,
                           const PlumeSoA *s, size_t n, size_t ntarget,
                           Lists *L, int nthreads)
+{
+    return build_lists_3d_for(o, g, s, n, ntarget, L, nthreads, 0);
+}
+
+/* all: lists for every particle, as search_neighs_consth builds them under
+ * USE_GSPH (neighs.cc:76, 136: ghosts need lists for their gradients) */
+static int build_lists_3d_for(const PlumeOptions *o, const PlumeGrid *g,
+                              const PlumeSoA *s, size_t n, size_t ntarget,
+                              Lists *L, int nthreads, int all)
 {
     long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
     long *bk = (long *)malloc(sizeof(long) * (n ? n : 1));
@@ -271,14 +284,14 @@ static int build_lists_3d(const PlumeOptions *o, const PlumeGrid *g,
     /* targets */
     size_t nt = 0;
     for (size_t i = 0; i < n; i++)
-        if (need_neigh(s->bc_type[i]) && nt < ntarget) nt++;
+        if ((all || need_neigh(s->bc_type[i])) && nt < ntarget) nt++;
     L->start = (size_t *)calloc(n + 1, sizeof(size_t));
     size_t *cnt = (size_t *)calloc(n + 1, sizeof(size_t));
     char *is_t = (char *)calloc(n ? n : 1, 1);
     {
         size_t c = 0;
         for (size_t i = 0; i < n && c < nt; i++)
-            if (need_neigh(s->bc_type[i])) { is_t[i] = 1; c++; }
+            if (all || need_neigh(s->bc_type[i])) { is_t[i] = 1; c++; }
     }
     int nbx = g->nb[0], nby = g->nb[1], nbz = g->nb[2];
     /* two passes: count, then fill */
@@ -496,6 +509,373 @@ static int momentum_pass(const PlumeOptions *o, PlumeSoA *s, size_t n,
     }
     if (err) return err;
     /* commit loop, mom_engr_update.cc:412-432 */
+    for (size_t i = 0; i < n; i++) {
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        s->vx[i] = w->nv[0][i];
+        if (D == 3) { s->vy[i] = w->nv[1][i]; s->vz[i] = w->nv[2][i]; }
+        s->e[i] = w->ne[i];
+        eos(o, s, i);
+    }
+    return PLUME_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* GSPH (USE_GSPH 1)                                                    */
+/* ------------------------------------------------------------------ */
+/* Gradients (calc_gradients, calculate_gradient.cc:22-208) of rho, the D
+ * velocity components and p of every particle with a list: the SPH sums
+ * A_ab = -sum_j dx_a (m_j/rho_j) dW_b(dx/h_i, h_i) and
+ * F_a,q = -sum_j (f_q,i - f_q,j) (m_j/rho_j) dW_a over the list entries
+ * j != i inside the CUTOFF2*h_i box; grad = linsolve(A, F) when more than
+ * 20 entries were inside the box, else zero.  linsolve (sph_lib.cc:
+ * 161-182) multiplies F by inv3(A) in 3D and by inv1(A) = -1/A in 1D (the
+ * reference's sign).  Layout: grad[i*NQ*D + q*D + k], q = rho, v_0..v_D-1,
+ * p. */
+static void gsph_gradients(const PlumeOptions *o, const PlumeSoA *s, size_t n,
+                           const Lists *L, double *grad, int nthreads)
+{
+    const int D = o->dim, NQ = D + 2;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        double *gi = grad + i * (size_t)(NQ * D);
+        for (int q = 0; q < NQ * D; q++) gi[q] = 0.0;
+        /* 1D lists belong to the need_neigh particles only (add_air.cc:470-479) */
+        if (D == 1 && !need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        double xi[3], vi[3], AA[9] = { 0 }, FF[3][5] = { { 0 } };
+        coords(s, i, D, xi);
+        vel(s, i, D, 0, vi);
+        double hi = s->h[i], supp = o->cutoff2 * hi;
+        int nreal = 0;
+        FOR_LIST(L, D, n, i, j, {
+            if (j != i) {
+                double xj[3], dx[3], sv[3];
+                coords(s, j, D, xj);
+                for (int k = 0; k < D; k++) dx[k] = xi[k] - xj[k];
+                if (in_support(dx, supp, D)) {
+                    nreal++;
+                    double dwm[3], vj[3];
+                    for (int k = 0; k < D; k++) sv[k] = dx[k] / hi;
+                    for (int k = 0; k < D; k++) dwm[k] = d_weight_gauss(sv, hi, k, D) * s->mass[j] / s->rho[j];
+                    for (int a = 0; a < D; a++)
+                        for (int b = 0; b < D; b++) AA[a * D + b] -= dx[a] * dwm[b];
+                    vel(s, j, D, 0, vj);
+                    for (int a = 0; a < D; a++) {
+                        FF[a][0] -= (s->rho[i] - s->rho[j]) * dwm[a];
+                        for (int b = 0; b < D; b++) FF[a][b + 1] -= (vi[b] - vj[b]) * dwm[a];
+                        FF[a][NQ - 1] -= (s->p[i] - s->p[j]) * dwm[a];
+                    }
+                }
+            }
+        });
+        if (nreal <= 20) continue;
+        double Ai[9];
+        if (D == 1) {
+            Ai[0] = -1 / AA[0];
+        } else {
+            /* inv3 (sph_lib.cc:86-110) returns the cofactor matrix over the
+             * determinant, entry (a,b) = C_ab: the inverse of A transposed,
+             * which is the inverse here since A is symmetric */
+            double C[9];
+            C[0] = AA[4] * AA[8] - AA[5] * AA[7];
+            C[1] = -(AA[3] * AA[8] - AA[5] * AA[6]);
+            C[2] = AA[3] * AA[7] - AA[4] * AA[6];
+            C[3] = -(AA[1] * AA[8] - AA[2] * AA[7]);
+            C[4] = AA[0] * AA[8] - AA[2] * AA[6];
+            C[5] = -(AA[0] * AA[7] - AA[1] * AA[6]);
+            C[6] = AA[1] * AA[5] - AA[2] * AA[4];
+            C[7] = -(AA[0] * AA[5] - AA[2] * AA[3]);
+            C[8] = AA[0] * AA[4] - AA[1] * AA[3];
+            double id = 1.0 / (AA[0] * C[0] + AA[1] * C[1] + AA[2] * C[2]);
+            for (int q = 0; q < 9; q++) Ai[q] = C[q] * id;
+        }
+        /* ff = Ai F (matrix_matrix_mult, sph_lib.cc:136-156); gradU[q*D+a] = ff[a][q] */
+        for (int a = 0; a < D; a++)
+            for (int q = 0; q < NQ; q++) {
+                double acc = 0.0;
+                for (int b = 0; b < D; b++) acc += Ai[a * D + b] * FF[b][q];
+                gi[q * D + a] = acc;
+            }
+    }
+}
+
+/* HLLC Riemann solver of the GSPH step (HLLC_RP_Solver, sph_lib.cc:
+ * 1753-1908, HLL_WAVE_SPEED_EVA 0, USE_GSPH 1): Roe-averaged interface
+ * state, wave speeds S_l = min(v_l - c_l, -c_lr), S_r = max(v_r + c_r, c_lr)
+ * relative to the Roe velocity, contact speed S_m; returns p* and u* of the
+ * region that contains the interface.  l is particle j's side, r particle
+ * i's. */
+static void hllc(double dl, double dr, double pl, double pr, double ul, double ur, double gl, double gr,
+                 double *p_star, double *u_star)
+{
+    double rdl = sqrt(dl), rdr = sqrt(dr);
+    double den = 1.0 / (rdl + rdr);
+    double ulr = (ul * rdl + ur * rdr) * den;
+    double plr = (pl * rdl + pr * rdr) * den;
+    double glr = (gl * rdl + gr * rdr) * den;
+    double dlr = (dl * rdl + dr * rdr) * den;
+    double clr = sqrt(glr * plr / dlr);
+    double vl = ul - ulr, vr = ur - ulr;
+    double cl = sqrt(gl * pl / dl), cr = sqrt(gr * pr / dr);
+    double Sl = fmin(vl - cl, -clr);
+    double Sr = fmax(vr + cr, clr);
+    double Sm = (dr * vr * (Sr - vr) - dl * vl * (Sl - vl) + pl - pr) / (dr * (Sr - vr) - dl * (Sl - vl));
+    double ph = dl * (vl - Sl) * (vl - Sm) + pl;
+    double Ml = dl * ul, Mr = dr * ur;
+    double El = dl * (pl / (dl * (gl - 1)) + 0.5 * ul * ul);
+    double Er = dr * (pr / (dr * (gr - 1)) + 0.5 * ur * ur);
+    if (Sl > 0) {
+        *p_star = pl;
+        *u_star = ul;
+    } else if (Sl <= 0 && Sm > 0) {
+        *p_star = Sm / (Sl - Sm) * ((Sl - vl) * Ml + (ph - pl)) + ph;
+        *u_star = (Sm / (Sl - Sm) * ((Sl - vl) * El + ph * Sm - pl * vl) + (Sm + ulr) * ph) / (*p_star);
+    } else if (Sm <= 0 && Sr > 0) {
+        *p_star = Sm / (Sr - Sm) * ((Sr - vr) * Mr + (ph - pr)) + ph;
+        *u_star = (Sm / (Sr - Sm) * ((Sr - vr) * Er + ph * Sm - pr * vr) + (Sm + ulr) * ph) / (*p_star);
+    } else if (Sr <= 0) {
+        *p_star = pr;
+        *u_star = ur;
+    } else {
+        /* a NaN wave speed: the reference leaves p*, u* unset */
+        *p_star = NAN;
+        *u_star = NAN;
+    }
+}
+
+/* Roe Riemann solver (Roe_RP_Solver, sph_lib.cc:1694-1750, RP_MASS_WEIGHTED
+ * 0, FLUID_COMPRESSIBILITY 0): Roe averages, the Lagrangian sound speed
+ * rho_lr c_lr, p* = p_lr - c/2 (u_r - u_l), u* = u_lr - (p_r - p_l)/(2c). */
+static void roe(double dl, double dr, double pl, double pr, double ul, double ur, double gl, double gr,
+                double *p_star, double *u_star)
+{
+    double rdl = sqrt(dl), rdr = sqrt(dr);
+    double den = 1.0 / (rdl + rdr);
+    double plr = (pl * rdl + pr * rdr) * den;
+    double glr = (gl * rdl + gr * rdr) * den;
+    double dlr = (dl * rdl + dr * rdr) * den;
+    double clr = sqrt(glr * plr / dlr);
+    clr = dlr * clr;
+    double ulr = (ul * rdl + ur * rdr) * den;
+    *p_star = plr - 0.5 * clr * (ur - ul);
+    *u_star = ulr - 0.5 * (pr - pl) / clr;
+}
+
+/* One pair's Riemann problem (Riemann_Solver, sph_lib.cc:2247-2598, USE_GSPH
+ * 1, RP_MASS_WEIGHTED 0, SWITCH_OFF_AV_FOR_EXPAN 0, SHEAR_VEL_APP 2): the
+ * states projected on e = (x_i - x_j)/|x_i - x_j|; unless the
+ * reconstruction is zeroth order, the gradients projected on e, limited
+ * (monotonicity: opposite velocity slopes, or C_SHOCK (u_j - u_i) -- its
+ * absolute value under the modified condition -- above the smaller sound
+ * speed), the interface placed at s* (GSPH_SPECIFIC_VOL_APP 0: midpoint;
+ * 1, 3: Compute_sij_star, sph_lib.cc:1655-1692) and the states moved to it
+ * over c dt/2 with the MINI_DERIVATIVE_COND fallback; the Roe or HLLC
+ * solution u* put back along e with the Roe-averaged transverse velocity. */
+typedef struct GsphSide {
+    double rho, p, c, gam, h;
+    const double *v;   /* velocity used by the step (smoothed under LANS) */
+    const double *g;   /* gradients (rho, v, p) x D, NULL when not computed */
+} GsphSide;
+
+static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const double *xj,
+                         const GsphSide *I, const GsphSide *J, double dt_half,
+                         double *p_star, double *v_star)
+{
+    double dx[3], e[3], dist = 0.0;
+    for (int k = 0; k < D; k++) dx[k] = xi[k] - xj[k];
+    for (int k = 0; k < D; k++) dist += dx[k] * dx[k];
+    dist = sqrt(dist);
+    for (int k = 0; k < D; k++) e[k] = dx[k] / dist;
+    double ui = 0.0, uj = 0.0;
+    for (int k = 0; k < D; k++) {
+        ui += I->v[k] * e[k];
+        uj += J->v[k] * e[k];
+    }
+    const int recon = o->gsph_recon;
+    double dr = I->rho, ur = ui, pr = I->p, dl = J->rho, ul = uj, pl = J->p;
+    if (recon != PLUME_RECON_ZEROTH) {
+        const int NQ = D + 2;
+        const double z3[15] = { 0 };
+        const double *gi = I->g ? I->g : z3, *gj = J->g ? J->g : z3;
+        double drhoi = 0, dpi = 0, drhoj = 0, dpj = 0, dv_i[3] = { 0, 0, 0 }, dv_j[3] = { 0, 0, 0 };
+        for (int k = 0; k < D; k++) {
+            drhoi += gi[0 * D + k] * e[k];
+            drhoj += gj[0 * D + k] * e[k];
+            dpi += gi[(NQ - 1) * D + k] * e[k];
+            dpj += gj[(NQ - 1) * D + k] * e[k];
+            for (int c = 0; c < D; c++) {
+                dv_i[c] += gi[(1 + c) * D + k] * e[k];
+                dv_j[c] += gj[(1 + c) * D + k] * e[k];
+            }
+        }
+        double ddui = 0.0, dduj = 0.0;
+        for (int c = 0; c < D; c++) {
+            ddui += dv_i[c] * e[c];
+            dduj += dv_j[c] * e[c];
+        }
+        if (ddui * dduj < 0) ddui = dduj = 0.0;
+        double du = uj - ui;
+        if (o->gsph_mono) du = fabs(du);
+        if (OR_C_SHOCK * du > fmin(I->c, J->c)) drhoi = dpi = ddui = drhoj = dpj = dduj = 0.0;
+        double Si = 0.5 * dist, Sj = -Si, sij = 0.0;
+        const double hij = 0.5 * (I->h + J->h), Vi = 1 / I->rho, Vj = 1 / J->rho;
+        if (o->gsph_vol == 1) {
+            double Cc = (Vi - Vj) / dist, Dd = (Vi + Vj) * 0.5, hsq = hij * hij;
+            double Vsq = 0.25 * hsq * Cc * Cc + Dd * Dd;
+            sij = 0.5 * (hsq * Cc * Dd) / Vsq;
+        } else if (o->gsph_vol == 3) {
+            double DVi = -Vi * Vi * drhoi, DVj = -Vj * Vj * drhoj;
+            double d2 = dist * dist, d3 = d2 * dist;
+            double A = -2.0 * (Vi - Vj) / d3 + (DVi + DVj) / d2;
+            double B = 0.5 * (DVi - DVj) / dist;
+            double Cc = 1.5 * (Vi - Vj) / dist - 0.25 * (DVi + DVj);
+            double Dd = 0.5 * (Vi + Vj) - 0.125 * (DVi - DVj) * dist;
+            double hsq = hij * hij, h4 = hsq * hsq, h6 = h4 * hsq;
+            double Vsq = 0.234375 * h6 * A * A + 0.1875 * h4 * (2.0 * A * Cc + B * B) +
+                         0.25 * hsq * (2.0 * B * Dd + Cc * Cc) + Dd * Dd;
+            sij = (0.46875 * h6 * A * B + 0.375 * h4 * (A * Dd + B * Cc) + 0.5 * hsq * Cc * Dd) / Vsq;
+        }
+        double delta_i = sij + I->c * dt_half - Si;
+        double delta_j = sij - J->c * dt_half - Sj;
+        dr = I->rho + drhoi * delta_i;
+        ur = ui + ddui * delta_i;
+        pr = I->p + dpi * delta_i;
+        dl = J->rho + drhoj * delta_j;
+        ul = uj + dduj * delta_j;
+        pl = J->p + dpj * delta_j;
+        if (recon == PLUME_RECON_ALL) {
+            if (dr < 0 || dl < 0 || pr < 0 || pl < 0) {
+                dr = I->rho; ur = ui; pr = I->p; dl = J->rho; ul = uj; pl = J->p;
+            }
+        } else if (recon == PLUME_RECON_PAIRWISE) {
+            if (dr < 0 || dl < 0) { dr = I->rho; dl = J->rho; }
+            if (pr < 0 || pl < 0) { pr = I->p; pl = J->p; }
+        } else if (recon == PLUME_RECON_EACH || recon == PLUME_RECON_EACH_SHOCK) {
+            if (dr < 0) dr = I->rho;
+            if (dl < 0) dl = J->rho;
+            if (pr < 0) pr = I->p;
+            if (pl < 0) pl = J->p;
+            if (recon == PLUME_RECON_EACH_SHOCK && 3.0 * fabs(ul - ur) > fmin(I->c, J->c)) {
+                ul = uj;
+                ur = ui;
+            }
+        }
+    }
+    double u_star;
+    if (o->gsph_solver == PLUME_RIEMANN_HLLC)
+        hllc(dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
+    else
+        roe(dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
+    double rdl = sqrt(dl), rdr = sqrt(dr);
+    double den = 1.0 / (rdl + rdr);
+    double ulr = (ul * rdl + ur * rdr) * den;
+    for (int k = 0; k < D; k++) {
+        double vlr = (J->v[k] * rdl + I->v[k] * rdr) * den;
+        v_star[k] = e[k] * u_star + vlr - ulr * e[k];
+    }
+}
+
+/* GSPH momentum and energy (mom_engr_update.cc:441-1146, ME_UPDATE_SML 2,
+ * ADAPTIVE_SML 1, HAVE_ENERGY_CUT 0): per need_neigh particle two passes
+ * over its list entries j != i inside the CUTOFF2*h_i box whose
+ * V_i^2 dW(dx/h_ij, h_ij) is non-zero (h_ij = (h_i+h_j)/2):
+ *   pass 1: rhs_v -= m_j (p* (V_i^2 + V_j^2) dW - tau dW), tau the LANS
+ *           stress SPH_epsilon_mom(v_i - v_j, V_j) (0 without LANS);
+ *   pass 2: the same Riemann problems again, rhs_e -= m_j (v* - xdot*) .
+ *           (p* (V_i^2 + V_j^2) dW - tau dW) + the LANS heat flux, with
+ *           xdot* = v_i + dt/2 (rhs_v + g);
+ * then v += dt (rhs_v + g e_D), e += dt (rhs_e + v_i,D g), and the commit
+ * with the EOS.  grad: the gradients of gsph_gradients or NULL. */
+static int gsph_momentum_pass(const PlumeOptions *o, PlumeSoA *s, size_t n, const Lists *L,
+                              double dt, const double *grad, Work *w, int nthreads)
+{
+    const int D = o->dim, NQ = D + 2;
+    const double grav = -o->g;
+    const double dt_half = 0.5 * dt;
+    int err = PLUME_OK;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (long ii = 0; ii < (long)n; ii++) {
+        size_t i = (size_t)ii;
+        if (!need_neigh(s->bc_type[i])) continue;
+        if (D == 3 && L->start[i + 1] == L->start[i]) continue;
+        double xi[3], veli[3], rhs_v[3] = { 0, 0, 0 }, rhs_e = 0;
+        coords(s, i, D, xi);
+        double hi = s->h[i];
+        double supp = o->cutoff2 * hi;
+        if (!(s->rho[i] > 0)) {
+#pragma omp critical
+            err = PLUME_E_NONPOSITIVE;
+            continue;
+        }
+        double Vi = 1.0 / s->rho[i];
+        vel(s, i, D, o->lans, veli);
+        GsphSide I = { s->rho[i], s->p[i], s->c[i], s->gamma[i], hi, veli,
+                       grad ? grad + i * (size_t)(NQ * D) : NULL };
+        for (int pass = 0; pass < 2; pass++) {
+            double xdot[3];
+            for (int k = 0; k < D; k++) xdot[k] = veli[k] + 0.5 * dt * (rhs_v[k] + (k == D - 1 ? grav : 0.0));
+            FOR_LIST(L, D, n, i, j, {
+                if (j != i) {
+                    double xj[3], dx[3], si[3];
+                    coords(s, j, D, xj);
+                    for (int k = 0; k < D; k++) dx[k] = xi[k] - xj[k];
+                    if (in_support(dx, supp, D)) {
+                        double Vj = 1.0 / s->rho[j];
+                        double hij = 0.5 * (hi + s->h[j]);
+                        double dwdx[3], vsqi[3], vsqj[3], max_dw = 0.0;
+                        for (int k = 0; k < D; k++) si[k] = dx[k] / hij;
+                        for (int k = 0; k < D; k++) dwdx[k] = d_weight_gauss(si, hij, k, D);
+                        for (int k = 0; k < D; k++) {
+                            vsqi[k] = Vi * Vi * dwdx[k];
+                            vsqj[k] = Vj * Vj * dwdx[k];
+                        }
+                        for (int k = 0; k < D; k++)
+                            if (fabs(vsqi[k]) > max_dw) max_dw = fabs(vsqi[k]);
+                        if (max_dw > 0) {
+                            double velj[3], velij[3], p_star, v_star[3], tau = 0.0;
+                            vel(s, j, D, o->lans, velj);
+                            GsphSide J = { s->rho[j], s->p[j], s->c[j], s->gamma[j], s->h[j], velj,
+                                           grad ? grad + j * (size_t)(NQ * D) : NULL };
+                            gsph_riemann(o, D, xi, xj, &I, &J, dt_half, &p_star, v_star);
+                            for (int k = 0; k < D; k++) velij[k] = veli[k] - velj[k];
+                            if (o->lans) tau = eps_mom(velij, Vj, D);
+                            if (pass == 0) {
+                                for (int k = 0; k < D; k++)
+                                    rhs_v[k] -= s->mass[j] * (p_star * (vsqi[k] + vsqj[k]) - tau * dwdx[k]);
+                            } else {
+                                double heat = 0.0;
+                                if (o->lans) {
+                                    double rhoab = 0.5 * (s->rho[i] + s->rho[j]);
+                                    double cab = 0.5 * (s->c[i] + s->c[j]);
+                                    double Cp_ij = 0.5 * (s->cp[j] + s->cp[i]);
+                                    double hab = 0.5 * (hi + s->h[j]);
+                                    (void)rhoab;
+                                    double kij = eps_heat(Cp_ij, dx, velij, hab, cab, D);
+                                    double Fij = compute_F(dwdx, dx, D);
+                                    heat = s->mass[j] * Vj * Vi * kij * (s->T[i] - s->T[j]) * Fij;
+                                }
+                                double de = 0.0;
+                                for (int k = 0; k < D; k++)
+                                    de -= s->mass[j] * (v_star[k] - xdot[k]) *
+                                          (p_star * (vsqi[k] + vsqj[k]) - tau * dwdx[k]);
+                                rhs_e += (de + heat);
+                            }
+                        }
+                    }
+                }
+            });
+        }
+        double vi[3];
+        vel(s, i, D, 0, vi);
+        double unew[3];
+        for (int k = 0; k < D; k++) unew[k] = vi[k] + dt * (rhs_v[k]);
+        unew[D - 1] += dt * grav;
+        for (int k = 0; k < D; k++) w->nv[k][i] = unew[k];
+        w->ne[i] = s->e[i] + dt * (rhs_e + veli[D - 1] * grav);
+    }
+    if (err) return err;
     for (size_t i = 0; i < n; i++) {
         if (!need_neigh(s->bc_type[i])) continue;
         if (D == 3 && L->start[i + 1] == L->start[i]) continue;
@@ -996,15 +1376,32 @@ int oracle_adaptive(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
 }
 
 /* One step of the hot loop: 3D main.cc:217-471, 1D main.cc:676-750. */
+typedef struct GradOut {
+    double *grad;
+    uint64_t *key;
+    size_t cap, n;
+} GradOut;
 static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                       size_t *n, OracleTime *t, int nsteps, double *dt_log,
-                      int nthreads, const Images *im, const Inlet *inl);
+                      int nthreads, const Images *im, const Inlet *inl, GradOut *go);
 
 int oracle_steps(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                  size_t *n, OracleTime *t, int nsteps, double *dt_log,
                  int nthreads)
 {
-    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL, NULL);
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL, NULL, NULL);
+}
+
+/* oracle_steps plus the GSPH gradients of the last step (n_grad rows with
+ * their keys; n_grad = 0 when the step computed none) */
+int oracle_steps_grad(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
+                      size_t *n, OracleTime *t, int nsteps, double *dt_log, int nthreads,
+                      double *grad, uint64_t *grad_key, size_t cap, size_t *n_grad)
+{
+    GradOut go = { grad, grad_key, cap, 0 };
+    int rc = steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, NULL, NULL, &go);
+    *n_grad = go.n;
+    return rc;
 }
 
 int oracle_steps_bc(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
@@ -1013,7 +1410,7 @@ int oracle_steps_bc(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                     size_t nimg)
 {
     Images im = { img_key, img_xyz, nimg };
-    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, NULL);
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, NULL, NULL);
 }
 
 int oracle_steps_inlet(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
@@ -1026,7 +1423,7 @@ int oracle_steps_inlet(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
     Images im = { img_key, img_xyz, nimg };
     Inlet in = { col_xy, col_vel, col_count, ncol, cap, par[0], par[1], par[2], par[3], par[4],
                  par[5], par[6], par[7], par[8], par[9], key_base };
-    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, &in);
+    return steps_impl(o, g, s, n, t, nsteps, dt_log, nthreads, &im, &in, NULL);
 }
 
 int oracle_apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, size_t n,
@@ -1038,7 +1435,7 @@ int oracle_apply_bcond(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, s
 
 static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
                       size_t *n, OracleTime *t, int nsteps, double *dt_log,
-                      int nthreads, const Images *im, const Inlet *inl)
+                      int nthreads, const Images *im, const Inlet *inl, GradOut *go)
 {
     int rc = check_opts(o, g, s);
     if (rc) return rc;
@@ -1053,8 +1450,11 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
         if (dt_log) dt_log[st] = dt;
         Lists L = { 0 };
         long *oldb = NULL;
+        const int gsph = o->method == PLUME_METHOD_GSPH;
+        const int recon = gsph && o->gsph_recon != PLUME_RECON_ZEROTH;
+        const int need_grad = gsph && (o->gsph_gradients || recon);
         if (D == 3) {
-            rc = build_lists_3d(o, g, s, nn, (size_t)-1, &L, nthreads);
+            rc = build_lists_3d_for(o, g, s, nn, (size_t)-1, &L, nthreads, need_grad);
             if (rc) return rc;
             oldb = (long *)malloc(sizeof(long) * (nn ? nn : 1));
             for (size_t i = 0; i < nn; i++) oldb[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
@@ -1064,7 +1464,25 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
         int interval = o->sml_interval > 0 ? o->sml_interval : 1;
         if (o->adaptive_sml && (t->step % interval) == 0)
             rc = adaptive_pass(o, s, nn, &L, nthreads, (size_t)-1);
-        if (!rc) rc = momentum_pass(o, s, nn, &L, t->dtime, &w, nthreads);
+        double *grad = NULL;
+        if (!rc && need_grad) {
+            /* calc_gradients after adaptive_sml (main.cc:341-343, 697-699) */
+            grad = (double *)malloc(sizeof(double) * (nn ? nn : 1) * (size_t)((D + 2) * D));
+            if (!grad) rc = PLUME_E_INVALID;
+            else gsph_gradients(o, s, nn, &L, grad, nthreads);
+        }
+        if (!rc) {
+            if (gsph) rc = gsph_momentum_pass(o, s, nn, &L, t->dtime, recon ? grad : NULL, &w, nthreads);
+            else rc = momentum_pass(o, s, nn, &L, t->dtime, &w, nthreads);
+        }
+        if (!rc && go && st == nsteps - 1) {
+            go->n = grad ? nn : 0;
+            if (grad && nn <= go->cap) {
+                memcpy(go->grad, grad, sizeof(double) * nn * (size_t)((D + 2) * D));
+                memcpy(go->key, s->key, sizeof(uint64_t) * nn);
+            }
+        }
+        free(grad);
         if (!rc) rc = density_pass(o, s, nn, &L, &w, nthreads);
         if (!rc && o->lans) rc = velocity_pass(o, s, nn, &L, nthreads);
         free_work(&w);

@@ -61,6 +61,12 @@ int oracle_steps_inlet(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA 
 int oracle_steps(const PlumeOptions *opt, const PlumeGrid *grid,
                  PlumeSoA *s, size_t *n, OracleTime *t, int nsteps,
                  double *dt_log, int nthreads);
+/* oracle_steps plus the GSPH gradients of the last step (calc_gradients,
+ * calculate_gradient.cc:22-208): (D+2)*D doubles per row, rows with their
+ * keys; *n_grad = 0 when the step computed none. */
+int oracle_steps_grad(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s,
+                      size_t *n, OracleTime *t, int nsteps, double *dt_log, int nthreads,
+                      double *grad, uint64_t *grad_key, size_t cap, size_t *n_grad);
 
 /* Neighbour pairs, same modes as plume_neighbor_pairs(). */
 int oracle_pairs(const PlumeOptions *opt, const PlumeGrid *grid,

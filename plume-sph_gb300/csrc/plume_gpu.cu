@@ -24,6 +24,7 @@
 #include "radix_sort.cuh"
 #include "sph_kernels.cuh"
 #include "sph_warp.cuh"
+#include "sph_gsph.cuh"
 #include "sph_adjoint.cuh"
 
 using namespace plume;
@@ -495,19 +496,24 @@ __global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict_
   }
   const int b = (bi[2] * g.nb[1] + bi[1]) * g.nb[0] + bi[0];
   const double R = o.ksupport * h27_all[g.bucket_base + b] * (1.0 + 1e-10);
-  // cell box of the walk: the reach R, clipped to the 27 buckets
-  int clo[3], chi[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const int l = cell_axis(g, a, refc[a] - R, nullptr, nullptr);
-    const int h = cell_axis(g, a, refc[a] + R, nullptr, nullptr);
-    clo[a] = max(l, max((bi[a] - 1) * g.s, 0));
-    chi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
-  }
   // the image point relative to its bucket (mixed path)
   const float ir[3] = {(float)(refc[0] - (g.mind[0] + bi[0] * g.del)),
                        (float)(refc[1] - (g.mind[1] + bi[1] * g.del)),
                        (float)(refc[2] - (g.mind[2] + bi[2] * g.del))};
+  // cell box of the walk: the reach R, clipped to the 27 buckets (the mixed
+  // path takes the conservative FP32 range; the weights test exactly)
+  int clo[3], chi[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if constexpr (MIXED) {
+      cell_range(g, a, bi[a], ir[a], R, clo[a], chi[a]);
+    } else {
+      const int l = cell_axis(g, a, refc[a] - R, nullptr, nullptr);
+      const int h = cell_axis(g, a, refc[a] + R, nullptr, nullptr);
+      clo[a] = max(l, max((bi[a] - 1) * g.s, 0));
+      chi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
+    }
+  }
   const float delf = (float)g.del;
   const float c2f = (float)o.cutoff2;
   Acc<T> a0, a1, a2, a3, a4, aw, ak;
@@ -566,19 +572,20 @@ __global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict_
       }
     }
   }
-  double u0 = a0.get(), u1 = a1.get(), u2 = a2.get(), u3 = a3.get(), u4 = a4.get();
-  double wn = aw.get(), ks = ak.get();
+  // the slot's partial sums: FP32 on the mixed path (eight terms), FP64 else
+  T q0 = a0.get(), q1 = a1.get(), q2 = a2.get(), q3 = a3.get(), q4 = a4.get(), qw = aw.get(), qk = ak.get();
 #pragma unroll
   for (int off = BCG / 2; off > 0; off >>= 1) {
-    u0 += __shfl_xor_sync(gmask, u0, off);
-    u1 += __shfl_xor_sync(gmask, u1, off);
-    u2 += __shfl_xor_sync(gmask, u2, off);
-    u3 += __shfl_xor_sync(gmask, u3, off);
-    u4 += __shfl_xor_sync(gmask, u4, off);
-    wn += __shfl_xor_sync(gmask, wn, off);
-    ks += __shfl_xor_sync(gmask, ks, off);
+    q0 += __shfl_xor_sync(gmask, q0, off);
+    q1 += __shfl_xor_sync(gmask, q1, off);
+    q2 += __shfl_xor_sync(gmask, q2, off);
+    q3 += __shfl_xor_sync(gmask, q3, off);
+    q4 += __shfl_xor_sync(gmask, q4, off);
+    qw += __shfl_xor_sync(gmask, qw, off);
+    qk += __shfl_xor_sync(gmask, qk, off);
   }
   if (sub) return;
+  double u0 = q0, u1 = q1, u2 = q2, u3 = q3, u4 = q4, wn = qw, ks = qk;
   if (wn > 0.) {
     u0 /= wn; u1 /= wn; u2 /= wn; u3 /= wn; u4 /= wn;
     ks = ks / wn;
@@ -780,6 +787,9 @@ struct plume_ctx {
   double* img_xyz = nullptr;
   int nimg = 0;
   int* bc_map = nullptr;  // row of (member, image), -1 when absent
+  // GSPH gradients of the last step ((D+2)*D doubles per row; GSPH only)
+  double* grad = nullptr;
+  bool grad_valid = false;
   // eruption inlet (plume_set_inlet)
   Inlet inlet{};
   double* inlet_buf = nullptr;              // column xy + vel
@@ -836,6 +846,11 @@ static Opt make_opt(const PlumeOptions& p) {
   o.timeoutput = p.timeoutput; o.stat_erupt = p.stat_erupt; o.end_erupt = p.end_erupt;
   o.ksupport = (p.kernel == PLUME_KERNEL_M4) ? 2.0 : 3.0;
   o.max_steps = p.max_steps;
+  o.method = p.method;
+  o.gsph_solver = p.gsph_solver;
+  o.gsph_recon = p.gsph_recon;
+  o.gsph_vol = p.gsph_vol;
+  o.gsph_mono = p.gsph_mono;
   return o;
 }
 
@@ -927,6 +942,22 @@ static int search(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
+// GSPH momentum: calc_gradients (when the states read them, or always
+// with gsph_gradients), then the two-pass Riemann sweep
+template <int D, typename T>
+static void launch_gsph(plume_ctx* ctx, int nb) {
+  cudaStream_t st = ctx->st;
+  const bool recon = ctx->o.gsph_recon != PLUME_RECON_ZEROTH;
+  ctx->grad_valid = recon || ctx->opt.gsph_gradients;
+  if (ctx->grad_valid) {
+    k_gsph_grad<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
+                                            ctx->grad);
+    ctx->launches++;
+  }
+  k_gsph_mom<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count,
+                                            ctx->ts, recon ? ctx->grad : nullptr);
+}
+
 template <int D, typename T, bool MULTI>
 static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   const Geos<MULTI> gs{ctx->hgeo[0], ctx->d_geo};
@@ -953,6 +984,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->nbk, ctx->hb, ctx->h27);
   const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
   const bool mixed = sizeof(T) == 4;
+  const bool gsph = ctx->o.method == PLUME_METHOD_GSPH;
   const bool lists = (D == 3) && ctx->use_lists;
   if constexpr (D == 3) {
     if (lists) {
@@ -986,7 +1018,9 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       ctx->launches++;
     }
     record_ev(ctx, 11);
-    if (lists)
+    if (gsph)
+      launch_gsph<D, T>(ctx, nb);
+    else if (lists)
       k_sweep3_list<T, WMom, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
     else if (ctx->sweep_warp)
       k_sweep3<T, WMom, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
@@ -994,7 +1028,10 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       k_sweep3<T, WMom, false, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
   } else {
     record_ev(ctx, 11);
-    k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
+    if (gsph)
+      launch_gsph<D, T>(ctx, nb);
+    else
+      k_momentum<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
   }
   record_ev(ctx, 5);
   k_commit_mom<D><<<nb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, ctx->W, ctx->d_count, ctx->ts);
@@ -1179,7 +1216,9 @@ static bool same_shared_options(const PlumeOptions& a, const PlumeOptions& b) {
          a.adaptive_sml == b.adaptive_sml && a.sml_interval == b.sml_interval && a.num_loop == b.num_loop &&
          a.thresh == b.thresh && a.c_smooth == b.c_smooth && a.eta_smooth == b.eta_smooth &&
          a.alpha == b.alpha && a.beta == b.beta && a.ata == b.ata && a.cutoff2 == b.cutoff2 &&
-         a.list_factor == b.list_factor && a.g == b.g;
+         a.list_factor == b.list_factor && a.g == b.g && a.method == b.method &&
+         a.gsph_solver == b.gsph_solver && a.gsph_recon == b.gsph_recon && a.gsph_vol == b.gsph_vol &&
+         a.gsph_mono == b.gsph_mono && a.gsph_gradients == b.gsph_gradients;
 }
 
 static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem, bool batch, plume_ctx** out) {
@@ -1195,6 +1234,20 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
   if (opt->dim != 1 && opt->dim != 3) {
     g_create_error = "dim must be 1 or 3";
     return PLUME_E_INVALID;
+  }
+  if (opt->method != PLUME_METHOD_SPH && opt->method != PLUME_METHOD_GSPH) {
+    g_create_error = "method must be PLUME_METHOD_SPH or PLUME_METHOD_GSPH";
+    return PLUME_E_INVALID;
+  }
+  if (opt->method == PLUME_METHOD_GSPH) {
+    const int r = opt->gsph_recon;
+    if ((opt->gsph_solver != PLUME_RIEMANN_ROE && opt->gsph_solver != PLUME_RIEMANN_HLLC) ||
+        !(r == 0 || r == 1 || r == 2 || r == 3 || r == 4 || r == 10) ||
+        !(opt->gsph_vol == 0 || opt->gsph_vol == 1 || opt->gsph_vol == 3) ||
+        (opt->gsph_mono != 0 && opt->gsph_mono != 1)) {
+      g_create_error = "GSPH: solver ROE/HLLC, recon 0-4 or 10, vol 0, 1 or 3, mono 0 or 1";
+      return PLUME_E_INVALID;
+    }
   }
   size_t capacity = 0;
   double ncell_tot = 0, nbk_tot = 0;
@@ -1317,6 +1370,9 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
           (rc = dev_alloc(ctx, (void**)&ctx->d_real, sizeof(int))))
         return fail(rc);
     }
+    if (opt->method == PLUME_METHOD_GSPH &&
+        (rc = dev_alloc(ctx, (void**)&ctx->grad, 8 * c * (size_t)((opt->dim + 2) * opt->dim))))
+      return fail(rc);
     if (opt->precision == PLUME_PREC_MIXED && opt->dim == 3) {
       if ((rc = dev_alloc(ctx, (void**)&ctx->K.P, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.Q, 16 * c)) ||
           (rc = dev_alloc(ctx, (void**)&ctx->K.R, 16 * c)) || (rc = dev_alloc(ctx, (void**)&ctx->K.S, 16 * c)))
@@ -2084,6 +2140,10 @@ int plume_adjoint_record(plume_ctx* ctx, int nsteps, int checkpoint_every) {
     ctx->err = "adjoint: the wall boundary is not differentiated (clear the wall images)";
     return PLUME_E_INVALID;
   }
+  if (ctx->o.method != PLUME_METHOD_SPH) {
+    ctx->err = "adjoint: the GSPH step is not differentiated";
+    return PLUME_E_INVALID;
+  }
   if (ctx->inlet_reserve) {
     ctx->err = "adjoint: the inlet is not differentiated (clear it)";
     return PLUME_E_INVALID;
@@ -2248,6 +2308,41 @@ int plume_adjoint_backward(plume_ctx* ctx, const PlumeSoA* final_bar, size_t n_f
   int rc = restore_ckpt(ctx, ctx->ckpts.back());
   if (rc) return rc;
   return finish_steps(ctx);
+}
+
+// ---------------------------------------------------------------- GSPH
+int plume_gsph_gradients(plume_ctx* ctx, uint64_t* key, double* grad, size_t cap, size_t* n) {
+  if (!ctx || !n) return PLUME_E_INVALID;
+  if (!ctx->grad || !ctx->grad_valid) {
+    ctx->err = "GSPH gradients: none computed by the last step";
+    return PLUME_E_INVALID;
+  }
+  int cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, ctx->d_count, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  *n = (size_t)cnt;
+  if (cap < (size_t)cnt) return PLUME_OK;
+  if (!key || !grad) return PLUME_E_INVALID;
+  const size_t per = (size_t)((ctx->o.dim + 2) * ctx->o.dim);
+  std::vector<uint8_t> bc((size_t)cnt);
+  std::vector<uint64_t> k((size_t)cnt);
+  std::vector<double> g((size_t)cnt * per);
+  if (cnt) {
+    CK(cudaMemcpyAsync(bc.data(), ctx->A.bc, (size_t)cnt, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(k.data(), ctx->A.key, 8 * (size_t)cnt, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(g.data(), ctx->grad, 8 * (size_t)cnt * per, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  // rows of the last step; rows deleted by it are left out
+  size_t r = 0;
+  for (int i = 0; i < cnt; i++) {
+    if (bc[i] == BC_DEAD) continue;
+    key[r] = k[i];
+    memcpy(grad + r * per, g.data() + (size_t)i * per, 8 * per);
+    r++;
+  }
+  *n = r;
+  return PLUME_OK;
 }
 
 // ---------------------------------------------------------------- wall boundary

@@ -38,6 +38,9 @@ struct Opt {
   double max_time, timeoutput, stat_erupt, end_erupt;
   double ksupport;  // kernel support in units of h (3 Gaussian box, 2 M4)
   int max_steps;
+  // GSPH (USE_GSPH 1): RIEMANN_SOLVER, MINI_DERIVATIVE_COND,
+  // GSPH_SPECIFIC_VOL_APP, GSPH_MODIFIED_MONOTONICITY
+  int method, gsph_solver, gsph_recon, gsph_vol, gsph_mono;
 };
 
 struct Geo {

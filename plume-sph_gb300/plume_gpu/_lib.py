@@ -89,6 +89,8 @@ def lib():
         L.plume_adjoint_record.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.plume_set_wall_images.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_double), C.c_size_t]
         L.plume_apply_bcond.argtypes = [C.c_void_p]
+        L.plume_gsph_gradients.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_double), C.c_size_t,
+                                           P(C.c_size_t)]
         L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
                                              P(C.c_size_t), P(C.c_double)]

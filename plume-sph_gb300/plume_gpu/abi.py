@@ -35,6 +35,9 @@ BC_ERUPT, BC_PRESSURE, BC_WALL, BC_NOSAVE_REAL, BC_REAL = 0, 1, 2, 99, 100
 BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_INACTIVE = 0x1, 0x2, 0x4
 PREC_FP64, PREC_MIXED = 0, 1
 KERNEL_GAUSS, KERNEL_M4 = 0, 1
+METHOD_SPH, METHOD_GSPH = 0, 1
+RIEMANN_ROE, RIEMANN_HLLC = 0, 1
+RECON_NONE, RECON_EACH, RECON_PAIRWISE, RECON_ALL, RECON_ZEROTH, RECON_EACH_SHOCK = 0, 1, 2, 3, 4, 10
 
 # field order of the double arrays (also the order of the oracle case files)
 DOUBLE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "vsx", "vsy", "vsz", "mass", "h",
@@ -58,6 +61,8 @@ class PlumeOptions(C.Structure):
         ("stat_erupt", C.c_double), ("end_erupt", C.c_double),
         ("max_steps", C.c_int), ("max_per_bucket", C.c_int),
         ("capacity", C.c_size_t),
+        ("method", C.c_int), ("gsph_solver", C.c_int), ("gsph_recon", C.c_int), ("gsph_vol", C.c_int),
+        ("gsph_mono", C.c_int), ("gsph_gradients", C.c_int),
     ]
 
 
@@ -132,6 +137,13 @@ class Options:
     max_steps: int = 1 << 30
     max_per_bucket: int = 1 << 30
     capacity: int = 0
+    # GSPH switches: the reference's 3D defaults (options.h:545-593)
+    method: int = METHOD_SPH
+    gsph_solver: int = RIEMANN_ROE
+    gsph_recon: int = RECON_EACH_SHOCK
+    gsph_vol: int = 3
+    gsph_mono: int = 1
+    gsph_gradients: int = 0
 
     def to_c(self) -> PlumeOptions:
         o = PlumeOptions()

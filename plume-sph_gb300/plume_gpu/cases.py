@@ -26,7 +26,8 @@ import numpy as np
 
 from .abi import (BC_ERUPT, BC_NOSAVE_REAL, BC_PRESSURE, BC_REAL, BC_WALL,
                   BUCKET_ABSORBING, BUCKET_MIXED, KERNEL_GAUSS, KERNEL_M4,
-                  PREC_FP64, Grid, Options, ParticleSet)
+                  METHOD_GSPH, METHOD_SPH, PREC_FP64, RECON_EACH, RECON_ZEROTH, RIEMANN_HLLC,
+                  Grid, Options, ParticleSet)
 
 
 @dataclass
@@ -122,15 +123,17 @@ def _shock_tube(rho_l, p_l, u_l, rho_r, p_r, u_r, middle, lo, hi, s0, nb, nnsrp_
 
 def options_1d(kernel=KERNEL_GAUSS, eta=1.0, cfl=0.1, cva=717.0, precision=PREC_FP64,
                max_time=0.2, timeoutput=0.1) -> Options:
-    """1D switches of src/plume/options.h:16-410 with USE_GSPH=0 and the 1D
-    constants of parameters.h:1225-1448."""
+    """1D switches of src/plume/options.h:16-410 (method SPH unless set;
+    the GSPH switches are the 1D defaults: HLLC, zeroth-order states) and the
+    1D constants of parameters.h:1225-1448."""
     return Options(dim=1, precision=precision, kernel=kernel, lans=0, energy_smooth=0,
                    pghost_contrib=2, adaptive_sml=1, sml_interval=1, num_loop=5,
                    thresh=1e-5, c_smooth=2.0, eta_smooth=eta, alpha=1.0, beta=2.0,
                    ata=0.01, cfl=cfl, cutoff2=12.0, list_factor=4.25, g=0.0, ng0=0.05,
                    cvs=1100.0, cvg=1348.0, cva=cva, rg=462.0, ra=287.0, vent_z=0.0,
                    sml_phase2=0.0, max_time=_f32(max_time), timeoutput=_f32(timeoutput),
-                   stat_erupt=0.0, end_erupt=7200.0)
+                   stat_erupt=0.0, end_erupt=7200.0, gsph_solver=RIEMANN_HLLC,
+                   gsph_recon=RECON_ZEROTH, gsph_vol=0, gsph_mono=0)
 
 
 def _grid_1d(ps: ParticleSet, opt: Options, cells_per_h: float = 0.5, travel: float = 0.0) -> Grid:
@@ -151,10 +154,13 @@ def _grid_1d(ps: ParticleSet, opt: Options, cells_per_h: float = 0.5, travel: fl
 
 def sod_1d(n_real: int = 2000, ghosts: int = 10, kernel: int = KERNEL_GAUSS,
            precision: int = PREC_FP64, t_end: float = 0.2,
-           states=((1.0, 1.0, 0.0), (0.125, 0.1, 0.0))) -> Case:
+           states=((1.0, 1.0, 0.0), (0.125, 0.1, 0.0)), eta: float = 1.3,
+           method: int = METHOD_SPH) -> Case:
     """The 1D Sod workload: [0,1] split at 0.5, equal-mass particles, ideal
-    gas gamma = 1.4 (R = 287, Cv = 717.5), h = 1.3 m/rho, alpha=1, beta=2,
-    CFL 0.3, `ghosts` ghosts per end, run to t = 0.2.
+    gas gamma = 1.4 (R = 287, Cv = 717.5), h = eta m/rho (eta 1.3),
+    alpha=1, beta=2, CFL 0.3, `ghosts` ghosts per end, run to t = 0.2;
+    method SPH (artificial viscosity) or GSPH (HLLC Riemann solver, the
+    reference's 1D default).
 
     The kernel defaults to the reference's Gaussian: with the cubic-spline
     kernel swapped in, the reference's own step (built from its sources)
@@ -176,9 +182,10 @@ def sod_1d(n_real: int = 2000, ghosts: int = 10, kernel: int = KERNEL_GAUSS,
     if best is None:
         raise ValueError(f"no spacing gives {n_real} particles")
     s0, ps = best[1], best[2]
-    opt = options_1d(kernel=kernel, eta=1.3, cfl=0.3, cva=717.5, precision=precision,
+    opt = options_1d(kernel=kernel, eta=eta, cfl=0.3, cva=717.5, precision=precision,
                      max_time=t_end, timeoutput=t_end / 2)
     opt.capacity = ps.n
+    opt.method = method
     return Case("sod_1d", opt, _grid_1d(ps, opt), ps, pre_adaptive=True,
                 info={"s0": s0, "n_real": n_real, "ghosts_per_end": ghosts})
 

@@ -155,6 +155,20 @@ class Solver:
     def apply_bcond(self):
         self._check(self.L.plume_apply_bcond(self.ctx), "plume_apply_bcond")
 
+    # -- GSPH -----------------------------------------------------------------
+    def gsph_gradients(self):
+        """(keys, (n, (D+2)*D) gradients) of the last GSPH step
+        (calc_gradients: d rho, d v_0.., d p; x_k fastest)"""
+        n = C.c_size_t(0)
+        self._check(self.L.plume_gsph_gradients(self.ctx, None, None, 0, C.byref(n)), "plume_gsph_gradients")
+        D = self.case.options.dim
+        keys = np.zeros(n.value, dtype=np.uint64)
+        grad = np.zeros((n.value, (D + 2) * D))
+        self._check(self.L.plume_gsph_gradients(self.ctx, keys.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                grad.ctypes.data_as(C.POINTER(C.c_double)), n.value,
+                                                C.byref(n)), "plume_gsph_gradients")
+        return keys[:n.value], grad[:n.value]
+
     # -- adjoint --------------------------------------------------------------
     def adjoint_record(self, nsteps: int, checkpoint_every: int = 25):
         """nsteps steps keeping checkpoints for adjoint_backward"""

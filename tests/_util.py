@@ -38,10 +38,30 @@ def unpack(d, prefix) -> ParticleSet:
     return ps
 
 
+def gsph_case(name):
+    """the cases of the GSPH fixtures (tests/golden/make_golden.py)"""
+    if name == "gsph_1d_sod":
+        c = cases.sod_1d(n_real=200, method=cases.METHOD_GSPH)
+    elif name == "gsph_1d_grad":
+        c = cases.sod_1d(n_real=200, ghosts=0, eta=2.0, method=cases.METHOD_GSPH)
+        c.options.gsph_recon = cases.RECON_EACH
+    elif name == "gsph_3d":
+        c = cases.plume_3d(half_width=200.0, height=400.0, dx=50.0, vent_radius=50.0,
+                           vent_dx=25.0, duct_depth=300.0, seed=5, name="gsph_3d")
+        c.options.method = cases.METHOD_GSPH
+        c.step0 = 48
+    else:
+        raise KeyError(name)
+    c.options.gsph_gradients = 1
+    return c
+
+
 def golden_case(name):
     """(case with the fixture's input particles, fixture dict)"""
     d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
-    if name == "sod_1d_200":
+    if name.startswith("gsph_"):
+        c = gsph_case(name)
+    elif name == "sod_1d_200":
         c = cases.sod_1d(n_real=200, kernel=cases.KERNEL_M4)
     elif name == "sod_1d_2000_end":
         c = cases.sod_1d(n_real=2000)

@@ -21,6 +21,7 @@ state and a summary of the reference's neighbour lists:
                        flat-ground image table of cases.wall_images, the
                        reference's apply_bcond before the loop and after each
                        of steps 49..51
+  gsph_*.npz           GSPH builds (make_gsph)
 
 Usage (in a container that has the reference tree):
   python tests/golden/make_golden.py [--ref /root/reference]
@@ -37,10 +38,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "plume-sph_gb300"))
+sys.path.insert(0, os.path.dirname(HERE))
 
 from plume_gpu import cases  # noqa: E402
 from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS  # noqa: E402
 from oracle import refio  # noqa: E402
+from _util import gsph_case  # noqa: E402
 
 MASK = np.uint64(0xFFFFFFFFFFFFFFFF)
 
@@ -112,6 +115,8 @@ def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_
     if images is not None:
         d["img_key"] = np.asarray(images[0], dtype=np.uint64)
         d["img_xyz"] = np.asarray(images[1], dtype=np.float64)
+    if "grad" in steps[-1]:
+        d["grad_key"], d["grad"] = steps[-1]["grad"]
     np.savez_compressed(path, **d)
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
@@ -133,6 +138,21 @@ def main():
     c.step0 = 48
     make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_small.npz"))
     make_bc()
+    make_gsph()
+
+
+def make_gsph():
+    """GSPH (USE_GSPH 1) fixtures with the last step's gradients:
+      gsph_1d_sod.npz   1D Sod, 200 reals, HLLC, zeroth-order states, 20 steps
+      gsph_1d_grad.npz  ghost-free 1D Sod with h = 2 m/rho, linear states
+                        (MINI_DERIVATIVE_COND 1), the reference's own
+                        calc_gradients, 20 steps
+      gsph_3d.npz       a 400 m cube of the 3D plume (seed 5) with the 3D GSPH defaults
+                        (Roe, cubic interface, MINI_DERIVATIVE_COND 10,
+                        modified monotonicity), steps 49..50"""
+    make(gsph_case("gsph_1d_sod"), "ref1d_gsph", 20, os.path.join(HERE, "gsph_1d_sod.npz"))
+    make(gsph_case("gsph_1d_grad"), "ref1d_gsph_grad", 20, os.path.join(HERE, "gsph_1d_grad.npz"))
+    make(gsph_case("gsph_3d"), "ref3d_gsph", 2, os.path.join(HERE, "gsph_3d.npz"))
 
 
 def make_bc():
@@ -143,4 +163,8 @@ def make_bc():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "--gsph":
+        refio.build_ref()
+        make_gsph()
+    else:
+        main()

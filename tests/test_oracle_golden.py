@@ -12,7 +12,7 @@ import pytest
 
 from oracle.binding import OracleRun
 from plume_gpu import cases
-from plume_gpu.abi import BYTE_FIELDS
+from plume_gpu.abi import BYTE_FIELDS, RIEMANN_ROE
 from _util import field_errors, golden_case, set_summary, unpack
 
 
@@ -129,3 +129,60 @@ def test_wall_image_table_restates_search_bnd_images():
     g = np.array([[ps.x[row[int(kk)]], ps.y[row[int(kk)]], ps.z[row[int(kk)]]] for kk in k])
     np.testing.assert_array_equal(x[:, :2], g[:, :2])
     np.testing.assert_allclose(x[:, 2], -g[:, 2], rtol=0, atol=0)  # mirrored in z = 0
+
+
+# ---------------------------------------------------------------- GSPH
+def _grad_by_key(keys, grad, want):
+    m = {int(k): r for r, k in enumerate(keys)}
+    return grad[np.array([m[int(k)] for k in want])]
+
+
+@pytest.mark.parametrize("name", ["gsph_1d_sod", "gsph_1d_grad"])
+def test_oracle_gsph_1d_bit_exact(name):
+    """GSPH (HLLC) steps and the last step's calc_gradients, bit for bit:
+    zeroth-order states (the 1D default), and linear states (MINI_DERIVATIVE
+    _COND 1) on a ghost-free tube that runs the reference's own
+    calc_gradients."""
+    case, d = golden_case(name)
+    o = OracleRun(case)
+    o.adaptive()
+    dts = o.steps_grad(int(d["nsteps"]))
+    np.testing.assert_array_equal(dts, d["dt"])
+    err = field_errors(o.ps, unpack(d, "out_"))
+    assert max(err.values()) == 0.0, err
+    gk, g = o.grad
+    np.testing.assert_array_equal(_grad_by_key(gk, g, d["grad_key"]), d["grad"])
+    assert np.count_nonzero(np.abs(d["grad"]).sum(axis=1)) > 100
+
+
+def test_oracle_gsph_differs_from_sph():
+    """the method switch reaches the step: GSPH and SPH part after one step"""
+    case, _ = golden_case("gsph_1d_sod")
+    a = OracleRun(case)
+    a.adaptive()
+    a.steps(1)
+    case.options.method = cases.METHOD_SPH
+    b = OracleRun(case)
+    b.adaptive()
+    b.steps(1)
+    assert max(field_errors(a.ps, b.ps, fields=("vx", "e")).values()) > 1e-6
+
+
+def test_oracle_gsph_3d_matches_reference():
+    """3D GSPH with the reference's 3D switches (Roe solver, cubic interface
+    position, MINI_DERIVATIVE_COND 10, modified monotonicity, LANS), steps
+    49..50: gradients of the last step bit for bit, fields to rounding."""
+    case, d = golden_case("gsph_3d")
+    assert case.options.gsph_solver == RIEMANN_ROE and case.options.gsph_recon == 10
+    o = OracleRun(case)
+    dts = o.steps_grad(int(d["nsteps"]))
+    np.testing.assert_allclose(dts, d["dt"], rtol=1e-12, atol=0)
+    ref = unpack(d, "out_")
+    err = field_errors(o.ps, ref)
+    assert max(err.values()) < 1e-12, err
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(o.ps.sorted_by_key(), f), getattr(ref, f))
+    gk, g = o.grad
+    gref = d["grad"]
+    gerr = np.abs(_grad_by_key(gk, g, d["grad_key"]) - gref).max(axis=0) / (np.abs(gref).max(axis=0) + 1e-300)
+    assert gerr.max() < 1e-12, gerr
