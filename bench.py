@@ -326,6 +326,38 @@ def adjoint_leg(steps=300, every=25, n_air=2.0e5, fd_rels=()):
     return out
 
 
+def gsph_leg(steps=20):
+    """Godunov SPH (USE_GSPH 1): particle-steps/s of the GSPH step on the
+    1D Sod tube (2,000 reals, HLLC, zeroth-order states, FP64) and on a
+    3D plume (4 km cube at 50 m, the reference's 3D GSPH switches: Roe,
+    MINI_DERIVATIVE_COND 10 with calc_gradients every step, cubic interface,
+    LANS), FP64 and mixed; device time from the step events."""
+    from plume_gpu import Solver, cases
+    from plume_gpu.abi import METHOD_GSPH, PREC_FP64, PREC_MIXED
+    out = {}
+
+    def timed(case, n, pre=False):
+        s = Solver(case)
+        if pre:
+            s.adaptive_sml()
+        s.steps(3)
+        _, nr0 = s.count()
+        s.steps(n)
+        ph = s.phase_times()
+        _, nr1 = s.count()
+        s.close()
+        t = ph["total"] / 1000.0
+        return {"value": 0.5 * (nr0 + nr1) * n / t, "unit": METRIC, "ms_per_step": 1000.0 * t / n,
+                "momentum_ms": ph["momentum"] / n, "n_real": int(nr1)}
+
+    out["sod1d_2000_fp64"] = timed(cases.sod_1d(n_real=2000, method=METHOD_GSPH), steps, pre=True)
+    for prec, tag in ((PREC_FP64, "fp64"), (PREC_MIXED, "mixed")):
+        c = small_plume(prec)
+        c.options.method = METHOD_GSPH
+        out["plume3d_4km_50m_" + tag] = timed(c, max(3, steps // 4))
+    return out
+
+
 def small_plume(prec):
     """the test-size workload of --small (4 km tall plume at 50 m)"""
     from plume_gpu import cases
@@ -382,6 +414,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="fixed cell tiles (4^3 per bucket)")
     ap.add_argument("--subcells", type=int, default=0, help="fixed cell tiles (N^3 per bucket), no tuning")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-gsph", action="store_true", help="skip the GSPH leg")
     ap.add_argument("--no-wall-bc", action="store_true",
                     help="leave the wall ghosts' states fixed (no apply_bcond in the step)")
     ap.add_argument("--adjoint-fd", action="store_true",
@@ -484,7 +517,7 @@ def main():
         sol.steps(1)
         n_host = sol.download_into(host)
         d2h += n_host * bytes_per
-        nrs += int(host.need_neigh()[:n_host].sum())
+        nrs += sol.count()[1]  # particles the step updated (device count)
     torch.cuda.synchronize()
     t_e2e = reduce_max(dist, time.perf_counter() - t0)
     e2e_value = ws * nrs / t_e2e
@@ -540,6 +573,13 @@ def main():
         except Exception as e:
             adj = {"failed": str(e)}
 
+    gsph = None
+    if not args.no_gsph and not args.small:
+        try:
+            gsph = gsph_leg()
+        except Exception as e:
+            gsph = {"failed": str(e)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -570,6 +610,7 @@ def main():
             "cpu_baseline": cpu,
             "ensembles": ens,
             "adjoint": adj,
+            "gsph": gsph,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

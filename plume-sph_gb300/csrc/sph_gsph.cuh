@@ -59,9 +59,13 @@ __global__ void k_gsph_grad(Opt o, const Geo* __restrict__ geo, Dev A, Work W, c
   for (int a = 0; a < D; a++)
 #pragma unroll
     for (int q = 0; q < NQ; q++) FF[a][q] = 0.0;
+  // The sums only gain from j with a non-zero dW (inside the kernel support
+  // of h_i), so the walk covers that reach; its in-list count is a lower
+  // bound of the reference's count over the CUTOFF2 h_i box.  Only when it
+  // is <= 20 does a second, count-only walk over the full box decide.
   int nreal = 0;
-  const double R = supp * (1.0 + 1e-10);
-  for_segments<D, double>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+  const double Rk = fmin(supp, o.ksupport * hi) * (1.0 + 1e-10);
+  for_segments<D, double>(g, cs, xi, bi, Rk, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
     for (uint32_t j = j0; j < j1; j++) {
       if (j == (uint32_t)i) continue;
       double dx[3];
@@ -92,7 +96,20 @@ __global__ void k_gsph_grad(Opt o, const Geo* __restrict__ geo, Dev A, Work W, c
       }
     }
   });
-  if (nreal <= 20) return;
+  if (nreal <= 20) {
+    nreal = 0;
+    for_segments<D, double>(g, cs, xi, bi, supp * (1.0 + 1e-10),
+                            [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+      for (uint32_t j = j0; j < j1; j++) {
+        if (j == (uint32_t)i) continue;
+        double dx[3];
+        dx[0] = xi[0] - A.x[j];
+        if (D == 3) { dx[1] = xi[1] - A.y[j]; dx[2] = xi[2] - A.z[j]; }
+        if ((own || in_box<D, double>(dx, Lb)) && in_box<D, double>(dx, supp)) nreal++;
+      }
+    });
+    if (nreal <= 20) return;
+  }
   double Ai[D * D];
   if constexpr (D == 1) {
     Ai[0] = -1 / AA[0];
@@ -305,18 +322,19 @@ __device__ __forceinline__ void gsph_riemann(const Opt& o, const T* dx, const GS
 
 // ---------------------------------------------------------------- momentum
 // GSPH momentum and energy (mom_engr_update.cc:441-1146, ME_UPDATE_SML 2,
-// ADAPTIVE_SML 1, HAVE_ENERGY_CUT 0).  Per need_neigh particle i, two passes
-// over its list entries j != i inside the CUTOFF2 h_i box whose
-// V_i^2 dW(dx/h_ij, h_ij) is non-zero, h_ij = (h_i + h_j)/2:
-//   pass 1: rhs_v -= m_j (p* (V_i^2 + V_j^2) dW - tau dW), tau the LANS
-//           stress SPH_epsilon_mom(v_i - v_j, V_j) (zero without LANS);
-//   pass 2: the same Riemann problems, rhs_e -= m_j (v* - xdot*) .
-//           (p* (V_i^2 + V_j^2) dW - tau dW), plus the LANS heat flux
-//           m_j V_j V_i k_ij (T_i - T_j) F_ij, with xdot* = v_i + dt/2
-//           (rhs_v + g) from pass 1;
-// then v_new = v + dt (rhs_v + g e_D) and e_new = e + dt (rhs_e + v_i,D g)
-// into W.nv*, W.ne for k_commit_mom.  grad: the step's gradients, or null
-// for zeroth-order states.
+// ADAPTIVE_SML 1, HAVE_ENERGY_CUT 0).  Over particle i's list entries
+// j != i inside the CUTOFF2 h_i box whose V_i^2 dW(dx/h_ij, h_ij) is
+// non-zero (h_ij = (h_i + h_j)/2), with F_j = p* (V_i^2 + V_j^2) dW - tau dW
+// (tau the LANS stress SPH_epsilon_mom(v_i - v_j, V_j), zero without LANS):
+//   rhs_v = -sum_j m_j F_j
+//   rhs_e = -sum_j m_j (v*_j - xdot*) . F_j + LANS heat flux,
+//           xdot* = v_i + dt/2 (rhs_v + g).
+// The reference walks the list twice, solving each Riemann problem again
+// once rhs_v is known; here one walk accumulates sum m_j v*_j . F_j and
+// rhs_v, and rhs_e = -sum m_j v*_j . F_j - xdot* . rhs_v + heat follows
+// (the same sum, regrouped).  Then v_new = v + dt (rhs_v + g e_D),
+// e_new = e + dt (rhs_e + v_i,D g) into W.nv*, W.ne for k_commit_mom.
+// grad: the step's gradients, or null for zeroth-order states.
 template <int D, typename T>
 __global__ void k_gsph_mom(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
                            const double* __restrict__ hmax_all, const int* __restrict__ d_count,
@@ -362,104 +380,102 @@ __global__ void k_gsph_mom(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
   const double hm = hmax[D == 3 ? b : 0];
   const double R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hm)) * (1.0 + 1e-10);
   const double grav = -o.g;
-  Acc<T> rhs_v[3], rhs_e;
-  T rv[3] = {0, 0, 0};  // pass-1 momentum sums, read by pass 2
-  for (int pass = 0; pass < 2; pass++) {
-    T xdot[3];
+  Acc<T> rhs_v[3], vF, heat_sum;
+  for_segments<D, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+    const T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
+    for (uint32_t j = j0; j < j1; j++) {
+      if (j == (uint32_t)i) continue;
+      T dx[3];
+      pair_dx<D, T>(xsh, xi, A, W, j, dx);
+      if (!own && !in_box<D, T>(dx, Lb)) continue;
+      if (!in_box<D, T>(dx, supp)) continue;
+      const T hj = T(A.h[j]);
+      const T hij = T(0.5) * (hi + hj);
+      const T Vj = T(1.0) / T(A.rho[j]);
+      T si[3], dw[3], vsqi[3], vsqj[3];
 #pragma unroll
-    for (int k = 0; k < D; k++) xdot[k] = I.v[k] + T(0.5) * T(dt) * (rv[k] + (k == D - 1 ? T(grav) : T(0)));
-    for_segments<D, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
-      const T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
-      for (uint32_t j = j0; j < j1; j++) {
-        if (j == (uint32_t)i) continue;
-        T dx[3];
-        pair_dx<D, T>(xsh, xi, A, W, j, dx);
-        if (!own && !in_box<D, T>(dx, Lb)) continue;
-        if (!in_box<D, T>(dx, supp)) continue;
-        const T hj = T(A.h[j]);
-        const T hij = T(0.5) * (hi + hj);
-        const T Vj = T(1.0) / T(A.rho[j]);
-        T si[3], dw[3], vsqi[3], vsqj[3];
+      for (int k = 0; k < D; k++) si[k] = dx[k] / hij;
+      kdw<D, T>(o.kernel, si, hij, dw);
+      T max_dw = 0;
 #pragma unroll
-        for (int k = 0; k < D; k++) si[k] = dx[k] / hij;
-        kdw<D, T>(o.kernel, si, hij, dw);
-        T max_dw = 0;
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          vsqi[k] = Vi * Vi * dw[k];
-          vsqj[k] = Vj * Vj * dw[k];
-          max_dw = fmax(max_dw, fabs(vsqi[k]));
-        }
-        if (!(max_dw > T(0))) continue;
-        GSide<T> J;
-        J.rho = T(A.rho[j]); J.p = T(A.p[j]); J.c = T(A.c[j]); J.gam = T(A.gam[j]); J.h = hj;
-        J.v[0] = T(lans ? A.vsx[j] : A.vx[j]);
-        if (D == 3) {
-          J.v[1] = T(lans ? A.vsy[j] : A.vy[j]);
-          J.v[2] = T(lans ? A.vsz[j] : A.vz[j]);
-        }
-        J.g = grad ? grad + (size_t)j * (NQ * D) : nullptr;
-        T p_star, v_star[3];
-        gsph_riemann<D, T>(o, dx, I, J, dt_half, p_star, v_star);
-        T velij[3], tau = 0;
-#pragma unroll
-        for (int k = 0; k < D; k++) velij[k] = I.v[k] - J.v[k];
-        if (lans) {
-          T dotv = 0;
-#pragma unroll
-          for (int k = 0; k < D; k++) dotv += velij[k] * velij[k];
-          tau = T(EPS_HALF) * dotv * Vj;
-        }
-        const T mj = T(A.mass[j]);
-        if (pass == 0) {
-#pragma unroll
-          for (int k = 0; k < D; k++) rhs_v[k].sub(mj * (p_star * (vsqi[k] + vsqj[k]) - tau * dw[k]));
-        } else {
-          T heat = 0;
-          if (lans) {
-            // SPH_epsilon_heat_conductivity (sph_lib.cc:1399-1440) with
-            // h_ab, c_ab; compute_F (sph_lib.cc:257-281) of the same dW
-            const T cab = T(0.5) * (I.c + J.c);
-            const T Cp_ij = T(0.5) * (T(A.cp[j]) + cpi);
-            T dotvr = 0, dotrr = 0, dotvv = 0, kij = 0;
-#pragma unroll
-            for (int k = 0; k < D; k++) dotvr += fabs(velij[k] * dx[k]);
-            if (dotvr != T(0)) {
-#pragma unroll
-              for (int k = 0; k < D; k++) dotrr += dx[k] * dx[k];
-#pragma unroll
-              for (int k = 0; k < D; k++) dotvv += velij[k] * velij[k];
-              const T kab = (D == 3) ? T(10.0) * T(EPS_HALF) * Cp_ij * dotrr * dotvv / (T(PRANDTL) * dotvr) : T(0);
-              kij = kab / (hij * cab);
-            }
-            T W_r = 0, r_sq = 0, Fij = 0;
-#pragma unroll
-            for (int k = 0; k < D; k++) W_r += dw[k] * dx[k];
-            if (W_r != T(0)) {
-#pragma unroll
-              for (int k = 0; k < D; k++) r_sq += dx[k] * dx[k];
-              Fij = W_r / r_sq;
-            }
-            heat = mj * Vj * Vi * kij * (tempi - T(A.T[j])) * Fij;
-          }
-          T de = 0;
-#pragma unroll
-          for (int k = 0; k < D; k++) de -= mj * (v_star[k] - xdot[k]) * (p_star * (vsqi[k] + vsqj[k]) - tau * dw[k]);
-          rhs_e.add(de + heat);
-        }
+      for (int k = 0; k < D; k++) {
+        vsqi[k] = Vi * Vi * dw[k];
+        vsqj[k] = Vj * Vj * dw[k];
+        max_dw = fmax(max_dw, fabs(vsqi[k]));
       }
-    });
+      if (!(max_dw > T(0))) continue;
+      GSide<T> J;
+      J.rho = T(A.rho[j]); J.p = T(A.p[j]); J.c = T(A.c[j]); J.gam = T(A.gam[j]); J.h = hj;
+      J.v[0] = T(lans ? A.vsx[j] : A.vx[j]);
+      if (D == 3) {
+        J.v[1] = T(lans ? A.vsy[j] : A.vy[j]);
+        J.v[2] = T(lans ? A.vsz[j] : A.vz[j]);
+      }
+      J.g = grad ? grad + (size_t)j * (NQ * D) : nullptr;
+      T p_star, v_star[3];
+      gsph_riemann<D, T>(o, dx, I, J, dt_half, p_star, v_star);
+      T velij[3], tau = 0;
 #pragma unroll
-    for (int k = 0; k < D; k++) rv[k] = rhs_v[k].get();
+      for (int k = 0; k < D; k++) velij[k] = I.v[k] - J.v[k];
+      if (lans) {
+        T dotv = 0;
+#pragma unroll
+        for (int k = 0; k < D; k++) dotv += velij[k] * velij[k];
+        tau = T(EPS_HALF) * dotv * Vj;
+      }
+      const T mj = T(A.mass[j]);
+      T vf = 0;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        const T F = mj * (p_star * (vsqi[k] + vsqj[k]) - tau * dw[k]);
+        rhs_v[k].sub(F);
+        vf += v_star[k] * F;
+      }
+      vF.add(vf);
+      if (lans) {
+        // SPH_epsilon_heat_conductivity (sph_lib.cc:1399-1440) with h_ab,
+        // c_ab; compute_F (sph_lib.cc:257-281) of the same dW
+        const T cab = T(0.5) * (I.c + J.c);
+        const T Cp_ij = T(0.5) * (T(A.cp[j]) + cpi);
+        T dotvr = 0, dotrr = 0, dotvv = 0, kij = 0;
+#pragma unroll
+        for (int k = 0; k < D; k++) dotvr += fabs(velij[k] * dx[k]);
+        if (dotvr != T(0)) {
+#pragma unroll
+          for (int k = 0; k < D; k++) dotrr += dx[k] * dx[k];
+#pragma unroll
+          for (int k = 0; k < D; k++) dotvv += velij[k] * velij[k];
+          const T kab = (D == 3) ? T(10.0) * T(EPS_HALF) * Cp_ij * dotrr * dotvv / (T(PRANDTL) * dotvr) : T(0);
+          kij = kab / (hij * cab);
+        }
+        T W_r = 0, r_sq = 0, Fij = 0;
+#pragma unroll
+        for (int k = 0; k < D; k++) W_r += dw[k] * dx[k];
+        if (W_r != T(0)) {
+#pragma unroll
+          for (int k = 0; k < D; k++) r_sq += dx[k] * dx[k];
+          Fij = W_r / r_sq;
+        }
+        heat_sum.add(mj * Vj * Vi * kij * (tempi - T(A.T[j])) * Fij);
+      }
+    }
+  });
+  double rv[3], xdot_rv = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    rv[k] = (double)rhs_v[k].get();
+    const double xdot = (double)I.v[k] + 0.5 * dt * (rv[k] + (k == D - 1 ? grav : 0.0));
+    xdot_rv += xdot * rv[k];
   }
+  const double rhs_e = -(double)vF.get() - xdot_rv + (double)heat_sum.get();
   const double vi[3] = {A.vx[i], D == 3 ? A.vy[i] : 0.0, D == 3 ? A.vz[i] : 0.0};
   double unew[3];
 #pragma unroll
-  for (int k = 0; k < D; k++) unew[k] = vi[k] + dt * (double)rv[k];
+  for (int k = 0; k < D; k++) unew[k] = vi[k] + dt * rv[k];
   unew[D - 1] += dt * grav;
   W.nv0[i] = unew[0];
   if (D == 3) { W.nv1[i] = unew[1]; W.nv2[i] = unew[2]; }
-  W.ne[i] = A.e[i] + dt * ((double)rhs_e.get() + (double)I.v[D - 1] * grav);
+  W.ne[i] = A.e[i] + dt * (rhs_e + (double)I.v[D - 1] * grav);
 }
 
 }  // namespace plume
