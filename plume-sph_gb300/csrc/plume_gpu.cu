@@ -950,8 +950,8 @@ static void launch_gsph(plume_ctx* ctx, int nb) {
   const bool recon = ctx->o.gsph_recon != PLUME_RECON_ZEROTH;
   ctx->grad_valid = recon || ctx->opt.gsph_gradients;
   if (ctx->grad_valid) {
-    k_gsph_grad<D><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
-                                            ctx->grad);
+    k_gsph_grad<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count,
+                                               ctx->ts, ctx->grad);
     ctx->launches++;
   }
   k_gsph_mom<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->h27, ctx->d_count,

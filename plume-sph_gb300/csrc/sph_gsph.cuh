@@ -26,8 +26,10 @@ constexpr double C_SHOCK = 3.0;  // C_SHOCK, constant.h:103
 // over j != i inside the CUTOFF2 h_i box; with more than 20 such j the
 // gradient is inv(A) F (linsolve, sph_lib.cc:161-182: the cofactor matrix
 // over the determinant in 3D, -1/A in 1D), else zero.  grad holds
-// (D+2)*D doubles per row: q-major, x_k fastest.
-template <int D>
+// (D+2)*D doubles per row: q-major, x_k fastest.  T = double: the
+// reference's arithmetic; T = float (mixed path): FP32 pair terms on
+// bucket-relative positions with compensated sums, the solve in FP64.
+template <int D, typename T>
 __global__ void k_gsph_grad(Opt o, const Geo* __restrict__ geo, Dev A, Work W, const uint32_t* __restrict__ cs_all,
                             const int* __restrict__ d_count, const TimeState* __restrict__ ts_all,
                             double* __restrict__ grad) {
@@ -47,86 +49,85 @@ __global__ void k_gsph_grad(Opt o, const Geo* __restrict__ geo, Dev A, Work W, c
   const double xi[3] = {A.x[i], D == 3 ? A.y[i] : 0.0, D == 3 ? A.z[i] : 0.0};
   int bi[3];
   bucket_coords<D>(g, A.bkt[i], bi);
-  const double hi = A.h[i];
-  const double supp = o.cutoff2 * hi;
-  const double Lb = o.list_factor * W.hlist[i];
-  const double rhoi = A.rho[i], pi = A.p[i];
-  const double vi[3] = {A.vx[i], D == 3 ? A.vy[i] : 0.0, D == 3 ? A.vz[i] : 0.0};
-  double AA[D * D], FF[D][NQ];
-#pragma unroll
-  for (int q = 0; q < D * D; q++) AA[q] = 0.0;
-#pragma unroll
-  for (int a = 0; a < D; a++)
-#pragma unroll
-    for (int q = 0; q < NQ; q++) FF[a][q] = 0.0;
+  T xs[3];
+  Pos<D, T>::load(A, W, i, xs);
+  const double hi_d = A.h[i];
+  const T hi = T(hi_d);
+  const T supp = T(o.cutoff2) * hi;
+  const T Lb = T(o.list_factor * W.hlist[i]);
+  const T rhoi = T(A.rho[i]), pi = T(A.p[i]);
+  const T vi[3] = {T(A.vx[i]), D == 3 ? T(A.vy[i]) : T(0), D == 3 ? T(A.vz[i]) : T(0)};
+  Acc<T> AA[D * D], FF[D][NQ];
   // The sums only gain from j with a non-zero dW (inside the kernel support
   // of h_i), so the walk covers that reach; its in-list count is a lower
   // bound of the reference's count over the CUTOFF2 h_i box.  Only when it
   // is <= 20 does a second, count-only walk over the full box decide.
   int nreal = 0;
-  const double Rk = fmin(supp, o.ksupport * hi) * (1.0 + 1e-10);
-  for_segments<D, double>(g, cs, xi, bi, Rk, [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+  const double Rk = fmin(o.cutoff2 * hi_d, o.ksupport * hi_d) * (1.0 + 1e-10);
+  for_segments<D, T>(g, cs, xi, bi, Rk, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+    const T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
     for (uint32_t j = j0; j < j1; j++) {
       if (j == (uint32_t)i) continue;
-      double dx[3];
-      dx[0] = xi[0] - A.x[j];
-      if (D == 3) { dx[1] = xi[1] - A.y[j]; dx[2] = xi[2] - A.z[j]; }
-      if (!own && !in_box<D, double>(dx, Lb)) continue;
-      if (!in_box<D, double>(dx, supp)) continue;
+      T dx[3];
+      pair_dx<D, T>(xsh, xi, A, W, j, dx);
+      if (!own && !in_box<D, T>(dx, Lb)) continue;
+      if (!in_box<D, T>(dx, supp)) continue;
       nreal++;
-      double sv[3], dw[3], dwm[3];
+      T sv[3], dw[3], dwm[3];
 #pragma unroll
       for (int k = 0; k < D; k++) sv[k] = dx[k] / hi;
-      kdw<D, double>(o.kernel, sv, hi, dw);
-      const double mj = A.mass[j], rhoj = A.rho[j];
+      kdw<D, T>(o.kernel, sv, hi, dw);
+      const T mj = T(A.mass[j]), rhoj = T(A.rho[j]);
 #pragma unroll
       for (int k = 0; k < D; k++) dwm[k] = dw[k] * mj / rhoj;
 #pragma unroll
       for (int a = 0; a < D; a++)
 #pragma unroll
-        for (int b = 0; b < D; b++) AA[a * D + b] -= dx[a] * dwm[b];
-      const double vj[3] = {A.vx[j], D == 3 ? A.vy[j] : 0.0, D == 3 ? A.vz[j] : 0.0};
-      const double dr = rhoi - rhoj, dp = pi - A.p[j];
+        for (int b = 0; b < D; b++) AA[a * D + b].sub(dx[a] * dwm[b]);
+      const T vj[3] = {T(A.vx[j]), D == 3 ? T(A.vy[j]) : T(0), D == 3 ? T(A.vz[j]) : T(0)};
+      const T dr = rhoi - rhoj, dp = pi - T(A.p[j]);
 #pragma unroll
       for (int a = 0; a < D; a++) {
-        FF[a][0] -= dr * dwm[a];
+        FF[a][0].sub(dr * dwm[a]);
 #pragma unroll
-        for (int b = 0; b < D; b++) FF[a][b + 1] -= (vi[b] - vj[b]) * dwm[a];
-        FF[a][NQ - 1] -= dp * dwm[a];
+        for (int b = 0; b < D; b++) FF[a][b + 1].sub((vi[b] - vj[b]) * dwm[a]);
+        FF[a][NQ - 1].sub(dp * dwm[a]);
       }
     }
   });
   if (nreal <= 20) {
     nreal = 0;
-    for_segments<D, double>(g, cs, xi, bi, supp * (1.0 + 1e-10),
-                            [&](uint32_t j0, uint32_t j1, bool own, double, double, double) {
+    for_segments<D, T>(g, cs, xi, bi, o.cutoff2 * hi_d * (1.0 + 1e-10),
+                       [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+      const T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
       for (uint32_t j = j0; j < j1; j++) {
         if (j == (uint32_t)i) continue;
-        double dx[3];
-        dx[0] = xi[0] - A.x[j];
-        if (D == 3) { dx[1] = xi[1] - A.y[j]; dx[2] = xi[2] - A.z[j]; }
-        if ((own || in_box<D, double>(dx, Lb)) && in_box<D, double>(dx, supp)) nreal++;
+        T dx[3];
+        pair_dx<D, T>(xsh, xi, A, W, j, dx);
+        if ((own || in_box<D, T>(dx, Lb)) && in_box<D, T>(dx, supp)) nreal++;
       }
     });
     if (nreal <= 20) return;
   }
-  double Ai[D * D];
+  double Ad[D * D], Ai[D * D];
+#pragma unroll
+  for (int q = 0; q < D * D; q++) Ad[q] = (double)AA[q].get();
   if constexpr (D == 1) {
-    Ai[0] = -1 / AA[0];
+    Ai[0] = -1 / Ad[0];
   } else {
     // entry (a,b) = cofactor C_ab over the determinant, as inv3 returns it;
     // A is symmetric, so this is its inverse
     double C[9];
-    C[0] = AA[4] * AA[8] - AA[5] * AA[7];
-    C[1] = -(AA[3] * AA[8] - AA[5] * AA[6]);
-    C[2] = AA[3] * AA[7] - AA[4] * AA[6];
-    C[3] = -(AA[1] * AA[8] - AA[2] * AA[7]);
-    C[4] = AA[0] * AA[8] - AA[2] * AA[6];
-    C[5] = -(AA[0] * AA[7] - AA[1] * AA[6]);
-    C[6] = AA[1] * AA[5] - AA[2] * AA[4];
-    C[7] = -(AA[0] * AA[5] - AA[2] * AA[3]);
-    C[8] = AA[0] * AA[4] - AA[1] * AA[3];
-    const double id = 1.0 / (AA[0] * C[0] + AA[1] * C[1] + AA[2] * C[2]);
+    C[0] = Ad[4] * Ad[8] - Ad[5] * Ad[7];
+    C[1] = -(Ad[3] * Ad[8] - Ad[5] * Ad[6]);
+    C[2] = Ad[3] * Ad[7] - Ad[4] * Ad[6];
+    C[3] = -(Ad[1] * Ad[8] - Ad[2] * Ad[7]);
+    C[4] = Ad[0] * Ad[8] - Ad[2] * Ad[6];
+    C[5] = -(Ad[0] * Ad[7] - Ad[1] * Ad[6]);
+    C[6] = Ad[1] * Ad[5] - Ad[2] * Ad[4];
+    C[7] = -(Ad[0] * Ad[5] - Ad[2] * Ad[3]);
+    C[8] = Ad[0] * Ad[4] - Ad[1] * Ad[3];
+    const double id = 1.0 / (Ad[0] * C[0] + Ad[1] * C[1] + Ad[2] * C[2]);
 #pragma unroll
     for (int q = 0; q < 9; q++) Ai[q] = C[q] * id;
   }
@@ -136,7 +137,7 @@ __global__ void k_gsph_grad(Opt o, const Geo* __restrict__ geo, Dev A, Work W, c
     for (int q = 0; q < NQ; q++) {
       double acc = 0.0;
 #pragma unroll
-      for (int b = 0; b < D; b++) acc += Ai[a * D + b] * FF[b][q];
+      for (int b = 0; b < D; b++) acc += Ai[a * D + b] * (double)FF[b][q].get();
       gi[q * D + a] = acc;
     }
 }
