@@ -143,9 +143,10 @@ struct VMom {
     re = 0;
     return true;
   }
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, double ox, double oy, double oz, double* dx,
                                          double& hj) const {
-    return f.filter(j, own, ox, oy, oz, dx, hj);
+    return f.template filter<LISTED>(j, own, ox, oy, oz, dx, hj);
   }
   __device__ __forceinline__ void math(uint32_t j, const double* dx, double hj) {
     const Dev& A = f.A;
@@ -387,9 +388,10 @@ struct VDens {
     hb = 0;
     return true;
   }
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, double ox, double oy, double oz, double* dx,
                                          double& hj) const {
-    return f.filter(j, own, ox, oy, oz, dx, hj);
+    return f.template filter<LISTED>(j, own, ox, oy, oz, dx, hj);
   }
   __device__ __forceinline__ void math(uint32_t j, const double* dx, double hj) {
     const Dev& A = f.A;
@@ -462,9 +464,10 @@ struct VVel {
     hb = 0;
     return true;
   }
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, double ox, double oy, double oz, double* dx,
                                          double& flag) const {
-    return f.filter(j, own, ox, oy, oz, dx, flag);
+    return f.template filter<LISTED>(j, own, ox, oy, oz, dx, flag);
   }
   __device__ __forceinline__ void math(uint32_t j, const double* dx, double) {
     const Dev& A = f.A;

@@ -222,6 +222,9 @@ struct WMom {
     W.nv2[ii] = unew2;
     W.ne[ii] = A.e[ii] + dt * (e + (double)veli[2] * grav);
   }
+  // LISTED: j comes from the stored list, which already passed the list
+  // box and the CUTOFF2 box (k_build_lists)
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& hj) const {
     if (j == i) return false;
     T xj[3];
@@ -229,8 +232,10 @@ struct WMom {
     dx[0] = (xs[0] + ox) - xj[0];
     dx[1] = (xs[1] + oy) - xj[1];
     dx[2] = (xs[2] + oz) - xj[2];
-    if (!own && !in_box<3, T>(dx, Lb)) return false;
-    if (!in_box<3, T>(dx, supp)) return false;
+    if (!LISTED) {
+      if (!own && !in_box<3, T>(dx, Lb)) return false;
+      if (!in_box<3, T>(dx, supp)) return false;
+    }
     const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
@@ -397,6 +402,7 @@ struct WDens {
     W.nrho[ii] = density;
     W.nY[ii] = r2 / density;
   }
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& hj) const {
     T xj[3];
     JPos<T>::get(A, K, j, xj, hj);
@@ -409,8 +415,10 @@ struct WDens {
     dx[0] = (xs[0] + ox) - xj[0];
     dx[1] = (xs[1] + oy) - xj[1];
     dx[2] = (xs[2] + oz) - xj[2];
-    if (!own && !in_box<3, T>(dx, Lb)) return false;
-    if (!in_box<3, T>(dx, supp)) return false;
+    if (!LISTED) {
+      if (!own && !in_box<3, T>(dx, Lb)) return false;
+      if (!in_box<3, T>(dx, supp)) return false;
+    }
     const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
@@ -506,6 +514,7 @@ struct WVel {
     A.vsy[ii] = vi_d[1] + d1 / wn;
     A.vsz[ii] = vi_d[2] + d2 / wn;
   }
+  template <bool LISTED = false>
   __device__ __forceinline__ bool filter(uint32_t j, bool own, T ox, T oy, T oz, T* dx, T& flag) const {
     T xj[3];
     JPos<T>::get(A, K, j, xj, flag);
@@ -517,8 +526,10 @@ struct WVel {
     dx[0] = (xs[0] + ox) - xj[0];
     dx[1] = (xs[1] + oy) - xj[1];
     dx[2] = (xs[2] + oz) - xj[2];
-    if (!own && !in_box<3, T>(dx, Lb)) return false;
-    if (!in_box<3, T>(dx, supp)) return false;
+    if (!LISTED) {
+      if (!own && !in_box<3, T>(dx, Lb)) return false;
+      if (!in_box<3, T>(dx, supp)) return false;
+    }
     return in_box<3, T>(dx, ks);
   }
   __device__ __forceinline__ void math(uint32_t j, const T* ds, T) {
@@ -773,7 +784,7 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
       const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
       mask &= mask - 1;
       T dx[3], hj;
-      if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
+      if (s.template filter<true>(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
     }
   }
 }
