@@ -94,6 +94,17 @@ extern "C" {
                                       against the domain faces (bucket.cc:435)*/
 #define PLUME_BUCKET_INACTIVE  0x4 /* not active: particles in it are not
                                       re-bucketed (update_pos.cc:203)        */
+#define PLUME_BUCKET_UNDERGROUND 0x8  /* bucket_type == UNDERGROUND          */
+#define PLUME_BUCKET_PRESS_BC    0x10 /* bucket_type == PRESS_BC (the grid's
+                                         outer pressure layer); a bucket with
+                                         neither these nor MIXED is OVERGROUND */
+
+/* ---- bucket involvement (Bucket::has_involved, bucket.h:230, 400-415):
+ *      bit 0 potentially involved particles, bit 1 involved particles ---- */
+#define PLUME_BINV_NONE       0  /* outside the domain (pressure ghosts)       */
+#define PLUME_BINV_POTENTIAL  1
+#define PLUME_BINV_INVOLVED   2
+#define PLUME_BINV_BOTH       3
 
 /* ---- arithmetic of the pair sweeps ------------------------------------ */
 #define PLUME_PREC_FP64   0  /* every pair term in FP64                       */
@@ -278,6 +289,31 @@ int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
  * If cap is smaller than the particle count nothing is written and *n
  * receives the count. */
 int plume_gsph_gradients(plume_ctx *ctx, uint64_t *key, double *grad, size_t cap, size_t *n);
+
+/* ---- domain growth (ADJUST_DOMAIN, main.cc:257-300, 433-436) ----------
+ * Every bucket carries an involvement state (PLUME_BINV_*), initially NONE
+ * for PLUME_BUCKET_ABSORBING buckets and POTENTIAL for the others
+ * (dataread.cc:457); plume_set_bucket_involvement overrides it (e.g. BOTH
+ * for the vent buckets, setup_influx.cc:206-209).
+ *
+ * plume_scan_outside_layer (scan_outside_layer.cc:37-121, run by the
+ * reference after every 3D step): a POTENTIAL bucket holding an involved
+ * particle (involved == 2) becomes BOTH; *adapt receives how many of those
+ * border a non-empty NONE bucket that is not UNDERGROUND (the reference's
+ * trigger for adapt_domain).
+ * plume_adapt_domain (adapt_domain.cc:41-194): every non-empty NONE bucket
+ * that is neither UNDERGROUND nor PRESS_BC and borders a bucket with
+ * involved particles (state bit 1) becomes POTENTIAL and stops absorbing;
+ * its particles turn real (bc 100) and potentially involved (1): on-ground
+ * MIXED buckets their pressure ghosts, other MIXED buckets those inside the
+ * domain (Bucket::determine_escape, bucket.cc:435-452), OVERGROUND buckets
+ * all.  The new pressure-ghost and wall-ghost layers of the reference's
+ * add_pressure_ghost / add_wall_ghost are particle creation on the host
+ * (plume_append), with a new image table (plume_set_wall_images). */
+int plume_set_bucket_involvement(plume_ctx *ctx, const uint8_t *state, size_t nbuckets);
+int plume_get_bucket_involvement(plume_ctx *ctx, uint8_t *state, size_t nbuckets);
+int plume_scan_outside_layer(plume_ctx *ctx, int *adapt);
+int plume_adapt_domain(plume_ctx *ctx);
 
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):

@@ -70,6 +70,11 @@ def lib():
                                         C.POINTER(OracleTime), C.c_int, C.POINTER(C.c_double), C.c_int,
                                         C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t,
                                         C.POINTER(C.c_size_t)]
+        L.oracle_scan_outside_layer.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                                C.POINTER(PlumeSoA), C.c_size_t, C.POINTER(C.c_uint8),
+                                                C.POINTER(C.c_int)]
+        L.oracle_adapt_domain.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid), C.POINTER(PlumeSoA),
+                                          C.c_size_t, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8)]
         _LIB = L
     return _LIB
 
@@ -179,6 +184,27 @@ class OracleRun:
         if n.value != self.ps.n:
             self.ps = self.ps.take(np.arange(n.value))
         return np.array(dts[:nsteps])
+
+    def scan_outside_layer(self, binv):
+        """scan_outside_layer on the current particles; binv (uint8 per
+        bucket) is updated in place; returns the count"""
+        s = self.ps.soa()
+        a = C.c_int(0)
+        rc = lib().oracle_scan_outside_layer(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n,
+                                             binv.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(a))
+        if rc:
+            raise RuntimeError(f"oracle_scan_outside_layer failed: {rc}")
+        return a.value
+
+    def adapt_domain(self, binv):
+        """adapt_domain; binv and the grid's flags (absorbing bit) updated in place"""
+        s = self.ps.soa()
+        flags = self.case.grid.flags
+        fp = flags.ctypes.data_as(C.POINTER(C.c_uint8)) if flags is not None else None
+        rc = lib().oracle_adapt_domain(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n,
+                                       binv.ctypes.data_as(C.POINTER(C.c_uint8)), fp)
+        if rc:
+            raise RuntimeError(f"oracle_adapt_domain failed: {rc}")
 
     def pairs(self, mode: int = 0):
         s = self.ps.soa()

@@ -69,6 +69,8 @@ struct Case {
   // optional wall images (3D): ghost key and image point of each
   std::vector<uint64_t> img_key;
   std::vector<double> img_xyz;
+  std::vector<uint8_t> binv;  // per-bucket has_involved (optional)
+  int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -123,6 +125,14 @@ static void read_case(const char *path, Case &c) {
     c.img_xyz.resize(3 * (size_t)nimg);
     rd(fp, c.img_key.data(), 8, (size_t)nimg);
     rd(fp, c.img_xyz.data(), 8, 3 * (size_t)nimg);
+  }
+  int64_t nbinv = 0;
+  if (fread(&nbinv, 8, 1, fp) == 1 && nbinv > 0) {
+    c.binv.resize((size_t)nbinv);
+    rd(fp, c.binv.data(), 1, (size_t)nbinv);
+    int32_t mode = 0;
+    rd(fp, &mode, 4, 1);
+    c.adapt_mode = mode;
   }
   fclose(fp);
 }
@@ -346,6 +356,9 @@ int main(int argc, char **argv) {
     out[1] = idx;
   };
   std::vector<Bucket *> bucks((size_t)nbx * nby * nbz);
+  bool explicit_types = false;
+  for (size_t b = 0; b < bucks.size(); b++)
+    explicit_types |= (c.flags[b] & (PLUME_BUCKET_UNDERGROUND | PLUME_BUCKET_PRESS_BC)) != 0;
   for (int i = 0; i < nbx; i++)
     for (int j = 0; j < nby; j++)
       for (int k = 0; k < nbz; k++) {
@@ -378,19 +391,30 @@ int main(int argc, char **argv) {
         int bt[6];
         for (int a = 0; a < 6; a++) bt[a] = c.face[6 * b + a];
         // bucket types of determine_bucket_type (preprocess.cc:404-439)
+        // (explicit UNDERGROUND / PRESS_BC flags, else an absorbing bucket
+        // is read as below or beside the ground)
         int btype = OVERGROUND;
         if (fl & PLUME_BUCKET_MIXED)
           btype = MIXED;
-        else if (fl & PLUME_BUCKET_ABSORBING)
+        else if (fl & PLUME_BUCKET_UNDERGROUND)
+          btype = UNDERGROUND;
+        else if (fl & PLUME_BUCKET_PRESS_BC)
+          btype = PRESS_BC;
+        else if ((fl & PLUME_BUCKET_ABSORBING) && !explicit_types)
           btype = (bt[4] == -1 && bt[5] == -1) ? UNDERGROUND : PRESS_BC;
         double flat[6] = { c.lo[0], c.hi[0], c.lo[1], c.hi[1], c.lo[2], c.hi[2] };
         double elev[4] = { c.lo[2], c.lo[2], c.lo[2], c.lo[2] };
         Bucket *bk = new Bucket(key, minx, maxx, btype, elev, 0, nproc, neigh, bt, flat);
         if (!(fl & PLUME_BUCKET_INACTIVE)) bk->mark_active();
-        if (fl & PLUME_BUCKET_ABSORBING)
+        if (!c.binv.empty()) {
           bk->set_has_no_involved();
-        else
+          if (c.binv[b] & 1) bk->set_has_potential_involved(true);
+          if (c.binv[b] & 2) bk->set_has_involved(true);
+        } else if (fl & PLUME_BUCKET_ABSORBING) {
+          bk->set_has_no_involved();
+        } else {
           bk->set_has_involved(true);
+        }
         bucks[b] = bk;
         BG->add(key, bk);
       }
@@ -497,9 +521,35 @@ int main(int argc, char **argv) {
       ndumped++;
     }
   }
+#if CODE_DIMENSION == 3 && defined(PLUME_ADJUST_DOMAIN)
+  // domain growth after the last step (main.cc:433-436, 257-265): the scan,
+  // then adapt_domain when it asks for it; the particles after it are an
+  // extra dumped record
+  int adapt_n = 0;
+  if (c.adapt_mode) {
+    adapt_n = scan_outside_layer(P, BG, 1, 0);
+    if (adapt_n) adapt_domain(P, BG, matprops, 1, 0);
+    dump_state(fo, P, c, *tp, 0.0);
+    ndumped++;
+  }
+#endif
   dump_lists(fo, P, c);
 #if USE_GSPH != 0
   dump_gradients(fo, P, c);
+#endif
+#if CODE_DIMENSION == 3 && defined(PLUME_ADJUST_DOMAIN)
+  // char[4] "ADPT"; int32 adapt; int64 nbk; uint8 has_involved per bucket
+  if (c.adapt_mode) {
+    fwrite("ADPT", 1, 4, fo);
+    int32_t a = adapt_n;
+    fwrite(&a, 4, 1, fo);
+    int64_t nbk = (int64_t)bucks.size();
+    fwrite(&nbk, 8, 1, fo);
+    for (size_t b = 0; b < bucks.size(); b++) {
+      uint8_t st = (uint8_t)bucks[b]->get_has_involved();
+      fwrite(&st, 1, 1, fo);
+    }
+  }
 #endif
   fseek(fo, 12, SEEK_SET);
   int32_t nd = ndumped;

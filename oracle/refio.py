@@ -18,9 +18,10 @@ def build_ref(ref_root: str = "/root/reference"):
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
 
 
-def write_case(path, case, nsteps, dump_last=False, images=None):
+def write_case(path, case, nsteps, dump_last=False, images=None, binv=None, adapt=False):
     """images: optional (ghost keys, image points (n, 3)) of the wall
-    boundary (3D)"""
+    boundary (3D); binv: optional per-bucket involvement states; adapt: run
+    scan_outside_layer / adapt_domain after the steps (ref3d_adapt)"""
     o, g, ps = case.options, case.grid, case.particles
     with open(path, "wb") as fp:
         fp.write(b"PLSPHIN1")
@@ -41,11 +42,15 @@ def write_case(path, case, nsteps, dump_last=False, images=None):
             fp.write(getattr(ps, f).astype("<f8").tobytes())
         for f in BYTE_FIELDS:
             fp.write(getattr(ps, f).astype(np.uint8).tobytes())
-        if images is not None:
-            keys, xyz = images
+        if images is not None or binv is not None:
+            keys, xyz = images if images is not None else (np.zeros(0, np.uint64), np.zeros((0, 3)))
             fp.write(struct.pack("<q", len(keys)))
             fp.write(np.ascontiguousarray(keys, dtype="<u8").tobytes())
             fp.write(np.ascontiguousarray(xyz, dtype="<f8").reshape(-1).tobytes())
+        if binv is not None:
+            fp.write(struct.pack("<q", len(binv)))
+            fp.write(np.ascontiguousarray(binv, dtype=np.uint8).tobytes())
+            fp.write(struct.pack("<i", int(adapt)))
 
 
 def read_result(path):
@@ -89,14 +94,21 @@ def read_result(path):
         nq = (dim + 2) * dim
         g = np.frombuffer(data, "<f8", ng * nq, off).copy().reshape(ng, nq); off += 8 * ng * nq
         steps[-1]["grad"] = (gk, g)
+    if data[off:off + 4] == b"ADPT":
+        # domain growth: the scan's count and the buckets' states after it
+        off += 4
+        (na,) = take("<i")
+        (nbk,) = take("<q")
+        st = np.frombuffer(data, np.uint8, nbk, off).copy(); off += nbk
+        steps[-1]["adapt"] = (int(na), st)
     return steps, lists
 
 
-def run_ref(variant, case, nsteps, workdir, dump_last=False, images=None):
+def run_ref(variant, case, nsteps, workdir, dump_last=False, images=None, binv=None, adapt=False):
     os.makedirs(workdir, exist_ok=True)
     cin = os.path.join(workdir, f"{case.name}.case")
     cout = os.path.join(workdir, f"{case.name}.out")
-    write_case(cin, case, nsteps, dump_last, images)
+    write_case(cin, case, nsteps, dump_last, images, binv, adapt)
     exe = os.path.join(HERE, "_ref", variant, "driver")
     subprocess.run([exe, cin, cout], check=True)
     return read_result(cout)

@@ -1508,6 +1508,150 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
     return PLUME_OK;
 }
 
+/* ------------------------------------------------------------------ */
+/* domain growth: scan_outside_layer (scan_outside_layer.cc:37-121) and */
+/* adapt_domain (adapt_domain.cc:41-194)                                */
+/* ------------------------------------------------------------------ */
+#define OR_UNDERGROUND 1
+#define OR_PRESS_BC    2
+#define OR_MIXED       3
+#define OR_OVERGROUND  4
+
+/* bucket_type as the harness builds it from the flags: explicit
+ * UNDERGROUND / PRESS_BC flags, else an absorbing bucket is below (both z
+ * faces -1) or beside the ground */
+static int bucket_type_of(const PlumeGrid *g, long b, int explicit_types)
+{
+    uint8_t f = bucket_flags(g, b);
+    if (f & PLUME_BUCKET_MIXED) return OR_MIXED;
+    if (f & PLUME_BUCKET_UNDERGROUND) return OR_UNDERGROUND;
+    if (f & PLUME_BUCKET_PRESS_BC) return OR_PRESS_BC;
+    if ((f & PLUME_BUCKET_ABSORBING) && !explicit_types) {
+        const int8_t *fi = g->face_index ? g->face_index + 6 * b : NULL;
+        return (fi && fi[4] == -1 && fi[5] == -1) ? OR_UNDERGROUND : OR_PRESS_BC;
+    }
+    return OR_OVERGROUND;
+}
+
+static int explicit_bucket_types(const PlumeGrid *g, long nbk)
+{
+    for (long b = 0; b < nbk && g->flags; b++)
+        if (g->flags[b] & (PLUME_BUCKET_UNDERGROUND | PLUME_BUCKET_PRESS_BC)) return 1;
+    return 0;
+}
+
+/* the in-grid neighbours of bucket b (26 at most) */
+static int bucket_neighbours(const PlumeGrid *g, long b, long *out)
+{
+    int nx = g->nb[0], ny = g->nb[1], nz = g->nb[2], k = 0;
+    int bx = (int)(b % nx), by = (int)((b / nx) % ny), bz = (int)(b / ((long)nx * ny));
+    for (int dx = -1; dx <= 1; dx++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dz = -1; dz <= 1; dz++) {
+                if (!dx && !dy && !dz) continue;
+                int cx = bx + dx, cy = by + dy, cz = bz + dz;
+                if (cx < 0 || cx >= nx || cy < 0 || cy >= ny || cz < 0 || cz >= nz) continue;
+                out[k++] = ((long)cz * ny + cy) * nx + cx;
+            }
+    return k;
+}
+
+int oracle_scan_outside_layer(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s, size_t n,
+                              uint8_t *binv, int *adapt)
+{
+    if (o->dim != 3 || !binv || !adapt) return PLUME_E_INVALID;
+    long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
+    size_t *cnt = (size_t *)calloc((size_t)nbk, sizeof(size_t));
+    char *inv = (char *)calloc((size_t)nbk, 1);
+    for (size_t i = 0; i < n; i++) {
+        long b = bucket_of(g, s->x[i], s->y[i], s->z[i]);
+        if (b < 0) { free(cnt); free(inv); return PLUME_E_OUTSIDE_GRID; }
+        cnt[b]++;
+        if (s->involved[i] == 2) inv[b] = 1;
+    }
+    int ex = explicit_bucket_types(g, nbk);
+    int a = 0;
+    long nbr[26];
+    for (long b = 0; b < nbk; b++) {
+        if (binv[b] != 1 || !inv[b]) continue;
+        binv[b] = 3; /* set_has_involved(HAS_BOTH): bit 1 on */
+        int k = bucket_neighbours(g, b, nbr);
+        for (int q = 0; q < k; q++) {
+            long nb = nbr[q];
+            if (cnt[nb] && binv[nb] == 0 && bucket_type_of(g, nb, ex) != OR_UNDERGROUND) {
+                a++;
+                break;
+            }
+        }
+    }
+    *adapt = a;
+    free(cnt);
+    free(inv);
+    return PLUME_OK;
+}
+
+/* flags (nbk, in/out): PLUME_BUCKET_ABSORBING leaves the converted buckets */
+int oracle_adapt_domain(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, size_t n,
+                        uint8_t *binv, uint8_t *flags)
+{
+    if (o->dim != 3 || !binv) return PLUME_E_INVALID;
+    long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
+    size_t *cnt = (size_t *)calloc((size_t)nbk, sizeof(size_t));
+    char *mark = (char *)calloc((size_t)nbk, 1);
+    long *bk = (long *)malloc(sizeof(long) * (n ? n : 1));
+    for (size_t i = 0; i < n; i++) {
+        bk[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
+        if (bk[i] < 0) { free(cnt); free(mark); free(bk); return PLUME_E_OUTSIDE_GRID; }
+        cnt[bk[i]]++;
+    }
+    int ex = explicit_bucket_types(g, nbk);
+    long nbr[26];
+    for (long b = 0; b < nbk; b++) {
+        int t = bucket_type_of(g, b, ex);
+        if (binv[b] != 0 || !cnt[b] || t == OR_UNDERGROUND || t == OR_PRESS_BC) continue;
+        int k = bucket_neighbours(g, b, nbr);
+        for (int q = 0; q < k; q++)
+            if (binv[nbr[q]] & 2) { mark[b] = 1; break; }
+    }
+    for (long b = 0; b < nbk; b++)
+        if (mark[b]) {
+            binv[b] = 1; /* set_has_involved(false), set_has_potential_involved(true) */
+            if (flags) flags[b] &= (uint8_t)~PLUME_BUCKET_ABSORBING;
+        }
+    for (size_t i = 0; i < n; i++) {
+        long b = bk[i];
+        if (!mark[b]) continue;
+        int t = bucket_type_of(g, b, ex);
+        const int8_t *fi = g->face_index ? g->face_index + 6 * b : NULL;
+        int turn;
+        if (t == OR_MIXED && fi && fi[4] == -1) {
+            turn = s->bc_type[i] == PLUME_BC_PRESSURE; /* on-ground MIXED: its pressure ghosts */
+        } else if (t == OR_MIXED) {
+            /* other MIXED: particles inside the domain (Bucket::determine_escape) */
+            double pos[3] = { s->x[i], s->y[i], s->z[i] };
+            int esc = 0;
+            for (int a = 0; a < 3 && fi; a++) {
+                if (fi[2 * a] == -1) {
+                    if ((pos[a] - g->domain_lo[a]) < -OR_TINY) esc = 1;
+                } else if (fi[2 * a + 1] == 1) {
+                    if ((pos[a] - g->domain_hi[a]) > OR_TINY) esc = 1;
+                }
+            }
+            turn = !esc;
+        } else {
+            turn = 1; /* OVERGROUND: every particle */
+        }
+        if (turn) {
+            s->bc_type[i] = PLUME_BC_REAL;
+            s->involved[i] = 1;
+        }
+    }
+    free(cnt);
+    free(mark);
+    free(bk);
+    return PLUME_OK;
+}
+
 int oracle_pairs(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
                  size_t n, int mode, uint64_t *key_i, uint64_t *key_j,
                  size_t cap, size_t *npairs)

@@ -68,6 +68,15 @@ int oracle_steps_grad(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *
                       size_t *n, OracleTime *t, int nsteps, double *dt_log, int nthreads,
                       double *grad, uint64_t *grad_key, size_t cap, size_t *n_grad);
 
+/* Domain growth (3D): scan_outside_layer and adapt_domain, the semantics
+ * of plume_scan_outside_layer / plume_adapt_domain; binv: per-bucket
+ * involvement states (in/out); flags (may be NULL): the bucket flags, whose
+ * ABSORBING bit adapt_domain clears on the buckets it converts. */
+int oracle_scan_outside_layer(const PlumeOptions *opt, const PlumeGrid *grid, const PlumeSoA *s, size_t n,
+                              uint8_t *binv, int *adapt);
+int oracle_adapt_domain(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA *s, size_t n,
+                        uint8_t *binv, uint8_t *flags);
+
 /* Neighbour pairs, same modes as plume_neighbor_pairs(). */
 int oracle_pairs(const PlumeOptions *opt, const PlumeGrid *grid,
                  const PlumeSoA *s, size_t n, int mode,

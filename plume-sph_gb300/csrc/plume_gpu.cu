@@ -609,6 +609,142 @@ __global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict_
   A.gam[i] = gam; A.p[i] = p; A.c[i] = c; A.T[i] = temp; A.cp[i] = cp;
 }
 
+// ---- domain growth (scan_outside_layer.cc:37-121, adapt_domain.cc:41-194)
+// Bucket types as the flags give them: explicit UNDERGROUND / PRESS_BC, else
+// an absorbing bucket is below (both z faces -1) or beside the ground.
+__device__ __forceinline__ int btype_of(uint8_t f, const int8_t* fi, bool explicit_types) {
+  if (f & PLUME_BUCKET_MIXED) return 3;
+  if (f & PLUME_BUCKET_UNDERGROUND) return 1;
+  if (f & PLUME_BUCKET_PRESS_BC) return 2;
+  if ((f & PLUME_BUCKET_ABSORBING) && !explicit_types) return (fi && fi[4] == -1 && fi[5] == -1) ? 1 : 2;
+  return 4;  // OVERGROUND
+}
+
+// particles of member-local bucket b: its s x s rows of s fine cells
+template <class F>
+__device__ __forceinline__ void for_bucket_rows(const Geo& g, const uint32_t* __restrict__ cs, int b, F&& f) {
+  const int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
+  for (int cz = bz * g.s; cz < bz * g.s + g.s; cz++)
+    for (int cy = by * g.s; cy < by * g.s + g.s; cy++) {
+      const size_t row = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0] + (size_t)bx * g.s;
+      f(cs[row], cs[row + g.s]);
+    }
+}
+
+__device__ __forceinline__ uint32_t bucket_count(const Geo& g, const uint32_t* __restrict__ cs, int b) {
+  uint32_t c = 0;
+  for_bucket_rows(g, cs, b, [&](uint32_t j0, uint32_t j1) { c += j1 - j0; });
+  return c;
+}
+
+// calls f(neighbour bucket) for the in-grid neighbours of b until f is true
+template <class F>
+__device__ __forceinline__ bool any_neighbour(const Geo& g, int b, F&& f) {
+  const int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
+  for (int dz = -1; dz <= 1; dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        if (!dx && !dy && !dz) continue;
+        const int cx = bx + dx, cy = by + dy, cz = bz + dz;
+        if (cx < 0 || cx >= g.nb[0] || cy < 0 || cy >= g.nb[1] || cz < 0 || cz >= g.nb[2]) continue;
+        if (f((cz * g.nb[1] + cy) * g.nb[0] + cx)) return true;
+      }
+  return false;
+}
+
+// One thread per bucket: a POTENTIAL bucket holding an involved particle
+// becomes BOTH (bit 1); it counts for the member when a neighbour is a
+// non-empty NONE bucket that is not UNDERGROUND.  1 -> 3 leaves every
+// "== 0" test unchanged, so the order of the buckets does not matter.
+__global__ void k_scan_outside(const Geo* __restrict__ geo, const uint16_t* __restrict__ bmember, Dev A,
+                               const uint32_t* __restrict__ cs_all, uint8_t* __restrict__ binv,
+                               const uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface, int nbk,
+                               int explicit_types, int* __restrict__ adapt) {
+  const int gb = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb >= nbk || binv[gb] != PLUME_BINV_POTENTIAL) return;
+  const int m = bmember[gb];
+  const Geo& g = geo[m];
+  const int b = gb - g.bucket_base;
+  const uint32_t* cs = cs_all + g.cell_base;
+  bool inv = false;
+  for_bucket_rows(g, cs, b, [&](uint32_t j0, uint32_t j1) {
+    for (uint32_t j = j0; j < j1 && !inv; j++) inv = A.inv[j] == 2;
+  });
+  if (!inv) return;
+  binv[gb] = PLUME_BINV_BOTH;
+  const bool grows = any_neighbour(g, b, [&](int nb) {
+    const int gn = g.bucket_base + nb;
+    const uint8_t f = bflags ? bflags[gn] : 0;
+    const int8_t* fi = bface ? bface + 6 * (size_t)gn : nullptr;
+    return binv[gn] == PLUME_BINV_NONE && btype_of(f, fi, explicit_types) != 1 && bucket_count(g, cs, nb) > 0;
+  });
+  if (grows) atomicAdd(adapt + m, 1);
+}
+
+// adapt_domain, buckets: a non-empty NONE bucket, neither UNDERGROUND nor
+// PRESS_BC, next to a bucket with involved particles becomes POTENTIAL and
+// stops absorbing (converted buckets get bit 1 clear, so the tests of the
+// other buckets do not see them change)
+__global__ void k_adapt_buckets(const Geo* __restrict__ geo, const uint16_t* __restrict__ bmember,
+                                const uint32_t* __restrict__ cs_all, uint8_t* __restrict__ binv,
+                                uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface, int nbk,
+                                int explicit_types, uint8_t* __restrict__ mark) {
+  const int gb = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb >= nbk) return;
+  mark[gb] = 0;
+  if (binv[gb] != PLUME_BINV_NONE) return;
+  const int m = bmember[gb];
+  const Geo& g = geo[m];
+  const int b = gb - g.bucket_base;
+  const uint8_t f = bflags ? bflags[gb] : 0;
+  const int t = btype_of(f, bface ? bface + 6 * (size_t)gb : nullptr, explicit_types);
+  if (t == 1 || t == 2) return;
+  const uint32_t* cs = cs_all + g.cell_base;
+  if (bucket_count(g, cs, b) == 0) return;
+  if (!any_neighbour(g, b, [&](int nb) { return (binv[g.bucket_base + nb] & PLUME_BINV_INVOLVED) != 0; })) return;
+  mark[gb] = 1;
+  binv[gb] = PLUME_BINV_POTENTIAL;
+  if (bflags) bflags[gb] = f & (uint8_t)~PLUME_BUCKET_ABSORBING;
+}
+
+// adapt_domain, particles of the converted buckets: real (100) and
+// potentially involved (1) -- on-ground MIXED buckets their pressure ghosts,
+// other MIXED buckets those inside the domain (determine_escape), OVERGROUND
+// buckets every particle
+__global__ void k_adapt_particles(const Geo* __restrict__ geo, Dev A, const int* __restrict__ d_count,
+                                  const uint8_t* __restrict__ mark, const uint8_t* __restrict__ bflags,
+                                  const int8_t* __restrict__ bface, int explicit_types) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count) return;
+  const uint8_t bc = A.bc[i];
+  if (bc == BC_DEAD) return;
+  const Geo& g = geo[A.mem[i]];
+  const int gb = g.bucket_base + A.bkt[i];
+  if (!mark[gb]) return;
+  const uint8_t f = bflags ? bflags[gb] : 0;
+  const int8_t* fi = bface ? bface + 6 * (size_t)gb : nullptr;
+  const int t = btype_of(f, fi, explicit_types);
+  bool turn = true;
+  if (t == 3 && fi && fi[4] == -1) {
+    turn = bc == PLUME_BC_PRESSURE;
+  } else if (t == 3) {
+    const double pos[3] = {A.x[i], A.y[i], A.z[i]};
+    bool esc = false;
+    for (int a = 0; a < 3 && fi; a++) {
+      if (fi[2 * a] == -1) {
+        if ((pos[a] - g.lo[a]) < -TINY_D) esc = true;
+      } else if (fi[2 * a + 1] == 1) {
+        if ((pos[a] - g.hi[a]) > TINY_D) esc = true;
+      }
+    }
+    turn = !esc;
+  }
+  if (turn) {
+    A.bc[i] = PLUME_BC_REAL;
+    A.inv[i] = 1;
+  }
+}
+
 // ---- eruption inlet (add_new_erupt, setup_erupt.cc:389-673) ---------------
 struct Inlet {
   const double* xy;   // column positions (2 per column)
@@ -787,6 +923,12 @@ struct plume_ctx {
   double* img_xyz = nullptr;
   int nimg = 0;
   int* bc_map = nullptr;  // row of (member, image), -1 when absent
+  // domain growth: involvement state per bucket, the scan's count per
+  // member, buckets converted by the last adapt_domain
+  uint8_t* binv = nullptr;
+  int* d_adapt = nullptr;
+  uint8_t* bmark = nullptr;
+  int explicit_types = 0;
   // GSPH gradients of the last step ((D+2)*D doubles per row; GSPH only)
   double* grad = nullptr;
   bool grad_valid = false;
@@ -1413,6 +1555,22 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
         memcpy(f.data() + 6 * (size_t)ctx->hgeo[m].bucket_base, grids[m].face_index, 6 * (size_t)ctx->hgeo[m].nbk);
     if ((rc = dev_alloc(ctx, (void**)&ctx->bface, 6 * (size_t)ctx->nbk))) return fail(rc);
     cudaMemcpy(ctx->bface, f.data(), 6 * (size_t)ctx->nbk, cudaMemcpyHostToDevice);
+  }
+  if (opt->dim == 3) {
+    // involvement: NONE where absorbing, POTENTIAL elsewhere (dataread.cc:457)
+    std::vector<uint8_t> st((size_t)ctx->nbk, PLUME_BINV_POTENTIAL);
+    for (int m = 0; m < nmem; m++)
+      if (grids[m].flags)
+        for (int b = 0; b < ctx->hgeo[m].nbk; b++) {
+          const uint8_t f = grids[m].flags[b];
+          if (f & PLUME_BUCKET_ABSORBING) st[ctx->hgeo[m].bucket_base + b] = PLUME_BINV_NONE;
+          if (f & (PLUME_BUCKET_UNDERGROUND | PLUME_BUCKET_PRESS_BC)) ctx->explicit_types = 1;
+        }
+    if ((rc = dev_alloc(ctx, (void**)&ctx->binv, ctx->nbk)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->bmark, ctx->nbk)) ||
+        (rc = dev_alloc(ctx, (void**)&ctx->d_adapt, sizeof(int) * (size_t)nmem)))
+      return fail(rc);
+    cudaMemcpy(ctx->binv, st.data(), ctx->nbk, cudaMemcpyHostToDevice);
   }
   if (cudaMallocHost(&ctx->h_ts, sizeof(TimeState) * (size_t)nmem) != cudaSuccess) {
     ctx->err = "cudaMallocHost";
@@ -2308,6 +2466,75 @@ int plume_adjoint_backward(plume_ctx* ctx, const PlumeSoA* final_bar, size_t n_f
   int rc = restore_ckpt(ctx, ctx->ckpts.back());
   if (rc) return rc;
   return finish_steps(ctx);
+}
+
+// ---------------------------------------------------------------- domain growth
+int plume_set_bucket_involvement(plume_ctx* ctx, const uint8_t* state, size_t nbuckets) {
+  if (!ctx || !state) return PLUME_E_INVALID;
+  if (!ctx->binv || nbuckets != (size_t)ctx->nbk) {
+    ctx->err = "bucket involvement: 3D only, one state per bucket of the context";
+    return PLUME_E_INVALID;
+  }
+  for (size_t b = 0; b < nbuckets; b++)
+    if (state[b] > PLUME_BINV_BOTH) {
+      ctx->err = "bucket involvement: states are 0..3";
+      return PLUME_E_INVALID;
+    }
+  CK(cudaMemcpyAsync(ctx->binv, state, nbuckets, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return PLUME_OK;
+}
+
+int plume_get_bucket_involvement(plume_ctx* ctx, uint8_t* state, size_t nbuckets) {
+  if (!ctx || !state) return PLUME_E_INVALID;
+  if (!ctx->binv || nbuckets != (size_t)ctx->nbk) {
+    ctx->err = "bucket involvement: 3D only, one state per bucket of the context";
+    return PLUME_E_INVALID;
+  }
+  CK(cudaMemcpyAsync(state, ctx->binv, nbuckets, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return PLUME_OK;
+}
+
+int plume_scan_outside_layer(plume_ctx* ctx, int* adapt) {
+  if (!ctx || !adapt) return PLUME_E_INVALID;
+  if (!ctx->binv) {
+    ctx->err = "scan_outside_layer: 3D only";
+    return PLUME_E_INVALID;
+  }
+  int rc = search(ctx);  // bucket contents of the current positions
+  if (rc) return rc;
+  cudaStream_t st = ctx->st;
+  cudaMemsetAsync(ctx->d_adapt, 0, sizeof(int) * (size_t)ctx->nmem, st);
+  k_scan_outside<<<nblocks(ctx->nbk), NTHREADS, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->A, ctx->cs, ctx->binv,
+                                                         ctx->bflags, ctx->bface, ctx->nbk, ctx->explicit_types,
+                                                         ctx->d_adapt);
+  std::vector<int> a((size_t)ctx->nmem);
+  CK(cudaMemcpyAsync(a.data(), ctx->d_adapt, sizeof(int) * (size_t)ctx->nmem, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  int sum = 0;
+  for (int v : a) sum += v;
+  *adapt = sum;
+  return PLUME_OK;
+}
+
+int plume_adapt_domain(plume_ctx* ctx) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (!ctx->binv) {
+    ctx->err = "adapt_domain: 3D only";
+    return PLUME_E_INVALID;
+  }
+  int rc = search(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->st;
+  k_adapt_buckets<<<nblocks(ctx->nbk), NTHREADS, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->cs, ctx->binv, ctx->bflags,
+                                                          ctx->bface, ctx->nbk, ctx->explicit_types, ctx->bmark);
+  const int n = (int)ctx->n_alloc;
+  k_adapt_particles<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->bmark,
+                                                             ctx->bflags, ctx->bface, ctx->explicit_types);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return PLUME_OK;
 }
 
 // ---------------------------------------------------------------- GSPH

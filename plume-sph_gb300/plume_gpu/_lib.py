@@ -91,6 +91,10 @@ def lib():
         L.plume_apply_bcond.argtypes = [C.c_void_p]
         L.plume_gsph_gradients.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_double), C.c_size_t,
                                            P(C.c_size_t)]
+        L.plume_set_bucket_involvement.argtypes = [C.c_void_p, P(C.c_uint8), C.c_size_t]
+        L.plume_get_bucket_involvement.argtypes = [C.c_void_p, P(C.c_uint8), C.c_size_t]
+        L.plume_scan_outside_layer.argtypes = [C.c_void_p, P(C.c_int)]
+        L.plume_adapt_domain.argtypes = [C.c_void_p]
         L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
                                              P(C.c_size_t), P(C.c_double)]

@@ -33,6 +33,8 @@ STATUS_NAMES = {
 
 BC_ERUPT, BC_PRESSURE, BC_WALL, BC_NOSAVE_REAL, BC_REAL = 0, 1, 2, 99, 100
 BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_INACTIVE = 0x1, 0x2, 0x4
+BUCKET_UNDERGROUND, BUCKET_PRESS_BC = 0x8, 0x10
+BINV_NONE, BINV_POTENTIAL, BINV_INVOLVED, BINV_BOTH = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 KERNEL_GAUSS, KERNEL_M4 = 0, 1
 METHOD_SPH, METHOD_GSPH = 0, 1

@@ -25,6 +25,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from .abi import (BC_ERUPT, BC_NOSAVE_REAL, BC_PRESSURE, BC_REAL, BC_WALL,
+                  BINV_NONE, BINV_POTENTIAL, BUCKET_PRESS_BC, BUCKET_UNDERGROUND,
                   BUCKET_ABSORBING, BUCKET_MIXED, KERNEL_GAUSS, KERNEL_M4,
                   METHOD_GSPH, METHOD_SPH, PREC_FP64, RECON_EACH, RECON_ZEROTH, RIEMANN_HLLC,
                   Grid, Options, ParticleSet)
@@ -334,6 +335,48 @@ def wall_images(case):
     img = pos[sel].copy()
     img[:, 2] = 2 * zg - img[:, 2]
     return keys, img
+
+
+def adapt_scenario(case):
+    """A domain-growth set-up on a plume built by plume_3d: explicit bucket
+    types (absorbing buckets below the ground UNDERGROUND, the other
+    absorbing ones PRESS_BC), involvement NONE where absorbing and POTENTIAL
+    elsewhere (dataread.cc:457); then the outermost non-absorbing bucket
+    layer on the +x side becomes a NONE layer of pressure ghosts (absorbing,
+    its real particles bc 1, as add_pressure_ghost leaves the ring around
+    the domain), and the particles of the layer inside it that sit in the
+    outer half of their bucket are marked involved (2).  The scan then finds
+    involved particles next to the pressure layer, and adapt_domain converts
+    that layer.  Returns (new case, per-bucket involvement states)."""
+    import dataclasses
+    g0 = case.grid
+    nb = np.array(g0.nb)
+    flags = np.array(g0.flags, dtype=np.uint8).copy()
+    face = np.asarray(g0.face_index, dtype=np.int8).reshape(-1, 6)
+    absorbing = (flags & BUCKET_ABSORBING) != 0
+    under = absorbing & (face[:, 4] == -1) & (face[:, 5] == -1)
+    flags[under] |= BUCKET_UNDERGROUND
+    flags[absorbing & ~under] |= BUCKET_PRESS_BC
+    binv = np.where(absorbing, BINV_NONE, BINV_POTENTIAL).astype(np.uint8)
+    idx = np.arange(len(flags))
+    bx = idx % nb[0]
+    bx_max = int(bx[~absorbing].max())
+    layer = (~absorbing) & (bx == bx_max)
+    inner = (~absorbing) & (bx == bx_max - 1)
+    flags[layer] |= BUCKET_ABSORBING
+    binv[layer] = BINV_NONE
+    ps = case.particles.copy()
+    pos = np.stack([ps.x, ps.y, ps.z], axis=1)
+    mind = np.array(g0.mindom)
+    b3 = np.clip(np.floor((pos - mind) / g0.del_).astype(np.int64), 0, nb - 1)
+    pb = (b3[:, 2] * nb[1] + b3[:, 1]) * nb[0] + b3[:, 0]
+    real = (ps.bc_type == BC_REAL) | (ps.bc_type == BC_NOSAVE_REAL)
+    ps.bc_type[layer[pb] & real] = BC_PRESSURE
+    ps.involved[layer[pb] & real] = 0
+    outer_half = (pos[:, 0] - (mind[0] + b3[:, 0] * g0.del_)) > 0.5 * g0.del_
+    ps.involved[inner[pb] & real & outer_half] = 2
+    grid = dataclasses.replace(g0, flags=flags, face_index=np.array(g0.face_index).copy())
+    return dataclasses.replace(case, grid=grid, particles=ps, name=case.name + "_adapt"), binv
 
 
 def inlet(case):

@@ -155,6 +155,28 @@ class Solver:
     def apply_bcond(self):
         self._check(self.L.plume_apply_bcond(self.ctx), "plume_apply_bcond")
 
+    # -- domain growth --------------------------------------------------------
+    def set_bucket_involvement(self, state):
+        """per-bucket involvement states (abi.BINV_*), x fastest"""
+        st = np.ascontiguousarray(state, dtype=np.uint8)
+        self._check(self.L.plume_set_bucket_involvement(self.ctx, st.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                        len(st)), "plume_set_bucket_involvement")
+
+    def bucket_involvement(self):
+        st = np.zeros(self.case.grid.nbuckets, dtype=np.uint8)
+        self._check(self.L.plume_get_bucket_involvement(self.ctx, st.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                        len(st)), "plume_get_bucket_involvement")
+        return st
+
+    def scan_outside_layer(self) -> int:
+        """scan_outside_layer: the count that asks for adapt_domain"""
+        a = C.c_int(0)
+        self._check(self.L.plume_scan_outside_layer(self.ctx, C.byref(a)), "plume_scan_outside_layer")
+        return a.value
+
+    def adapt_domain(self):
+        self._check(self.L.plume_adapt_domain(self.ctx), "plume_adapt_domain")
+
     # -- GSPH -----------------------------------------------------------------
     def gsph_gradients(self):
         """(keys, (n, (D+2)*D) gradients) of the last GSPH step

@@ -56,6 +56,14 @@ def gsph_case(name):
     return c
 
 
+def adapt_case():
+    """the plume of the domain-growth fixture, before cases.adapt_scenario"""
+    c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
+                       vent_dx=25.0, duct_depth=300.0, seed=6, name="adapt_3d")
+    c.step0 = 48
+    return c
+
+
 def golden_case(name):
     """(case with the fixture's input particles, fixture dict)"""
     d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))

@@ -22,6 +22,8 @@ state and a summary of the reference's neighbour lists:
                        reference's apply_bcond before the loop and after each
                        of steps 49..51
   gsph_*.npz           GSPH builds (make_gsph)
+  adapt_3d.npz         domain growth: scan_outside_layer + adapt_domain
+                       (make_adapt)
 
 Usage (in a container that has the reference tree):
   python tests/golden/make_golden.py [--ref /root/reference]
@@ -43,7 +45,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 from plume_gpu import cases  # noqa: E402
 from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS  # noqa: E402
 from oracle import refio  # noqa: E402
-from _util import gsph_case  # noqa: E402
+from _util import adapt_case, gsph_case  # noqa: E402
 
 MASK = np.uint64(0xFFFFFFFFFFFFFFFF)
 
@@ -139,6 +141,7 @@ def main():
     make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_small.npz"))
     make_bc()
     make_gsph()
+    make_adapt()
 
 
 def make_gsph():
@@ -155,6 +158,27 @@ def make_gsph():
     make(gsph_case("gsph_3d"), "ref3d_gsph", 2, os.path.join(HERE, "gsph_3d.npz"))
 
 
+def make_adapt():
+    """adapt_3d.npz: domain growth on the small plume (seed 6): one step
+    (step 49), then the reference's scan_outside_layer and adapt_domain on
+    the set-up of cases.adapt_scenario; stores the input, the bucket flags
+    and involvement states before and after, the scan's count, and the
+    particles' key, bc type, involvement and x after adapt_domain."""
+    c = adapt_case()
+    c, binv = cases.adapt_scenario(c)
+    steps, _ = refio.run_ref("ref3d_adapt", c, 1, "/tmp/plume_golden", binv=binv, adapt=True)
+    na, st = steps[-1]["adapt"]
+    out = steps[-1]["particles"].sorted_by_key()
+    d = {"nsteps": 1, "step0": c.step0, "pre_adaptive": 0, "dim": 3,
+         "flags": np.asarray(c.grid.flags, dtype=np.uint8), "binv_in": binv, "binv_out": st,
+         "adapt": np.int64(na), "out_key": out.key, "out_bc_type": out.bc_type,
+         "out_involved": out.involved, "out_x": out.x}
+    d.update(pack("in_", c.particles))
+    path = os.path.join(HERE, "adapt_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def make_bc():
     c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
                        vent_dx=25.0, duct_depth=300.0, seed=4, name="plume_3d_bc")
@@ -166,5 +190,8 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--gsph":
         refio.build_ref()
         make_gsph()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
+        refio.build_ref()
+        make_adapt()
     else:
         main()

@@ -7,6 +7,8 @@ to the last bit on its first step and to rounding afterwards (the
 reference re-orders bucket lists when particles move, update_pos.cc:171-463,
 which changes the summation order).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -186,3 +188,37 @@ def test_oracle_gsph_3d_matches_reference():
     gref = d["grad"]
     gerr = np.abs(_grad_by_key(gk, g, d["grad_key"]) - gref).max(axis=0) / (np.abs(gref).max(axis=0) + 1e-300)
     assert gerr.max() < 1e-12, gerr
+
+
+# ---------------------------------------------------------------- domain growth
+def _adapt_fixture():
+    from _util import adapt_case
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "adapt_3d.npz")))
+    c, binv = cases.adapt_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    c.grid.flags = np.array(d["flags"], dtype=np.uint8)
+    np.testing.assert_array_equal(binv, d["binv_in"])
+    return c, d
+
+
+def test_oracle_domain_growth_matches_reference():
+    """one step, then scan_outside_layer and adapt_domain: the scan's count,
+    every bucket's involvement state and every particle's bc type and
+    involvement identical to the reference's"""
+    c, d = _adapt_fixture()
+    o = OracleRun(c)
+    o.steps(int(d["nsteps"]))
+    binv = np.array(d["binv_in"], dtype=np.uint8)
+    a = o.scan_outside_layer(binv)
+    assert a == int(d["adapt"]) and a > 0
+    o.adapt_domain(binv)
+    np.testing.assert_array_equal(binv, d["binv_out"])
+    ps = o.ps.sorted_by_key()
+    np.testing.assert_array_equal(ps.key, d["out_key"])
+    np.testing.assert_array_equal(ps.bc_type, d["out_bc_type"])
+    np.testing.assert_array_equal(ps.involved, d["out_involved"])
+    np.testing.assert_allclose(ps.x, d["out_x"], rtol=0, atol=1e-9)
+    assert (d["binv_out"] == 1).sum() > (d["binv_in"] == 1).sum()  # buckets were converted
+    # the converted buckets stopped absorbing
+    conv = (d["binv_in"] == 0) & (d["binv_out"] == 1)
+    assert not np.any(c.grid.flags[conv] & cases.BUCKET_ABSORBING)
