@@ -272,19 +272,38 @@ struct WMom {
       vis -= T(EPS_HALF) * dotv * Vj;
     }
     const T mpvsqij = mj * (pVVj + pvsqi + vis);
-    T dwdx[3];
-    if (sizeof(T) == 8 || o.kernel == 1) {
-      kdw<3, T>(o.kernel, si, h, dwdx);
-    } else {
-      // Gaussian, mixed: W = (T1/h)^3 exp(-s.s), dW/dx_k = -2 s_k / h W
-      const T w = (fabs(si[0]) > T(3) || fabs(si[1]) > T(3) || fabs(si[2]) > T(3))
-                      ? T(0)
-                      : (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) *
-                            __expf(-(si[0] * si[0] + si[1] * si[1] + si[2] * si[2]));
-      const T f = T(-2) * ih * w;
+    if constexpr (sizeof(T) == 4) {
+      if (o.kernel != 1) {
+        // Gaussian, mixed: dW/dx_k = f s_k with f = -2 W / h; the reference's
+        // sums regrouped with s = dx / h: dW . v_ij = f vrab / h,
+        // dW . dx = f |dx|^2 / h, so F_ij = dW . dx / |dx|^2 = f / h
+        const T w = (fabs(si[0]) > T(3) || fabs(si[1]) > T(3) || fabs(si[2]) > T(3))
+                        ? T(0)
+                        : (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) * (T(T1_INV_SQRT_PI) * ih) *
+                              __expf(-(si[0] * si[0] + si[1] * si[1] + si[2] * si[2]));
+        const T f = T(-2) * ih * w;
+        const T gm = mpvsqij * f;
 #pragma unroll
-      for (int k = 0; k < 3; k++) dwdx[k] = f * si[k];
+        for (int k = 0; k < 3; k++) rv[k].sub(gm * si[k]);
+        T heat_tran = 0;
+        if (lans && f != T(0)) {
+          const T Cp_ij = T(0.5) * (cpj + Cp_i);
+          T dotvr = 0;
+#pragma unroll
+          for (int k = 0; k < 3; k++) dotvr += fabs(velij[k] * dx[k]);
+          if (dotvr != T(0)) {
+            // k_ij = 10 eps Cp_ij |dx|^2 |v_ij|^2 / (Pr dotvr h c_ab), one reciprocal
+            const T kij = T(10.0) * T(EPS_HALF) * Cp_ij * dist_sq * dotv *
+                          rcp<T>(T(PRANDTL) * dotvr * h * sndspdab);
+            heat_tran = mj * Vj * Vi * kij * (tempi - Tj) * (f * ih);
+          }
+        }
+        re.add(T(0.5) * gm * ih * vrab + heat_tran);
+        return;
+      }
     }
+    T dwdx[3];
+    kdw<3, T>(o.kernel, si, h, dwdx);
     T heat_tran = 0;
     if (lans) {
       const T Cp_ij = T(0.5) * (cpj + Cp_i);
@@ -437,6 +456,29 @@ struct WDens {
     const T ih = rcp<T>(hh);
 #pragma unroll
     for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hh : ds[k] * ih;
+    if constexpr (sizeof(T) == 4) {
+      if (o.kernel != 1) {
+        // Gaussian, mixed: W(s, h) = r^3 exp(-s.s), r = 1/(sqrt(pi) h); the
+        // energy-smoothing kernel at h/4 is 64 r^3 exp(-16 s.s), zero once
+        // any |s_k| > 3/4
+        const float ax = fabsf(sv[0]), ay = fabsf(sv[1]), az = fabsf(sv[2]);
+        const float q = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2];
+        const float r = float(T1_INV_SQRT_PI) * ih;
+        const float r3 = r * r * r;
+        if (esm && fmaxf(ax, fmaxf(ay, az)) <= 0.75f) {
+          const float w_e = 64.0f * r3 * __expf(-16.0f * q);
+          wnorm_e.add(w_e * mvr);
+          engr.add(w_e * mer);
+        }
+        if (fmaxf(ax, fmaxf(ay, az)) > 3.0f) return;
+        const float wm = r3 * __expf(-q) * mj;
+        if (ph == 1.0f)
+          rho1.add(wm);
+        else
+          rho2.add(wm);
+        return;
+      }
+    }
     if (esm) {
       T s_e[3];
 #pragma unroll
