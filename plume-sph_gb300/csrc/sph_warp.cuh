@@ -521,6 +521,7 @@ struct WVel {
   const Packed& K;
   const Opt& o;
   T xs[3], hi, supp, ks, Lb, vi[3];
+  T ihi, r3;  // 1/h_i and (1/(sqrt(pi) h_i))^3 (mixed Gaussian)
   Acc<T> dv[3], wnorm;
   __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   double vi_d[3];
@@ -534,6 +535,8 @@ struct WVel {
     supp = T(o.cutoff2) * hi;
     ks = T(o.ksupport * (1.0 + 1e-6)) * hi;
     Lb = T(o.list_factor * W.hlist[ii]);
+    ihi = rcp<T>(hi);
+    r3 = (T(T1_INV_SQRT_PI) * ihi) * (T(T1_INV_SQRT_PI) * ihi) * (T(T1_INV_SQRT_PI) * ihi);
     vi_d[0] = A.vx[ii]; vi_d[1] = A.vy[ii]; vi_d[2] = A.vz[ii];
     vi[0] = T(vi_d[0]); vi[1] = T(vi_d[1]); vi[2] = T(vi_d[2]);
     R = fmin(o.cutoff2, o.ksupport) * hi_d * (1.0 + 1e-10);
@@ -585,10 +588,16 @@ struct WVel {
       mvr = q.x; vj[0] = q.y; vj[1] = q.z; vj[2] = q.w;
     }
     T sv[3];
-    const T ih = rcp<T>(hi);
 #pragma unroll
-    for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hi : ds[k] * ih;
-    const T wght = kw<3, T>(o.kernel, sv, hi);
+    for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hi : ds[k] * ihi;
+    T wght;
+    if (sizeof(T) == 4 && o.kernel != 1) {
+      // Gaussian, mixed: the normalisation of h_i formed once per particle
+      const T q = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2];
+      wght = (fabs(sv[0]) > T(3) || fabs(sv[1]) > T(3) || fabs(sv[2]) > T(3)) ? T(0) : r3 * __expf(-q);
+    } else {
+      wght = kw<3, T>(o.kernel, sv, hi);
+    }
     const T mvw = (sizeof(T) == 8) ? wght * mj / rhoj : wght * mvr;
 #pragma unroll
     for (int k = 0; k < 3; k++) dv[k].add(mvw * (vj[k] - vi[k]));
