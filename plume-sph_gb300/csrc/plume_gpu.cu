@@ -1634,6 +1634,82 @@ int plume_destroy(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
+// ---- host <-> device particle copies
+// A table of copies in one launch: when every host array is page-locked
+// (mapped into the device's address space), the device moves the whole
+// particle table itself, reading or writing host memory over the
+// CPU-GPU link, instead of one DMA transfer per field.
+struct CopyJob {
+  char* dst;
+  const char* src;
+  unsigned long long bytes;
+};
+struct CopyJobs {
+  CopyJob j[24];
+  int n;
+};
+__global__ void k_copy_multi(CopyJobs J) {
+  const CopyJob c = J.j[blockIdx.y];
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const uintptr_t al = (uintptr_t)c.dst | (uintptr_t)c.src;
+  size_t done = 0;
+  if ((al & 15) == 0) {
+    const size_t nv = c.bytes >> 4;
+    const uint4* sv = reinterpret_cast<const uint4*>(c.src);
+    uint4* dv = reinterpret_cast<uint4*>(c.dst);
+    for (size_t k = tid; k < nv; k += stride) dv[k] = sv[k];
+    done = nv << 4;
+  } else if ((al & 7) == 0) {
+    const size_t nv = c.bytes >> 3;
+    const uint2* sv = reinterpret_cast<const uint2*>(c.src);
+    uint2* dv = reinterpret_cast<uint2*>(c.dst);
+    for (size_t k = tid; k < nv; k += stride) dv[k] = sv[k];
+    done = nv << 3;
+  }
+  for (size_t k = done + tid; k < c.bytes; k += stride) c.dst[k] = c.src[k];
+}
+
+// device-side address of a page-locked host array, or null
+static void* mapped_host(const void* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// issues the copies (the host side is src for H2D, dst for D2H); one kernel
+// when every host array is mapped, else one cudaMemcpyAsync each (also for
+// device-to-device copies)
+static int run_copies(plume_ctx* ctx, const std::vector<CopyJob>& jobs, cudaMemcpyKind kind) {
+  cudaStream_t st = ctx->st;
+  const bool h2d = kind == cudaMemcpyHostToDevice;
+  CopyJobs J{};
+  bool mapped = jobs.size() <= 24 && (h2d || kind == cudaMemcpyDeviceToHost);
+  for (size_t q = 0; q < jobs.size() && mapped; q++) {
+    CopyJob c = jobs[q];
+    void* dp = mapped_host(h2d ? (const void*)c.src : (const void*)c.dst);
+    if (!dp) {
+      mapped = false;
+      break;
+    }
+    if (h2d) c.src = (const char*)dp; else c.dst = (char*)dp;
+    J.j[J.n++] = c;
+  }
+  if (mapped && J.n > 0) {
+    dim3 grid(2 * 152, J.n);
+    k_copy_multi<<<grid, 256, 0, st>>>(J);
+    ctx->launches++;
+    CK(cudaGetLastError());
+    return PLUME_OK;
+  }
+  for (const CopyJob& c : jobs)
+    if (c.bytes) CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, kind, st));
+  return PLUME_OK;
+}
+
 static int check_soa(plume_ctx* ctx, const PlumeSoA* s) {
   if (!s || !s->key || !s->x || !s->vx || !s->mass || !s->h || !s->rho || !s->e || !s->p || !s->Y ||
       !s->gamma || !s->c || !s->T || !s->cp || !s->phase || !s->bc_type || !s->involved) {
@@ -1662,34 +1738,36 @@ static int copy_soa(plume_ctx* ctx, const PlumeSoA* s, size_t off, size_t n, cud
   const bool d3 = ctx->o.dim == 3;
   cudaStream_t st = ctx->st;
   Dev& A = ctx->A;
-  CK(cudaMemcpyAsync(A.key + off, s->key, 8 * n, kind, st));
+  std::vector<CopyJob> jobs;
+  auto job = [&](void* d, const void* h, size_t bytes) { jobs.push_back(CopyJob{(char*)d, (const char*)h, bytes}); };
+  job(A.key + off, s->key, 8 * n);
   struct F { double* d; const double* h; } f[] = {
       {A.x, s->x}, {A.vx, s->vx}, {A.mass, s->mass}, {A.h, s->h}, {A.rho, s->rho}, {A.e, s->e},
       {A.p, s->p}, {A.Y, s->Y}, {A.gam, s->gamma}, {A.c, s->c}, {A.T, s->T}, {A.cp, s->cp}};
-  for (auto& q : f) CK(cudaMemcpyAsync(q.d + off, q.h, 8 * n, kind, st));
+  for (auto& q : f) job(q.d + off, q.h, 8 * n);
   if (d3) {
-    CK(cudaMemcpyAsync(A.y + off, s->y, 8 * n, kind, st));
-    CK(cudaMemcpyAsync(A.z + off, s->z, 8 * n, kind, st));
-    CK(cudaMemcpyAsync(A.vy + off, s->vy, 8 * n, kind, st));
-    CK(cudaMemcpyAsync(A.vz + off, s->vz, 8 * n, kind, st));
+    job(A.y + off, s->y, 8 * n);
+    job(A.z + off, s->z, 8 * n);
+    job(A.vy + off, s->vy, 8 * n);
+    job(A.vz + off, s->vz, 8 * n);
   }
   // smoothed velocity: optional on upload (zero when absent)
   double* vs[3] = {A.vsx, A.vsy, A.vsz};
   const double* hv[3] = {s->vsx, s->vsy, s->vsz};
   for (int a = 0; a < (d3 ? 3 : 1); a++) {
     if (hv[a])
-      CK(cudaMemcpyAsync(vs[a] + off, hv[a], 8 * n, kind, st));
+      job(vs[a] + off, hv[a], 8 * n);
     else
       CK(cudaMemsetAsync(vs[a] + off, 0, 8 * n, st));
   }
-  CK(cudaMemcpyAsync(A.phase + off, s->phase, n, kind, st));
-  CK(cudaMemcpyAsync(A.bc + off, s->bc_type, n, kind, st));
-  CK(cudaMemcpyAsync(A.inv + off, s->involved, n, kind, st));
+  job(A.phase + off, s->phase, n);
+  job(A.bc + off, s->bc_type, n);
+  job(A.inv + off, s->involved, n);
   if (member)
-    CK(cudaMemcpyAsync(A.mem + off, member, 2 * n, kind, st));
+    job(A.mem + off, member, 2 * n);
   else
     CK(cudaMemsetAsync(A.mem + off, 0, 2 * n, st));
-  return PLUME_OK;
+  return run_copies(ctx, jobs, kind);
 }
 
 static int set_count(plume_ctx* ctx, size_t n) {
@@ -1875,10 +1953,11 @@ int plume_download(plume_ctx* ctx, PlumeSoA* host, size_t cap, size_t* n) {
   if (rc) return rc;
   Dev& A = ctx->A;
   cudaStream_t st = ctx->st;
-  auto d2h = [&](void* h, const void* d, size_t bytes) -> cudaError_t {
-    return h ? cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+  std::vector<CopyJob> jobs;
+  auto d2h = [&](void* h, const void* d, size_t bytes) {
+    if (h) jobs.push_back(CopyJob{(char*)h, (const char*)d, bytes});
   };
-  CK(d2h(host->key, A.key, 8 * nt));
+  d2h(host->key, A.key, 8 * nt);
   const double* src[] = {A.x, A.y, A.z, A.vx, A.vy, A.vz, A.vsx, A.vsy, A.vsz, A.mass, A.h, A.rho, A.e,
                          A.p, A.Y, A.gam, A.c, A.T, A.cp};
   double* dst[] = {host->x, host->y, host->z, host->vx, host->vy, host->vz, host->vsx, host->vsy,
@@ -1891,11 +1970,13 @@ int plume_download(plume_ctx* ctx, PlumeSoA* host, size_t cap, size_t* n) {
       if (dst[f]) memset(dst[f], 0, 8 * nt);
       continue;
     }
-    CK(d2h(dst[f], src[f], 8 * nt));
+    d2h(dst[f], src[f], 8 * nt);
   }
-  CK(d2h(host->phase, A.phase, nt));
-  CK(d2h(host->bc_type, A.bc, nt));
-  CK(d2h(host->involved, A.inv, nt));
+  d2h(host->phase, A.phase, nt);
+  d2h(host->bc_type, A.bc, nt);
+  d2h(host->involved, A.inv, nt);
+  rc = run_copies(ctx, jobs, cudaMemcpyDeviceToHost);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(st));
   return PLUME_OK;
 }
