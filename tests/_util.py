@@ -42,6 +42,8 @@ def gsph_case(name):
     """the cases of the GSPH fixtures (tests/golden/make_golden.py)"""
     if name == "gsph_1d_sod":
         c = cases.sod_1d(n_real=200, method=cases.METHOD_GSPH)
+    elif name == "gsph_1d_2000_end":
+        c = cases.sod_1d(n_real=2000, method=cases.METHOD_GSPH)
     elif name == "gsph_1d_grad":
         c = cases.sod_1d(n_real=200, ghosts=0, eta=2.0, method=cases.METHOD_GSPH)
         c.options.gsph_recon = cases.RECON_EACH

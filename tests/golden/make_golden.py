@@ -141,7 +141,18 @@ def main():
     make(c, "ref3d_plume", 3, os.path.join(HERE, "plume_3d_small.npz"))
     make_bc()
     make_gsph()
+    make_gsph_end()
     make_adapt()
+
+
+def make_gsph_end():
+    """gsph_1d_2000_end.npz: the 1D Sod workload (2,000 reals) with GSPH
+    (HLLC, zeroth-order states) to t = 0.2, final state only, plus the
+    reference's one-ulp sensitivity run"""
+    sod = cases.sod_1d(n_real=2000, method=cases.METHOD_GSPH)
+    wall = int(sod.particles.key[sod.particles.need_neigh()][0])
+    make(sod, "ref1d_gsph", -1, os.path.join(HERE, "gsph_1d_2000_end.npz"),
+         sample_lists=4, dump_last=True, perturb_key=wall)
 
 
 def make_gsph():
@@ -193,5 +204,8 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--gsph-end":
+        refio.build_ref()
+        make_gsph_end()
     else:
         main()

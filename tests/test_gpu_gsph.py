@@ -124,3 +124,81 @@ def test_gsph_gradients_absent_without_request():
     s.steps(1)
     with pytest.raises(RuntimeError):
         s.gsph_gradients()
+
+
+@pytest.mark.parametrize("precision", [0, PREC_MIXED])
+def test_gsph_ensemble_members_equal_single_runs(precision):
+    """GSPH members stepped together compute what they compute alone, bit
+    for bit (1D Riemann members with HLLC, and 3D plumes with the 3D
+    switches, gradients every step)"""
+    from plume_gpu import Ensemble, PlumeError
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, METHOD_GSPH
+
+    def same(a, b, label):
+        a, b = a.sorted_by_key(), b.sorted_by_key()
+        assert a.n == b.n, label
+        for f in DOUBLE_FIELDS + BYTE_FIELDS:
+            np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f"{label}: {f}")
+
+    cs = cases.riemann_ensemble(4, seed=7, n_lo=150, n_hi=400, precision=precision)
+    for c in cs:
+        c.options.method = METHOD_GSPH
+    ens = Ensemble(cs)
+    ens.adaptive_sml()
+    ens.steps(15)
+    parts = ens.split()
+    _, _, run, status = ens.member_times()
+    n_ok = 0
+    for k, c in enumerate(cs):
+        s = Solver(c)
+        s.adaptive_sml()
+        try:
+            s.steps(15)
+        except PlumeError as e:
+            assert status[k] == e.status and not run[k]
+            continue
+        same(parts[k], s.download(), f"1D member {k}")
+        n_ok += 1
+    assert n_ok >= 2
+    ps = cases.plume_ensemble(2, seed=4, dx=50.0, n_lo=2000, n_hi=6000, duct_depth=300.0, precision=precision)
+    for c in ps:
+        c.options.method = METHOD_GSPH
+        c.options.gsph_gradients = 1
+        c.step0 = 49
+    ens = Ensemble(ps)
+    ens.set_time(0.0, 49, 0, ps[0].options.timeoutput)
+    ens.steps(2)
+    parts = ens.split()
+    for k, c in enumerate(ps):
+        solo = Solver(c)
+        solo.steps(2)
+        same(parts[k], solo.download(), f"3D member {k}")
+
+
+def test_gsph_sod_2000_full_run_matches_reference():
+    """The 1D Sod workload (2,000 reals) with GSPH to t = 0.2 against the
+    reference's GSPH build, within 3x the reference's own one-ulp
+    sensitivity floor (relative L1 over the real particles, equal time)"""
+    case, d = golden_case("gsph_1d_2000_end")
+    s = Solver(case)
+    s.adaptive_sml()
+    t, step, _ = s.time()
+    while t < case.options.max_time - 0.02:
+        s.steps(100)
+        t, step, _ = s.time()
+    while not (t >= case.options.max_time):
+        s.steps(1)
+        t, step, _ = s.time()
+    assert t == float(d["time"][-1])
+    assert abs(step - int(d["step"][-1])) <= 20
+    g = s.download().sorted_by_key()
+    ref = unpack(d, "out_")
+    ulp = unpack(d, "ulp_")
+    real = ref.bc_type >= 99
+    assert np.array_equal(g.key, ref.key)
+    for f in ("rho", "vx", "p", "e"):
+        r, u, x = getattr(ref, f)[real], getattr(ulp, f)[real], getattr(g, f)[real]
+        floor = np.abs(u - r).sum() / np.abs(r).sum()
+        err = np.abs(x - r).sum() / np.abs(r).sum()
+        print(f"GSPH sod t=0.2 {f}: L1 gpu-ref {err:.3e}, reference one-ulp floor {floor:.3e}")
+        assert err <= 3.0 * floor + 1e-12, (f, err, floor)

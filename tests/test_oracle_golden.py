@@ -222,3 +222,17 @@ def test_oracle_domain_growth_matches_reference():
     # the converted buckets stopped absorbing
     conv = (d["binv_in"] == 0) & (d["binv_out"] == 1)
     assert not np.any(c.grid.flags[conv] & cases.BUCKET_ABSORBING)
+
+
+def test_oracle_gsph_sod_2000_full_run_bit_exact():
+    """The 1D Sod workload (2,000 particles) with GSPH (HLLC) to t = 0.2:
+    2,173 steps, final state identical to the reference's GSPH build"""
+    case, d = golden_case("gsph_1d_2000_end")
+    case.options.gsph_gradients = 0  # zeroth-order states read no gradients
+    o = OracleRun(case)
+    o.adaptive()
+    o.steps(int(d["nsteps"]))
+    assert o.t.step == int(d["step"][-1])
+    assert o.t.time == float(d["time"][-1])
+    err = field_errors(o.ps, unpack(d, "out_"))
+    assert max(err.values()) == 0.0, err
