@@ -923,6 +923,12 @@ struct plume_ctx {
   double* img_xyz = nullptr;
   int nimg = 0;
   int* bc_map = nullptr;  // row of (member, image), -1 when absent
+  // tile order of the list sweeps (single 3D runs with lists)
+  int ntiles = 0;
+  unsigned int* tcount = nullptr;
+  unsigned long long *toffs = nullptr, *tsums = nullptr, *ttot = nullptr;
+  uint32_t* real_tile = nullptr;
+  int* d_real_tile = nullptr;
   // domain growth: involvement state per bucket, the scan's count per
   // member, buckets converted by the last adapt_domain
   uint8_t* binv = nullptr;
@@ -1128,20 +1134,40 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   const bool mixed = sizeof(T) == 4;
   const bool gsph = ctx->o.method == PLUME_METHOD_GSPH;
   const bool lists = (D == 3) && ctx->use_lists;
+  // order of the list sweeps: tile by tile for single runs
+  const bool tiled = !MULTI && ctx->ntiles;
+  const uint32_t* sweep_idx = tiled ? ctx->real_tile : ctx->real_idx;
+  const int* sweep_cnt = tiled ? ctx->d_real_tile : ctx->d_real;
   if constexpr (D == 3) {
     if (lists) {
       const int ns = n ? n : 1, nsb = (ns + 1023) / 1024;
+      // the list build walks the need_neigh particles in sorted order; the
+      // sweeps of a single run walk them tile by tile
       k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->ts, ctx->rflag);
       k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, ns, ctx->roffs, ctx->rsums);
       k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
       k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, ns, ctx->rsums);
       k_real_scatter<<<nb, NTHREADS, 0, st>>>(ctx->rflag, ctx->roffs, ns, ctx->real_idx, ctx->d_real, ctx->rtot);
       ctx->launches += 5;
+      if (tiled) {
+        const Geo& g0 = ctx->hgeo[0];
+        const int ntx = (g0.G[0] + TILE_X - 1) / TILE_X, nty = (g0.G[1] + TILE_Y - 1) / TILE_Y;
+        const int nt = ctx->ntiles, ntb = (nt + 1023) / 1024;
+        k_tile_count<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
+                                                       ctx->tcount);
+        k_scan_blocks<<<ntb, 1024, 0, st>>>(ctx->tcount, nt, ctx->toffs, ctx->tsums);
+        k_scan_sums<<<1, 1024, 0, st>>>(ctx->tsums, ntb, ctx->ttot);
+        k_scan_add<<<ntb, 1024, 0, st>>>(ctx->toffs, nt, ctx->tsums);
+        k_tile_fill<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
+                                                      ctx->toffs, ctx->ttot, ctx->real_tile, ctx->d_real_tile);
+        ctx->launches += 5;
+      }
       if (mixed) {
         k_pack_pos<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
         ctx->launches++;
       }
-      k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts, ctx->L);
+      k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
+                                                       ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
       ctx->launches++;
       if (rec) {
         dcopy(rec->L.e, ctx->L.e, sizeof(uint2) * (size_t)LCAP * n, st);
@@ -1163,7 +1189,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
     if (gsph)
       launch_gsph<D, T>(ctx, nb);
     else if (lists)
-      k_sweep3_list<T, WMom, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      k_sweep3_list<T, WMom, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
     else if (ctx->sweep_warp)
       k_sweep3<T, WMom, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
@@ -1191,7 +1217,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       ctx->launches++;
     }
     if (lists)
-      k_sweep3_list<T, WDens, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      k_sweep3_list<T, WDens, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
     else if (ctx->sweep_warp)
       k_sweep3<T, WDens, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
@@ -1214,7 +1240,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         ctx->launches++;
       }
       if (lists)
-        k_sweep3_list<T, WVel, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+        k_sweep3_list<T, WVel, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
       else if (ctx->sweep_warp)
         k_sweep3<T, WVel, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
       else
@@ -1511,6 +1537,22 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
           (rc = dev_alloc(ctx, (void**)&ctx->real_idx, 4 * c)) ||
           (rc = dev_alloc(ctx, (void**)&ctx->d_real, sizeof(int))))
         return fail(rc);
+      const char* tl = getenv("PLUME_TILES");
+      if (nmem == 1 && !(tl && !strcmp(tl, "0"))) {
+        const Geo& g0 = ctx->hgeo[0];
+        const long long nt = (long long)((g0.G[0] + TILE_X - 1) / TILE_X) * ((g0.G[1] + TILE_Y - 1) / TILE_Y) *
+                             ((g0.G[2] + TILE_Z - 1) / TILE_Z);
+        if (nt > 0 && nt < (1ll << 30)) {
+          ctx->ntiles = (int)nt;
+          if ((rc = dev_alloc(ctx, (void**)&ctx->tcount, 4 * (size_t)nt)) ||
+              (rc = dev_alloc(ctx, (void**)&ctx->toffs, 8 * (size_t)nt)) ||
+              (rc = dev_alloc(ctx, (void**)&ctx->tsums, 8 * ((size_t)nt / 1024 + 2))) ||
+              (rc = dev_alloc(ctx, (void**)&ctx->ttot, 8)) ||
+              (rc = dev_alloc(ctx, (void**)&ctx->real_tile, 4 * c)) ||
+              (rc = dev_alloc(ctx, (void**)&ctx->d_real_tile, sizeof(int))))
+            return fail(rc);
+        }
+      }
     }
     if (opt->method == PLUME_METHOD_GSPH &&
         (rc = dev_alloc(ctx, (void**)&ctx->grad, 8 * c * (size_t)((opt->dim + 2) * opt->dim))))

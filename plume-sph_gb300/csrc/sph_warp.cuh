@@ -725,18 +725,18 @@ __device__ __forceinline__ void decode_offsets(T delT, int code, bool& own, T& o
 
 // union filter of the momentum, density and velocity sweeps
 template <typename T, bool MULTI>
+// (over the compacted need_neigh particles of the stepping members: only
+// their lists are read)
 __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
                                                      const uint32_t* __restrict__ cs_all,
                                                      const double* __restrict__ hmax_all,
-                                                     const int* __restrict__ d_count,
+                                                     const int* __restrict__ d_real,
+                                                     const uint32_t* __restrict__ real_idx,
                                                      const TimeState* __restrict__ ts_all, NList L) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *d_count) return;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *d_real) return;
+  const int i = (int)real_idx[r];
   const int m = geo.member(A, i);
-  if (!need_neigh(A.bc[i]) || !ts_all[m].active) {
-    L.cnt[i] = 0;
-    return;
-  }
   const Geo& g = geo.of(m);
   const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
   const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
@@ -902,6 +902,59 @@ __global__ void k_real_scatter(const unsigned int* __restrict__ flag, const unsi
   if (i == 0) *d_real = (int)*total;
   if (i >= n) return;
   if (flag[i]) real_idx[offs[i]] = (uint32_t)i;
+}
+
+// Processing order of the list build and the list sweeps for single runs:
+// tiles of TILE_X x TILE_Y x TILE_Z fine cells (x fastest), the
+// need_neigh particles of a tile consecutive.  The per-particle work does
+// not depend on the order; a block of threads then draws its particles
+// from a compact 3D region instead of a line of cells, so the candidate
+// records the block's warps load overlap more in L1.
+constexpr int TILE_X = 4, TILE_Y = 4, TILE_Z = 2;
+__device__ __forceinline__ void tile_rows(const Geo& g, int t, int ntx, int nty, int& cx0, int& cx1, int& cy0,
+                                          int& cy1, int& cz0, int& cz1) {
+  const int tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
+  cx0 = tx * TILE_X; cx1 = min(cx0 + TILE_X, g.G[0]);
+  cy0 = ty * TILE_Y; cy1 = min(cy0 + TILE_Y, g.G[1]);
+  cz0 = tz * TILE_Z; cz1 = min(cz0 + TILE_Z, g.G[2]);
+}
+__global__ void k_tile_count(Geo g, Dev A, const uint32_t* __restrict__ cs, const int* __restrict__ d_count,
+                             const TimeState* __restrict__ ts, int ntx, int nty, int ntiles,
+                             unsigned int* __restrict__ tcount) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  unsigned int c = 0;
+  if (ts[0].active) {
+    const uint32_t n = (uint32_t)*d_count;
+    int cx0, cx1, cy0, cy1, cz0, cz1;
+    tile_rows(g, t, ntx, nty, cx0, cx1, cy0, cy1, cz0, cz1);
+    for (int cz = cz0; cz < cz1; cz++)
+      for (int cy = cy0; cy < cy1; cy++) {
+        const size_t row = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+        const uint32_t j1 = min(cs[row + cx1], n);
+        for (uint32_t j = cs[row + cx0]; j < j1; j++) c += need_neigh(A.bc[j]) ? 1u : 0u;
+      }
+  }
+  tcount[t] = c;
+}
+__global__ void k_tile_fill(Geo g, Dev A, const uint32_t* __restrict__ cs, const int* __restrict__ d_count,
+                            const TimeState* __restrict__ ts, int ntx, int nty, int ntiles,
+                            const unsigned long long* __restrict__ toffs, const unsigned long long* __restrict__ total,
+                            uint32_t* __restrict__ real_idx, int* __restrict__ d_real) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) *d_real = (int)*total;
+  if (t >= ntiles || !ts[0].active) return;
+  const uint32_t n = (uint32_t)*d_count;
+  unsigned long long o = toffs[t];
+  int cx0, cx1, cy0, cy1, cz0, cz1;
+  tile_rows(g, t, ntx, nty, cx0, cx1, cy0, cy1, cz0, cz1);
+  for (int cz = cz0; cz < cz1; cz++)
+    for (int cy = cy0; cy < cy1; cy++) {
+      const size_t row = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      const uint32_t j1 = min(cs[row + cx1], n);
+      for (uint32_t j = cs[row + cx0]; j < j1; j++)
+        if (need_neigh(A.bc[j])) real_idx[o++] = j;
+    }
 }
 
 // position records for the list build: P (xr, yr, zr, h)
