@@ -750,6 +750,9 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
   const T supp = T(o.cutoff2) * hi;
   const T Lb = T(o.list_factor * W.hlist[i]);
   const T kmarg = T(o.ksupport * (1.0 + 1e-6));
+  // support term of the mixed test: kmarg2 max(h_i/2 + |h_j|/2, h_i)
+  const float kmarg2 = (float)(o.ksupport * (1.0 + 4e-6));
+  const float kA = kmarg2 * 0.5f * (float)hi, kB = kmarg2 * 0.5f, kC = kmarg2 * (float)hi;
   const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
   uint2* out = L.e + (size_t)i * LCAP;
   const T delT = T(g.del);
@@ -760,6 +763,10 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
     T ox, oy, oz;
     decode_offsets<T>(delT, code, own, ox, oy, oz);
     const T xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
+    // mixed: one threshold per candidate, min(list and CUTOFF2 boxes,
+    // support box) -- the first exactly as the sweeps assume, the support
+    // term (which the sweeps test again) with a wider margin
+    const float Ti = own ? (float)supp : fminf((float)Lb, (float)supp);
     for (uint32_t wb = j0; wb < j1; wb += 32) {
       const int nb = (int)min(32u, j1 - wb);
       uint32_t mask = 0;
@@ -774,9 +781,8 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
           for (int u = 0; u < 4; u++) {
             const float dx0 = fabsf(xsh[0] - pr[u].x), dx1 = fabsf(xsh[1] - pr[u].y), dx2 = fabsf(xsh[2] - pr[u].z);
             const float m = fmaxf(dx0, fmaxf(dx1, dx2));
-            const float hs = fmaxf(0.5f * (hi + fabsf(pr[u].w)), hi);
-            const bool pass = (own || m <= Lb) && (m <= supp) && (m <= kmarg * hs);
-            mask |= (uint32_t)pass << (q + u);
+            const float thr = fminf(Ti, fmaxf(fmaf(kB, fabsf(pr[u].w), kA), kC));
+            mask |= (uint32_t)(m <= thr) << (q + u);
           }
         }
         mask &= (nb == 32) ? 0xffffffffu : ((1u << nb) - 1u);
