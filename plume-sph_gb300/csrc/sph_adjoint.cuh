@@ -123,6 +123,7 @@ struct AdjIn {
 // formed again for the adjoint of dt.
 struct VMom {
   WMom<double> f;
+  __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
   double dt;
@@ -365,6 +366,7 @@ struct VMom {
 // W(dx, h_ij/4) / sum (m_j/rho_j) W(dx, h_ij/4).
 struct VDens {
   WDens<double> f;
+  __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
   double r1b, r2b, wnb, enb;
@@ -441,6 +443,7 @@ struct VDens {
 // v_i) / sum w_j, w_j = (m_j / rho_j) W(dx, h_i).
 struct VVel {
   WVel<double> f;
+  __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
   double ob[3], dvb[3], wnb, vib[3];

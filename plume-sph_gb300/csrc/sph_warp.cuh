@@ -166,6 +166,7 @@ struct WMom {
   bool lans;
   uint32_t i;
   T xs[3], hi, supp, Lb, rhoi, Vi, pvsqi, ci, tempi, Cp_i, veli[3];
+  __device__ __forceinline__ const T* xpos() const { return xs; }
   T ks_half, ata, alpha, beta;  // option constants in the sweep's type
   Acc<T> rv[3], re;
   __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
@@ -229,9 +230,10 @@ struct WMom {
     if (j == i) return false;
     T xj[3];
     JPos<T>::get(A, K, j, xj, hj);
-    dx[0] = (xs[0] + ox) - xj[0];
-    dx[1] = (xs[1] + oy) - xj[1];
-    dx[2] = (xs[2] + oz) - xj[2];
+    // listed: ox, oy, oz are i's position shifted into j's bucket
+    dx[0] = (LISTED ? ox : xs[0] + ox) - xj[0];
+    dx[1] = (LISTED ? oy : xs[1] + oy) - xj[1];
+    dx[2] = (LISTED ? oz : xs[2] + oz) - xj[2];
     if (!LISTED) {
       if (!own && !in_box<3, T>(dx, Lb)) return false;
       if (!in_box<3, T>(dx, supp)) return false;
@@ -376,6 +378,7 @@ struct WDens {
   const Opt& o;
   int pgc;
   T xs[3], hi, supp, Lb, ks_half;
+  __device__ __forceinline__ const T* xpos() const { return xs; }
   Acc<T> rho1, rho2, wnorm_e, engr;
   bool esm;
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
@@ -431,9 +434,10 @@ struct WDens {
     } else if (hj < T(0)) {
       return false;
     }
-    dx[0] = (xs[0] + ox) - xj[0];
-    dx[1] = (xs[1] + oy) - xj[1];
-    dx[2] = (xs[2] + oz) - xj[2];
+    // listed: ox, oy, oz are i's position shifted into j's bucket
+    dx[0] = (LISTED ? ox : xs[0] + ox) - xj[0];
+    dx[1] = (LISTED ? oy : xs[1] + oy) - xj[1];
+    dx[2] = (LISTED ? oz : xs[2] + oz) - xj[2];
     if (!LISTED) {
       if (!own && !in_box<3, T>(dx, Lb)) return false;
       if (!in_box<3, T>(dx, supp)) return false;
@@ -521,6 +525,7 @@ struct WVel {
   const Packed& K;
   const Opt& o;
   T xs[3], hi, supp, ks, Lb, vi[3];
+  __device__ __forceinline__ const T* xpos() const { return xs; }
   T ihi, r3;  // 1/h_i and (1/(sqrt(pi) h_i))^3 (mixed Gaussian)
   Acc<T> dv[3], wnorm;
   __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
@@ -568,9 +573,10 @@ struct WVel {
     } else if (flag < T(0)) {
       return false;
     }
-    dx[0] = (xs[0] + ox) - xj[0];
-    dx[1] = (xs[1] + oy) - xj[1];
-    dx[2] = (xs[2] + oz) - xj[2];
+    // listed: ox, oy, oz are i's position shifted into j's bucket
+    dx[0] = (LISTED ? ox : xs[0] + ox) - xj[0];
+    dx[1] = (LISTED ? oy : xs[1] + oy) - xj[1];
+    dx[2] = (LISTED ? oz : xs[2] + oz) - xj[2];
     if (!LISTED) {
       if (!own && !in_box<3, T>(dx, Lb)) return false;
       if (!in_box<3, T>(dx, supp)) return false;
@@ -830,13 +836,16 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     uint32_t mask = en.y;
     bool own;
     T ox, oy, oz;
+    // listed entries get i's position shifted into the window's bucket
     decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
+    ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
     while (true) {
       if (mask == 0) {  // stored windows are never empty: one step suffices
         if (++q >= c) break;
         en = ent[q];
         mask = en.y;
         decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
+        ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
       }
       const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
       mask &= mask - 1;
