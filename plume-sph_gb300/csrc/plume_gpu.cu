@@ -904,7 +904,8 @@ struct plume_ctx {
   RadixSorter sorter;
   std::vector<void*> allocs;
   int host_step = 0;
-  bool pending_dead = false;
+  bool pending_dead = false;  // row order unknown: search before row-order reads
+  bool has_dead = false;      // rows deleted by the last steps are still in the table
   std::string err;
   // per-step event sets (NEV events each) for the phase times of a call
   std::vector<cudaEvent_t> evs;
@@ -1079,6 +1080,7 @@ static int search(plume_ctx* ctx) {
   k_cell_start<<<nblocks((size_t)ctx->ncells + 2, 256), 256, 0, st>>>(ctx->keys, n, ctx->ncells, ctx->cs, ctx->d_count);
   ctx->launches += 2;
   ctx->pending_dead = false;
+  ctx->has_dead = false;
   if (ctx->rec) snap_search(ctx);
   if (ctx->inlet_reserve) {
     // rows the inlet may fill this step: dead until it does
@@ -1322,6 +1324,7 @@ static int step_async(plume_ctx* ctx) {
   k_end_step<<<mb, NTHREADS, 0, st>>>(ctx->d_opt, ctx->ts, ctx->nmem);
   ctx->launches += 2;
   ctx->pending_dead = true;
+  ctx->has_dead = true;
   if (ctx->rec) {
     dcopy(ctx->rec->bc3, ctx->A.bc, (size_t)n, st);
     dcopy(ctx->rec->ts, ctx->ts, sizeof(TimeState), st);
@@ -1959,10 +1962,49 @@ int plume_adapt_sml(plume_ctx* ctx) {
   return ctx_sync_status(ctx);
 }
 
+// live rows (not deleted) of [0, count)
+__global__ void k_live_flags(Dev A, const int* __restrict__ d_count, int n, unsigned int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = (i < *d_count && A.bc[i] != BC_DEAD) ? 1u : 0u;
+}
+__global__ void k_live_scatter(const unsigned int* __restrict__ flag, const unsigned long long* __restrict__ offs,
+                               int n, uint32_t* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[i]) perm[offs[i]] = (uint32_t)i;
+}
+
+// drops the rows deleted by the last steps without re-sorting (the next
+// step sorts anyway); a search where the scan buffers are absent
+static int compact(plume_ctx* ctx) {
+  if (!ctx->rflag) return search(ctx);
+  cudaStream_t st = ctx->st;
+  const int n = (int)ctx->n_alloc;
+  if (n > 0) {
+    const int nsb = (n + 1023) / 1024;
+    k_live_flags<<<nblocks(n), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, n, ctx->rflag);
+    k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, n, ctx->roffs, ctx->rsums);
+    k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
+    k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, n, ctx->rsums);
+    k_live_scatter<<<nblocks(n), NTHREADS, 0, st>>>(ctx->rflag, ctx->roffs, n, ctx->perm);
+    unsigned long long live = 0;
+    CK(cudaMemcpyAsync(&live, ctx->rtot, sizeof(live), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (live) k_gather<<<nblocks((size_t)live), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->B, ctx->W, ctx->perm, (int)live);
+    std::swap(ctx->A, ctx->B);
+    const int nl = (int)live;
+    CK(cudaMemcpyAsync(ctx->d_count, &nl, sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    ctx->n_alloc = live;
+  }
+  ctx->has_dead = false;
+  return PLUME_OK;
+}
+
 int plume_count(plume_ctx* ctx, size_t* n_total, size_t* n_real) {
   if (!ctx) return PLUME_E_INVALID;
-  if (ctx->pending_dead) {
-    int rc = search(ctx);
+  if (ctx->has_dead) {
+    int rc = compact(ctx);
     if (rc) return rc;
     int s = ctx_sync_status(ctx);
     if (s) return s;
