@@ -906,6 +906,7 @@ struct plume_ctx {
   int host_step = 0;
   bool pending_dead = false;  // row order unknown: search before row-order reads
   bool has_dead = false;      // rows deleted by the last steps are still in the table
+  unsigned long long* d_nreal = nullptr;  // plume_count's real-particle count
   std::string err;
   // per-step event sets (NEV events each) for the phase times of a call
   std::vector<cudaEvent_t> evs;
@@ -1663,6 +1664,7 @@ int plume_destroy(plume_ctx* ctx) {
   if (ctx->img_key) cudaFree(ctx->img_key);
   if (ctx->img_xyz) cudaFree(ctx->img_xyz);
   if (ctx->bc_map) cudaFree(ctx->bc_map);
+  if (ctx->d_nreal) cudaFree(ctx->d_nreal);
   if (ctx->inlet_buf) cudaFree(ctx->inlet_buf);
   if (ctx->inlet_colcnt) cudaFree(ctx->inlet_colcnt);
   if (ctx->inlet_rowctr) cudaFree(ctx->inlet_rowctr);
@@ -1962,6 +1964,14 @@ int plume_adapt_sml(plume_ctx* ctx) {
   return ctx_sync_status(ctx);
 }
 
+// real particles (bc 100 or 99) of [0, count): one atomic per warp
+__global__ void k_count_real(Dev A, const int* __restrict__ d_count, int n, unsigned long long* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool r = i < n && i < *d_count && is_real(A.bc[i]);
+  const unsigned b = __ballot_sync(0xffffffffu, r);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
+}
+
 // live rows (not deleted) of [0, count)
 __global__ void k_live_flags(Dev A, const int* __restrict__ d_count, int n, unsigned int* __restrict__ flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2014,11 +2024,14 @@ int plume_count(plume_ctx* ctx, size_t* n_total, size_t* n_real) {
   }
   if (n_total) *n_total = ctx->n_alloc;
   if (n_real) {
-    std::vector<uint8_t> bc(ctx->n_alloc);
-    CK(cudaMemcpy(bc.data(), ctx->A.bc, ctx->n_alloc, cudaMemcpyDeviceToHost));
-    size_t r = 0;
-    for (uint8_t b : bc) r += (b == 100 || b == 99);
-    *n_real = r;
+    if (!ctx->d_nreal) CK(cudaMalloc(&ctx->d_nreal, sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(ctx->d_nreal, 0, sizeof(unsigned long long), ctx->st));
+    const int n = (int)ctx->n_alloc;
+    if (n) k_count_real<<<nblocks(n), NTHREADS, 0, ctx->st>>>(ctx->A, ctx->d_count, n, ctx->d_nreal);
+    unsigned long long r = 0;
+    CK(cudaMemcpyAsync(&r, ctx->d_nreal, sizeof(r), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *n_real = (size_t)r;
   }
   return PLUME_OK;
 }
