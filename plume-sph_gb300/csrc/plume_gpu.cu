@@ -212,11 +212,11 @@ __global__ void k_gather(const Geo* __restrict__ geo, Dev A, Dev B, Work W, cons
       bi[0] = b % g.nb[0];
       bi[1] = (b / g.nb[0]) % g.nb[1];
       bi[2] = b / (g.nb[0] * g.nb[1]);
-      W.xr[p] = (float)(A.x[q] - (g.mind[0] + bi[0] * g.del));
-      W.yr[p] = (float)(A.y[q] - (g.mind[1] + bi[1] * g.del));
-      W.zr[p] = (float)(A.z[q] - (g.mind[2] + bi[2] * g.del));
+      W.xr[p] = f32_rz(A.x[q] - (g.mind[0] + bi[0] * g.del));
+      W.yr[p] = f32_rz(A.y[q] - (g.mind[1] + bi[1] * g.del));
+      W.zr[p] = f32_rz(A.z[q] - (g.mind[2] + bi[2] * g.del));
     } else {
-      W.xr[p] = (float)(A.x[q] - (g.mind[0] + b * g.del));
+      W.xr[p] = f32_rz(A.x[q] - (g.mind[0] + b * g.del));
     }
   }
 }
@@ -426,23 +426,6 @@ __global__ void k_bc_map(Dev A, const int* __restrict__ d_count, const uint64_t*
     if (ikey[mid] < k) l = mid + 1; else h = mid;
   }
   if (l < nimg && ikey[l] == k) map[(size_t)A.mem[i] * nimg + l] = i;
-}
-
-// binary64 -> binary32 rounding toward zero on the integer pipe (the
-// exponent rebiased, the top 23 fraction bits kept): the FP64 pipe, which
-// executes F2F, is narrow on this part.  Below the binary32 normal range the
-// result is a signed zero, above it a signed infinity; NaN stays NaN.
-__device__ __forceinline__ float f32_rz(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32);
-  const unsigned sign = hi & 0x80000000u;
-  const int ex = (int)((hi >> 20) & 0x7ffu);
-  const int e = ex - 1023 + 127;
-  unsigned r = sign | ((unsigned)e << 23) | ((unsigned)(b >> 29) & 0x7fffffu);
-  if (e <= 0) r = sign;
-  if (e >= 255) r = sign | 0x7f800000u;
-  if (ex == 0x7ff && (b & 0xfffffffffffffull)) r = 0x7fc00000u;
-  return __uint_as_float(r);
 }
 
 // BCG threads per (member, image) slot, slots in image-key order, so that
@@ -1483,6 +1466,7 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
     g.cw = grid->del / s;
     g.idel = 1.0 / g.del;
     g.icw = 1.0 / g.cw;
+    g.icwf = (float)g.icw;
     g.dim = opt->dim;
     for (int a = 0; a < 3; a++) g.G[a] = (opt->dim == 3 || a == 0) ? g.nb[a] * s : 1;
     g.nbk = (opt->dim == 3) ? g.nb[0] * g.nb[1] * g.nb[2] : 1;

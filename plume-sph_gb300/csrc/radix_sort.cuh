@@ -182,8 +182,7 @@ struct RadixSorter {
     rs_iota<<<(n + 255) / 256, 256, 0, st>>>(vals, n);
     launches++;
     uint32_t *ka = keys, *va = vals, *kb = keys_alt, *vb = vals_alt;
-    int passes = (bits + 3) / 4;
-    if (passes & 1) passes++;  // even number of passes: result lands in `keys`
+    const int passes = (bits + 3) / 4;
     for (int p = 0; p < passes; p++) {
       int shift = 4 * p;
       rs_count<<<ntiles, RS_THREADS, 0, st>>>(ka, n, shift, hist, ntiles);
@@ -193,6 +192,10 @@ struct RadixSorter {
       uint32_t* t;
       t = ka; ka = kb; kb = t;
       t = va; va = vb; vb = t;
+    }
+    if (ka != keys) {  // odd pass count: the result is in the spare buffers
+      cudaMemcpyAsync(keys, ka, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(vals, va, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
     }
     return launches;
   }

@@ -48,6 +48,7 @@ struct Geo {
   double del;
   double cw;  // fine cell edge = del / s
   double idel, icw;  // 1/del, 1/cw (multiplies instead of FP64 divisions)
+  float icwf;        // 1/cw in FP32 (fine-cell index within a bucket)
   int nb[3];
   int s;
   int G[3];   // fine cells per axis = nb * s
@@ -254,12 +255,32 @@ __device__ __forceinline__ int bucket_axis(double x, double mind, double del, do
   return b;
 }
 // fine cell per axis: bucket * s + clamped sub-cell (monotone in x)
+// binary64 -> binary32 rounding toward zero on the integer pipe (the
+// exponent rebiased, the top 23 fraction bits kept): the FP64 pipe, which
+// executes F2F, is narrow on this part.  Below the binary32 normal range the
+// result is a signed zero, above it a signed infinity; NaN stays NaN.
+__device__ __forceinline__ float f32_rz(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int ex = (int)((hi >> 20) & 0x7ffu);
+  const int e = ex - 1023 + 127;
+  unsigned r = sign | ((unsigned)e << 23) | ((unsigned)(b >> 29) & 0x7fffffu);
+  if (e <= 0) r = sign;
+  if (e >= 255) r = sign | 0x7f800000u;
+  if (ex == 0x7ff && (b & 0xfffffffffffffull)) r = 0x7fc00000u;
+  return __uint_as_float(r);
+}
+
+// Fine cell of x on axis a: the bucket exactly (Bucket::contains), the cell
+// inside it from the FP32 offset (a monotone function of x, which is all the
+// cell walks need: every user of cells calls this one function)
 __device__ __forceinline__ int cell_axis(const Geo& g, int a, double x, int* bucket, bool* outside) {
   int b = bucket_axis(x, g.mind[a], g.del, g.idel, g.nb[a], outside);
   if (bucket) *bucket = b;
-  double off = x - (g.mind[a] + b * g.del);
-  double f = floor(off * g.icw);
-  int sub = (f > 0.0) ? (int)fmin(f, (double)(g.s - 1)) : 0;
+  const double off = x - (g.mind[a] + b * g.del);
+  const float f = floorf(f32_rz(off) * g.icwf);
+  int sub = (f > 0.f) ? (int)fminf(f, (float)(g.s - 1)) : 0;
   return b * g.s + sub;
 }
 

@@ -360,14 +360,15 @@ __device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& mj, float
 __global__ void k_pack_mom(Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
-  const double rho = A.rho[j], V = 1.0 / rho;
-  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], (float)A.h[j]);
-  K.Q[j] = make_float4((float)A.mass[j], (float)rho, (float)V, (float)(A.p[j] * V * V));
+  // fields narrowed on the integer pipe, V and p V^2 formed in FP32
+  const float rho = f32_rz(A.rho[j]), V = 1.0f / rho;
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], f32_rz(A.h[j]));
+  K.Q[j] = make_float4(f32_rz(A.mass[j]), rho, V, f32_rz(A.p[j]) * V * V);
   const double vx = lans ? A.vsx[j] : A.vx[j];
   const double vy = lans ? A.vsy[j] : A.vy[j];
   const double vz = lans ? A.vsz[j] : A.vz[j];
-  K.R[j] = make_float4((float)A.c[j], (float)A.T[j], (float)A.cp[j], (float)vx);
-  K.S[j] = make_float4((float)vy, (float)vz, 0.f, 0.f);
+  K.R[j] = make_float4(f32_rz(A.c[j]), f32_rz(A.T[j]), f32_rz(A.cp[j]), f32_rz(vx));
+  K.S[j] = make_float4(f32_rz(vy), f32_rz(vz), 0.f, 0.f);
 }
 
 // ------------------------------------------------------------ density
@@ -512,10 +513,10 @@ __global__ void k_pack_dens(Dev A, Packed K, Work W, int pgc, const int* __restr
   if (j >= *d_count) return;
   const uint8_t ph = A.phase[j];
   const bool c = contr_dens(A.bc[j], pgc) && (ph == 1 || ph == 2);
-  const float h = (float)A.h[j];
-  const double m = A.mass[j], mr = m / A.rho[j];
+  const float h = f32_rz(A.h[j]);
+  const float m = f32_rz(A.mass[j]), mr = m / f32_rz(A.rho[j]);
   K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], c ? h : -h);
-  K.Q[j] = make_float4((float)m, (float)mr, (float)(mr * A.e[j]), (float)ph);
+  K.Q[j] = make_float4(m, mr, mr * f32_rz(A.e[j]), (float)ph);
 }
 
 // ------------------------------------------------------------ velocity
@@ -617,7 +618,7 @@ __global__ void k_pack_vel(Dev A, Packed K, Work W, const int* __restrict__ d_co
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
   K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], contr_vel_smooth(A.bc[j]) ? 1.f : -1.f);
-  K.Q[j] = make_float4((float)(A.mass[j] / A.rho[j]), (float)A.vx[j], (float)A.vy[j], (float)A.vz[j]);
+  K.Q[j] = make_float4(f32_rz(A.mass[j]) / f32_rz(A.rho[j]), f32_rz(A.vx[j]), f32_rz(A.vy[j]), f32_rz(A.vz[j]));
 }
 
 
@@ -976,7 +977,7 @@ __global__ void k_tile_fill(Geo g, Dev A, const uint32_t* __restrict__ cs, const
 __global__ void k_pack_pos(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
-  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], (float)A.h[j]);
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], f32_rz(A.h[j]));
 }
 
 }  // namespace plume
