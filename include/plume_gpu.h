@@ -279,6 +279,22 @@ int plume_set_time(plume_ctx *ctx, double time, int step, int ioutput,
 int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
                          uint64_t *key_j, size_t cap, size_t *n);
 
+/* ---- output snapshots ---------------------------------------------------
+ * The fields that write_h5part writes (h5part_writer.cc:41-275: x, y, z,
+ * vx, vy, vz, rho, e, Y, p, phase, bc_type; plus key, mass and h) of the
+ * current particles, staged on the device and copied to the caller's host
+ * arrays on a side stream while the caller keeps stepping.
+ * plume_snapshot_begin: host needs key, x, vx, rho, e, Y, p, mass, h,
+ *   phase, bc_type (and y, z, vy, vz in 3D); involved is filled when not
+ *   NULL; other pointers are ignored.  Rows are every particle (ghosts
+ *   too, bc_type tells them apart), in the context's order.
+ *   Page-locked host arrays are filled by the device directly.  Returns
+ *   after the staging is queued; PLUME_E_CAPACITY if cap is too small.
+ * plume_snapshot_end: waits for the copy; *n rows, the time and step of the
+ *   snapshot.  One snapshot in flight per context. */
+int plume_snapshot_begin(plume_ctx *ctx, PlumeSoA *host, size_t cap);
+int plume_snapshot_end(plume_ctx *ctx, size_t *n, double *time, int *step);
+
 /* Gradients of the last GSPH step (calc_gradients, calculate_gradient.cc:
  * 22-208: the renormalised SPH gradient of rho, the D velocity components
  * and p of every particle over its neighbour list, zero when the list holds

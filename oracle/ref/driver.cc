@@ -521,6 +521,13 @@ int main(int argc, char **argv) {
       ndumped++;
     }
   }
+#if CODE_DIMENSION == 1 && defined(PLUME_WRITE_CSV)
+  // the shock-tube text output of the final state (main.cc:749): appends
+  // to pvplot_out.csv in the working directory.  The table iterates in
+  // ascending key order here (every key hashes to slot 0), which is the
+  // case's row order.
+  write_csv(0, 1, P, tp);
+#endif
 #if CODE_DIMENSION == 3 && defined(PLUME_ADJUST_DOMAIN)
   // domain growth after the last step (main.cc:433-436, 257-265): the scan,
   // then adapt_domain when it asks for it; the particles after it are an

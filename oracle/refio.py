@@ -110,5 +110,5 @@ def run_ref(variant, case, nsteps, workdir, dump_last=False, images=None, binv=N
     cout = os.path.join(workdir, f"{case.name}.out")
     write_case(cin, case, nsteps, dump_last, images, binv, adapt)
     exe = os.path.join(HERE, "_ref", variant, "driver")
-    subprocess.run([exe, cin, cout], check=True)
+    subprocess.run([exe, cin, cout], check=True, cwd=workdir)
     return read_result(cout)

@@ -890,6 +890,13 @@ struct plume_ctx {
   bool pending_dead = false;  // row order unknown: search before row-order reads
   bool has_dead = false;      // rows deleted by the last steps are still in the table
   unsigned long long* d_nreal = nullptr;  // plume_count's real-particle count
+  // output snapshot: staging arrays (lazily sized), side stream, events
+  Dev snap{};
+  size_t snap_cap = 0, snap_n = 0;
+  cudaStream_t snap_st = nullptr;
+  cudaEvent_t snap_staged = nullptr, snap_done = nullptr;
+  bool snap_busy = false;
+  TimeState* snap_ts = nullptr;  // pinned: time and step at the snapshot
   std::string err;
   // per-step event sets (NEV events each) for the phase times of a call
   std::vector<cudaEvent_t> evs;
@@ -1649,6 +1656,17 @@ int plume_destroy(plume_ctx* ctx) {
   if (ctx->img_xyz) cudaFree(ctx->img_xyz);
   if (ctx->bc_map) cudaFree(ctx->bc_map);
   if (ctx->d_nreal) cudaFree(ctx->d_nreal);
+  if (ctx->snap_st) cudaStreamSynchronize(ctx->snap_st);
+  if (ctx->snap_cap) {
+    void* sp[] = {ctx->snap.key, ctx->snap.x, ctx->snap.y, ctx->snap.z, ctx->snap.vx, ctx->snap.vy, ctx->snap.vz,
+                  ctx->snap.mass, ctx->snap.h, ctx->snap.rho, ctx->snap.e, ctx->snap.p, ctx->snap.Y,
+                  ctx->snap.phase, ctx->snap.bc, ctx->snap.inv};
+    for (void* q : sp) if (q) cudaFree(q);
+  }
+  if (ctx->snap_staged) cudaEventDestroy(ctx->snap_staged);
+  if (ctx->snap_done) cudaEventDestroy(ctx->snap_done);
+  if (ctx->snap_st) cudaStreamDestroy(ctx->snap_st);
+  if (ctx->snap_ts) cudaFreeHost(ctx->snap_ts);
   if (ctx->inlet_buf) cudaFree(ctx->inlet_buf);
   if (ctx->inlet_colcnt) cudaFree(ctx->inlet_colcnt);
   if (ctx->inlet_rowctr) cudaFree(ctx->inlet_rowctr);
@@ -2628,6 +2646,131 @@ int plume_adjoint_backward(plume_ctx* ctx, const PlumeSoA* final_bar, size_t n_f
   int rc = restore_ckpt(ctx, ctx->ckpts.back());
   if (rc) return rc;
   return finish_steps(ctx);
+}
+
+// ---------------------------------------------------------------- snapshots
+int plume_snapshot_begin(plume_ctx* ctx, PlumeSoA* host, size_t cap) {
+  if (!ctx || !host) return PLUME_E_INVALID;
+  const bool d3 = ctx->o.dim == 3;
+  if (!host->key || !host->x || !host->vx || !host->rho || !host->e || !host->Y || !host->p || !host->mass ||
+      !host->h || !host->phase || !host->bc_type || (d3 && (!host->y || !host->z || !host->vy || !host->vz))) {
+    ctx->err = "snapshot: missing host array";
+    return PLUME_E_INVALID;
+  }
+  if (ctx->nmem != 1) {
+    ctx->err = "snapshot: single-run contexts only";
+    return PLUME_E_INVALID;
+  }
+  if (ctx->snap_busy) {
+    ctx->err = "snapshot: one in flight (plume_snapshot_end first)";
+    return PLUME_E_INVALID;
+  }
+  size_t nt = 0;
+  int rc = plume_count(ctx, &nt, nullptr);  // drops deleted rows
+  if (rc) return rc;
+  if (nt > cap) {
+    ctx->err = "snapshot capacity too small";
+    return PLUME_E_CAPACITY;
+  }
+  if (!ctx->snap_st) {
+    CK(cudaStreamCreateWithFlags(&ctx->snap_st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->snap_staged, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->snap_done, cudaEventDisableTiming));
+    CK(cudaMallocHost(&ctx->snap_ts, sizeof(TimeState)));
+  }
+  if (ctx->snap_cap < nt) {
+    void* sp[] = {ctx->snap.key, ctx->snap.x, ctx->snap.y, ctx->snap.z, ctx->snap.vx, ctx->snap.vy, ctx->snap.vz,
+                  ctx->snap.mass, ctx->snap.h, ctx->snap.rho, ctx->snap.e, ctx->snap.p, ctx->snap.Y,
+                  ctx->snap.phase, ctx->snap.bc, ctx->snap.inv};
+    for (void* q : sp) if (q) cudaFree(q);
+    ctx->snap = Dev{};
+    const size_t c = std::max(nt, (size_t)1);
+    double** dd[] = {&ctx->snap.x, &ctx->snap.y, &ctx->snap.z, &ctx->snap.vx, &ctx->snap.vy, &ctx->snap.vz,
+                     &ctx->snap.mass, &ctx->snap.h, &ctx->snap.rho, &ctx->snap.e, &ctx->snap.p, &ctx->snap.Y};
+    CK(cudaMalloc(&ctx->snap.key, 8 * c));
+    for (double** q : dd) CK(cudaMalloc(q, 8 * c));
+    CK(cudaMalloc(&ctx->snap.phase, c));
+    CK(cudaMalloc(&ctx->snap.bc, c));
+    CK(cudaMalloc(&ctx->snap.inv, c));
+    ctx->snap_cap = c;
+  }
+  // stage on the main stream (later steps overwrite the table in place)
+  cudaStream_t st = ctx->st;
+  Dev& A = ctx->A;
+  Dev& S = ctx->snap;
+  std::vector<CopyJob> stage = {
+      {(char*)S.key, (const char*)A.key, 8 * nt},   {(char*)S.x, (const char*)A.x, 8 * nt},
+      {(char*)S.vx, (const char*)A.vx, 8 * nt},     {(char*)S.mass, (const char*)A.mass, 8 * nt},
+      {(char*)S.h, (const char*)A.h, 8 * nt},       {(char*)S.rho, (const char*)A.rho, 8 * nt},
+      {(char*)S.e, (const char*)A.e, 8 * nt},       {(char*)S.p, (const char*)A.p, 8 * nt},
+      {(char*)S.Y, (const char*)A.Y, 8 * nt},       {(char*)S.phase, (const char*)A.phase, nt},
+      {(char*)S.bc, (const char*)A.bc, nt},         {(char*)S.inv, (const char*)A.inv, nt}};
+  if (d3) {
+    stage.push_back({(char*)S.y, (const char*)A.y, 8 * nt});
+    stage.push_back({(char*)S.z, (const char*)A.z, 8 * nt});
+    stage.push_back({(char*)S.vy, (const char*)A.vy, 8 * nt});
+    stage.push_back({(char*)S.vz, (const char*)A.vz, 8 * nt});
+  }
+  if (nt) {
+    CopyJobs J{};
+    for (const CopyJob& c : stage) J.j[J.n++] = c;
+    k_copy_multi<<<dim3(2 * 152, J.n), 256, 0, st>>>(J);
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(ctx->snap_ts, ctx->ts, sizeof(TimeState), cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(ctx->snap_staged, st));
+  // then to the host on the side stream
+  CK(cudaStreamWaitEvent(ctx->snap_st, ctx->snap_staged, 0));
+  std::vector<CopyJob> out = {
+      {(char*)host->key, (const char*)S.key, 8 * nt},   {(char*)host->x, (const char*)S.x, 8 * nt},
+      {(char*)host->vx, (const char*)S.vx, 8 * nt},     {(char*)host->mass, (const char*)S.mass, 8 * nt},
+      {(char*)host->h, (const char*)S.h, 8 * nt},       {(char*)host->rho, (const char*)S.rho, 8 * nt},
+      {(char*)host->e, (const char*)S.e, 8 * nt},       {(char*)host->p, (const char*)S.p, 8 * nt},
+      {(char*)host->Y, (const char*)S.Y, 8 * nt},       {(char*)host->phase, (const char*)S.phase, nt},
+      {(char*)host->bc_type, (const char*)S.bc, nt}};
+  if (host->involved) out.push_back({(char*)host->involved, (const char*)S.inv, nt});
+  if (d3) {
+    out.push_back({(char*)host->y, (const char*)S.y, 8 * nt});
+    out.push_back({(char*)host->z, (const char*)S.z, 8 * nt});
+    out.push_back({(char*)host->vy, (const char*)S.vy, 8 * nt});
+    out.push_back({(char*)host->vz, (const char*)S.vz, 8 * nt});
+  }
+  if (nt) {
+    // page-locked host arrays: one kernel writes them; else DMA per field
+    CopyJobs J{};
+    bool mapped = true;
+    for (CopyJob c : out) {
+      void* dp = mapped_host(c.dst);
+      if (!dp) { mapped = false; break; }
+      c.dst = (char*)dp;
+      J.j[J.n++] = c;
+    }
+    if (mapped) {
+      k_copy_multi<<<dim3(2 * 152, J.n), 256, 0, ctx->snap_st>>>(J);
+      CK(cudaGetLastError());
+    } else {
+      for (const CopyJob& c : out) CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, ctx->snap_st));
+    }
+  }
+  CK(cudaEventRecord(ctx->snap_done, ctx->snap_st));
+  ctx->snap_n = nt;
+  ctx->snap_busy = true;
+  return PLUME_OK;
+}
+
+int plume_snapshot_end(plume_ctx* ctx, size_t* n, double* time, int* step) {
+  if (!ctx) return PLUME_E_INVALID;
+  if (!ctx->snap_busy) {
+    ctx->err = "snapshot: none in flight";
+    return PLUME_E_INVALID;
+  }
+  CK(cudaEventSynchronize(ctx->snap_done));
+  CK(cudaEventSynchronize(ctx->snap_staged));
+  ctx->snap_busy = false;
+  if (n) *n = ctx->snap_n;
+  if (time) *time = ctx->snap_ts->time;
+  if (step) *step = ctx->snap_ts->step;
+  return PLUME_OK;
 }
 
 // ---------------------------------------------------------------- domain growth

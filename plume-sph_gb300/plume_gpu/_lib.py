@@ -95,6 +95,8 @@ def lib():
         L.plume_get_bucket_involvement.argtypes = [C.c_void_p, P(C.c_uint8), C.c_size_t]
         L.plume_scan_outside_layer.argtypes = [C.c_void_p, P(C.c_int)]
         L.plume_adapt_domain.argtypes = [C.c_void_p]
+        L.plume_snapshot_begin.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t]
+        L.plume_snapshot_end.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_double), P(C.c_int)]
         L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,
                                              P(C.c_size_t), P(C.c_double)]

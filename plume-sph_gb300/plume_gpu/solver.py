@@ -177,6 +177,25 @@ class Solver:
     def adapt_domain(self):
         self._check(self.L.plume_adapt_domain(self.ctx), "plume_adapt_domain")
 
+    # -- output snapshots -----------------------------------------------------
+    def snapshot_begin(self, host: ParticleSet):
+        """queue a copy of the current particles into host's arrays (the
+        fields write_h5part writes, h5part_writer.cc:41-275) and return;
+        stepping may continue while the copy runs.  Arrays in page-locked
+        memory (pinned_set) are written by the device directly."""
+        s = host.soa()
+        self._check(self.L.plume_snapshot_begin(self.ctx, C.byref(s), host.n), "plume_snapshot_begin")
+        self._snap = (host, s)
+
+    def snapshot_end(self):
+        """wait for the snapshot: (rows, time, step)"""
+        n, t, st = C.c_size_t(), C.c_double(), C.c_int()
+        self._check(self.L.plume_snapshot_end(self.ctx, C.byref(n), C.byref(t), C.byref(st)),
+                    "plume_snapshot_end")
+        host, _ = self._snap
+        self._snap = None
+        return host.take(slice(0, n.value)), t.value, st.value
+
     # -- GSPH -----------------------------------------------------------------
     def gsph_gradients(self):
         """(keys, (n, (D+2)*D) gradients) of the last GSPH step

@@ -143,6 +143,7 @@ def main():
     make_gsph()
     make_gsph_end()
     make_adapt()
+    make_csv()
 
 
 def make_gsph_end():
@@ -190,6 +191,27 @@ def make_adapt():
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def make_csv():
+    """sod_1d_csv.npz: the 1D Sod tube (200 reals, Gaussian kernel) after 20
+    steps and the text the reference's write_csv appends for that state
+    (h5part_writer.cc:448-490; rows in key order, see oracle/ref/driver.cc)"""
+    case = cases.sod_1d(n_real=200)
+    work = "/tmp/plume_golden_csv"
+    os.makedirs(work, exist_ok=True)
+    out = os.path.join(work, "pvplot_out.csv")
+    if os.path.exists(out):
+        os.remove(out)
+    steps, _ = refio.run_ref("ref1d_csv", case, 20, work, dump_last=True)
+    with open(out) as f:
+        text = f.read()
+    d = {"nsteps": 20, "step0": case.step0, "pre_adaptive": int(case.pre_adaptive), "dim": 1,
+         "csv": np.array(text)}
+    d.update(pack("out_", steps[-1]["particles"].sorted_by_key()))
+    path = os.path.join(HERE, "sod_1d_csv.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def make_bc():
     c = cases.plume_3d(half_width=300.0, height=600.0, dx=50.0, vent_radius=50.0,
                        vent_dx=25.0, duct_depth=300.0, seed=4, name="plume_3d_bc")
@@ -204,6 +226,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--csv":
+        refio.build_ref()
+        make_csv()
     elif len(sys.argv) > 1 and sys.argv[1] == "--gsph-end":
         refio.build_ref()
         make_gsph_end()

@@ -15,7 +15,7 @@ import pytest
 from oracle.binding import OracleRun
 from plume_gpu import cases
 from plume_gpu.abi import BYTE_FIELDS, RIEMANN_ROE
-from _util import field_errors, golden_case, set_summary, unpack
+from _util import GOLDEN, field_errors, golden_case, set_summary, unpack
 
 
 @pytest.mark.parametrize("name", ["sod_1d_200", "shock_tube_1d"])
@@ -236,3 +236,21 @@ def test_oracle_gsph_sod_2000_full_run_bit_exact():
     assert o.t.time == float(d["time"][-1])
     err = field_errors(o.ps, unpack(d, "out_"))
     assert max(err.values()) == 0.0, err
+
+
+def test_csv_writer_matches_reference_write_csv(tmp_path):
+    """the 1D text output (plume_gpu.output.write_csv) of the reference's
+    final Sod state is byte-for-byte the text the reference's write_csv
+    wrote for it (tests/golden/sod_1d_csv.npz); a second call appends a
+    second header and the rows again"""
+    from plume_gpu.output import CSV_HEADER, write_csv
+    d = np.load(os.path.join(GOLDEN, "sod_1d_csv.npz"))
+    ps = unpack(d, "out_")  # sorted by key: the reference's row order
+    path = tmp_path / "pvplot_out.csv"
+    n = write_csv(str(path), ps, order=np.arange(ps.n))
+    text = path.read_text()
+    assert text == str(d["csv"])
+    assert n == int(np.sum(ps.bc_type == 100)) > 0
+    write_csv(str(path), ps, order=np.arange(ps.n))
+    assert path.read_text() == 2 * str(d["csv"])
+    assert text.startswith(CSV_HEADER)
