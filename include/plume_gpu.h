@@ -476,6 +476,21 @@ int plume_adjoint_backward(plume_ctx *ctx, const PlumeSoA *final_bar, size_t n_f
 int plume_timestep_noalloc(const double *h, const double *c, const uint8_t *bc_type,
                            size_t n, double cfl, double *dt_out, void *stream);
 
+/* ---- bucket grid ------------------------------------------------------
+ * The preprocessor's bucket grid for a flat-ground domain (preprocess.cc:
+ * 68-177, 386-464; the funkyNNNN.h5 files that Read_Grid loads,
+ * dataread.cc:247), computed on the device: the original domain [lo, hi]
+ * padded by 1.5 buckets of edge 8 * h0, bucket counts rounded up, and the
+ * face indices and types of every bucket (MIXED; absorbing with
+ * PLUME_BUCKET_UNDERGROUND or PLUME_BUCKET_PRESS_BC; OVERGROUND none).
+ * Fills grid (mindom, del, nb, subcells, domain_lo/hi) and *nbk (buckets,
+ * x fastest); with flags and face_index (host arrays of cap and 6 * cap
+ * entries) also those, and points grid->flags / face_index at them.  Call
+ * with flags NULL to size.  PLUME_E_CAPACITY when *nbk > cap. */
+int plume_grid_generate(const double lo[3], const double hi[3], double h0, int subcells,
+                        PlumeGrid *grid, uint8_t *flags, int8_t *face_index, size_t cap,
+                        size_t *nbk);
+
 /* Library version string "major.minor.patch". */
 const char *plume_version(void);
 

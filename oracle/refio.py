@@ -112,3 +112,41 @@ def run_ref(variant, case, nsteps, workdir, dump_last=False, images=None, binv=N
     exe = os.path.join(HERE, "_ref", variant, "driver")
     subprocess.run([exe, cin, cout], check=True, cwd=workdir)
     return read_result(cout)
+
+
+# bucket records of oracle/ref/preproc_dump.cc (KEYLENGTH 2, NEIGH_SIZE 27)
+_PP_KEYLEN, _PP_NEIGH = 2, 27
+
+
+def run_preproc(lo, hi, h0, workdir, nproc=1):
+    """the reference's preprocessor on the flat-ground domain [lo, hi] with
+    smoothing length h0: (htvars, dict of per-bucket arrays over all
+    processes' records: key (n, 2), type, proc, index (n, 6), lo (n, 3),
+    hi (n, 3), neighs (n, 27, 2), neigh_proc (n, 27))"""
+    os.makedirs(workdir, exist_ok=True)
+    out = os.path.join(workdir, "funky_dump.bin")
+    if os.path.exists(out):
+        os.remove(out)
+    env = dict(os.environ, ORACLE_DOMAIN=" ".join(repr(float(v)) for v in list(lo) + list(hi)))
+    exe = os.path.join(HERE, "_ref", "preproc", "preprocess")
+    subprocess.run([exe, str(nproc), repr(float(h0)), "0"], check=True, cwd=workdir, env=env,
+                   stdout=subprocess.DEVNULL)
+    data = open(out, "rb").read()
+    rec = np.dtype([("key", "<u4", _PP_KEYLEN), ("type", "<i4"), ("proc", "<i4"), ("index", "<i4", 6),
+                    ("xc", "<f8", 2), ("yc", "<f8", 2), ("zc", "<f8", 2),
+                    ("neighs", "<u4", _PP_NEIGH * _PP_KEYLEN), ("neigh_proc", "<i4", _PP_NEIGH)])
+    off, parts, ht = 0, [], None
+    while off < len(data):
+        off += 4  # myid
+        ht = np.frombuffer(data, "<f8", 6, off).copy(); off += 48
+        (nb,) = np.frombuffer(data, "<i8", 1, off); off += 8
+        parts.append(np.frombuffer(data, rec, int(nb), off)); off += int(nb) * rec.itemsize
+        (npart,) = np.frombuffer(data, "<i8", 1, off); off += 8 + 4 * int(npart)
+    r = np.concatenate(parts)
+    return ht, {"key": r["key"].copy(), "type": r["type"].copy(), "proc": r["proc"].copy(),
+                "index": r["index"].copy(),
+                "lo": np.stack([r["xc"][:, 0], r["yc"][:, 0], r["zc"][:, 0]], axis=1),
+                "hi": np.stack([r["xc"][:, 1], r["yc"][:, 1], r["zc"][:, 1]], axis=1),
+                "neighs": r["neighs"].reshape(-1, _PP_NEIGH, _PP_KEYLEN).copy(),
+                "neigh_proc": r["neigh_proc"].copy()}
+

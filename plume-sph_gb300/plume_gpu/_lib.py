@@ -37,7 +37,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         nvcc = "/usr/local/cuda/bin/nvcc"
     tmp = LIBPATH + ".tmp"
     cmd = [nvcc] + NVCC_FLAGS + ["-o", tmp, os.path.join(CSRC, "plume_gpu.cu"),
-                                 os.path.join(CSRC, "timestep_noalloc.cu")]
+                                 os.path.join(CSRC, "timestep_noalloc.cu"),
+                                 os.path.join(CSRC, "grid_generate.cu")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed:\n" + r.stderr[-4000:])
@@ -96,6 +97,8 @@ def lib():
         L.plume_scan_outside_layer.argtypes = [C.c_void_p, P(C.c_int)]
         L.plume_adapt_domain.argtypes = [C.c_void_p]
         L.plume_snapshot_begin.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t]
+        L.plume_grid_generate.argtypes = [P(C.c_double), P(C.c_double), C.c_double, C.c_int, P(PlumeGrid),
+                                          P(C.c_uint8), P(C.c_int8), C.c_size_t, P(C.c_size_t)]
         L.plume_snapshot_end.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_double), P(C.c_int)]
         L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,

@@ -272,7 +272,13 @@ def _face(crd, lo, hi):
 
 
 def plume_grid(lo, hi, h0, subcells=4) -> Grid:
-    """Bucket grid of the preprocessor (preprocess.cc:100-177, :404-439)."""
+    """Bucket grid of the preprocessor (preprocess.cc:100-177, :404-464):
+    the original domain [lo, hi] padded by EXT_DOM_COF = EXT_DOM_COF_BOT =
+    1.5 buckets of edge PARTICLE_DENSITY * h0 = 8 h0; bucket types from the
+    face indices (a bucket outside the domain on some axis is UNDERGROUND
+    when it lies wholly below the ground, else PRESS_BC -- both absorbing
+    here; one straddling the domain's edge is MIXED; and every bucket that
+    straddles the ground is MIXED, whatever its other axes say)."""
     del_ = 8.0 * h0                     # PARTICLE_DENSITY * smoothing length
     mind = [lo[a] - 1.5 * del_ for a in range(3)]
     maxd = [hi[a] + 1.5 * del_ for a in range(3)]
@@ -292,7 +298,9 @@ def plume_grid(lo, hi, h0, subcells=4) -> Grid:
                     bt += [_face(c0[a], lo[a], hi[a]), _face(c1[a], lo[a], hi[a])]
                 flag = [abs(bt[2 * a] + bt[2 * a + 1]) for a in range(3)]
                 face[6 * b:6 * b + 6] = bt
-                if 2 in flag:
+                if bt[4] == -1 and bt[5] == 0:
+                    flags[b] = BUCKET_MIXED              # straddles the ground (:462-463)
+                elif 2 in flag:
                     flags[b] = BUCKET_ABSORBING          # underground or pressure bc
                 elif 1 in flag:
                     flags[b] = BUCKET_MIXED
@@ -360,9 +368,12 @@ def adapt_scenario(case):
     binv = np.where(absorbing, BINV_NONE, BINV_POTENTIAL).astype(np.uint8)
     idx = np.arange(len(flags))
     bx = idx % nb[0]
-    bx_max = int(bx[~absorbing].max())
-    layer = (~absorbing) & (bx == bx_max)
-    inner = (~absorbing) & (bx == bx_max - 1)
+    # non-absorbing buckets not wholly beyond the domain in +x (the
+    # ground-straddling MIXED ring outside the domain is left as it is)
+    cand = ~absorbing & (face[:, 0] != 1)
+    bx_max = int(bx[cand].max())
+    layer = cand & (bx == bx_max)
+    inner = cand & (bx == bx_max - 1)
     flags[layer] |= BUCKET_ABSORBING
     binv[layer] = BINV_NONE
     ps = case.particles.copy()

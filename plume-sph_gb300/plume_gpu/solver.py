@@ -18,6 +18,31 @@ from .abi import (DOUBLE_FIELDS, STATUS_NAMES, ParticleSet, PlumeGrid, PlumeOpti
                   PlumeStepLog)
 
 
+def generate_grid(lo, hi, h0: float, subcells: int = 4):
+    """the preprocessor's bucket grid for the flat-ground domain [lo, hi]
+    and smoothing length h0, computed on the device (plume_grid_generate);
+    the same grid as cases.plume_grid, with the explicit UNDERGROUND /
+    PRESS_BC bits on the absorbing buckets"""
+    from .abi import Grid
+    L = _lib.lib()
+    lo3 = (C.c_double * 3)(*[float(v) for v in lo])
+    hi3 = (C.c_double * 3)(*[float(v) for v in hi])
+    g = PlumeGrid()
+    n = C.c_size_t()
+    rc = L.plume_grid_generate(lo3, hi3, float(h0), int(subcells), C.byref(g), None, None, 0, C.byref(n))
+    if rc:
+        raise PlumeError(rc, "plume_grid_generate")
+    flags = np.zeros(n.value, dtype=np.uint8)
+    face = np.zeros(6 * n.value, dtype=np.int8)
+    rc = L.plume_grid_generate(lo3, hi3, float(h0), int(subcells), C.byref(g),
+                               flags.ctypes.data_as(C.POINTER(C.c_uint8)),
+                               face.ctypes.data_as(C.POINTER(C.c_int8)), n.value, C.byref(n))
+    if rc:
+        raise PlumeError(rc, "plume_grid_generate")
+    return Grid(mindom=tuple(g.mindom), del_=g.del_, nb=tuple(g.nb), subcells=g.subcells, flags=flags,
+                face_index=face, domain_lo=tuple(g.domain_lo), domain_hi=tuple(g.domain_hi))
+
+
 class PlumeError(RuntimeError):
     def __init__(self, status: int, where: str, detail: str = ""):
         self.status = status

@@ -144,6 +144,7 @@ def main():
     make_gsph_end()
     make_adapt()
     make_csv()
+    make_grid()
 
 
 def make_gsph_end():
@@ -191,6 +192,32 @@ def make_adapt():
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+GRID_DOMAINS = (
+    # (name, lo, hi, h0, nproc): the 20 km plume domain at 150 m, the 600 m
+    # test plume at 50 m, and a ragged domain above 1.5 km (bucket counts
+    # rounded up, records split over three processes)
+    ("plume_20km", (-1.0e4, -1.0e4, 0.0), (1.0e4, 1.0e4, 2.0e4), 150.0, 1),
+    ("plume_600m", (-300.0, -300.0, 0.0), (300.0, 300.0, 600.0), 50.0, 1),
+    ("ragged", (-2400.0, -2350.0, 1500.0), (2410.0, 2400.0, 14000.0), 137.3, 3),
+)
+
+
+def make_grid():
+    """grid_3d.npz: the reference preprocessor's buckets (type,
+    bucket_index, lower corner) and hash-table bounds for GRID_DOMAINS"""
+    d = {}
+    for name, lo, hi, h0, nproc in GRID_DOMAINS:
+        ht, r = refio.run_preproc(lo, hi, h0, "/tmp/plume_golden_grid", nproc)
+        d[f"{name}_ht"] = ht
+        d[f"{name}_type"] = r["type"].astype(np.int8)
+        d[f"{name}_index"] = r["index"].astype(np.int8)
+        d[f"{name}_lo"] = r["lo"]
+        d[f"{name}_domain"] = np.array(list(lo) + list(hi) + [h0])
+    path = os.path.join(HERE, "grid_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def make_csv():
     """sod_1d_csv.npz: the 1D Sod tube (200 reals, Gaussian kernel) after 20
     steps and the text the reference's write_csv appends for that state
@@ -226,6 +253,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--grid":
+        refio.build_ref()
+        make_grid()
     elif len(sys.argv) > 1 and sys.argv[1] == "--csv":
         refio.build_ref()
         make_csv()

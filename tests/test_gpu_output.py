@@ -84,3 +84,31 @@ def test_snapshot_csv_of_sod_tube():
     a.snapshot_begin(host)
     snap, _, _ = a.snapshot_end()
     assert csv_lines(snap) == csv_lines(b.download())
+
+
+@pytest.mark.parametrize("name", ["plume_20km", "plume_600m", "ragged"])
+def test_device_grid_equals_preprocessor(name):
+    """plume_grid_generate against the reference preprocessor's buckets
+    (tests/golden/grid_3d.npz) and cases.plume_grid"""
+    import os
+    from plume_gpu import generate_grid
+    from plume_gpu.abi import (BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_PRESS_BC,
+                               BUCKET_UNDERGROUND)
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "grid_3d.npz"))
+    dom = d[f"{name}_domain"]
+    g = generate_grid(tuple(dom[:3]), tuple(dom[3:6]), float(dom[6]))
+    h = cases.plume_grid(tuple(dom[:3]), tuple(dom[3:6]), float(dom[6]))
+    assert (g.mindom, g.del_, g.nb) == (h.mindom, h.del_, h.nb)
+    np.testing.assert_array_equal(g.face_index, h.face_index)
+    np.testing.assert_array_equal(g.flags & (BUCKET_ABSORBING | BUCKET_MIXED), h.flags)
+    ht, typ, lo = d[f"{name}_ht"], d[f"{name}_type"], d[f"{name}_lo"]
+    nb = np.array(g.nb)
+    np.testing.assert_array_equal(ht[0::2], np.array(g.mindom))
+    ijk = np.rint((lo - np.array(g.mindom)) / g.del_).astype(np.int64)
+    b = (ijk[:, 2] * nb[1] + ijk[:, 1]) * nb[0] + ijk[:, 0]
+    f = g.flags[b]
+    np.testing.assert_array_equal(f & BUCKET_UNDERGROUND != 0, typ == 1)
+    np.testing.assert_array_equal(f & BUCKET_PRESS_BC != 0, typ == 4)
+    np.testing.assert_array_equal(f & BUCKET_MIXED != 0, typ == 2)
+    np.testing.assert_array_equal(f == 0, typ == 3)
+    np.testing.assert_array_equal(g.face_index.reshape(-1, 6)[b], d[f"{name}_index"])

@@ -254,3 +254,30 @@ def test_csv_writer_matches_reference_write_csv(tmp_path):
     write_csv(str(path), ps, order=np.arange(ps.n))
     assert path.read_text() == 2 * str(d["csv"])
     assert text.startswith(CSV_HEADER)
+
+
+@pytest.mark.parametrize("name", ["plume_20km", "plume_600m", "ragged"])
+def test_bucket_grid_matches_reference_preprocessor(name):
+    """cases.plume_grid against the buckets of the reference's preprocess.cc
+    (tests/golden/grid_3d.npz): hash-table bounds, bucket count and corners,
+    bucket_index per face, and bucket types (UNDERGROUND / PRESS_BC are the
+    absorbing buckets, MIXED the mixed ones, OVERGROUND neither)"""
+    from plume_gpu.abi import BUCKET_ABSORBING, BUCKET_MIXED
+    d = np.load(os.path.join(GOLDEN, "grid_3d.npz"))
+    dom = d[f"{name}_domain"]
+    g = cases.plume_grid(tuple(dom[:3]), tuple(dom[3:6]), float(dom[6]))
+    ht, typ, idx, lo = d[f"{name}_ht"], d[f"{name}_type"], d[f"{name}_index"], d[f"{name}_lo"]
+    nb = np.array(g.nb)
+    assert typ.shape[0] == nb.prod()
+    np.testing.assert_array_equal(ht[0::2], np.array(g.mindom))
+    np.testing.assert_array_equal(ht[1::2], np.array(g.mindom) + nb * g.del_)
+    ijk = np.rint((lo - np.array(g.mindom)) / g.del_).astype(np.int64)
+    np.testing.assert_array_equal(lo, np.array(g.mindom) + ijk * g.del_)
+    b = (ijk[:, 2] * nb[1] + ijk[:, 1]) * nb[0] + ijk[:, 0]
+    assert len(np.unique(b)) == len(b)
+    face = np.asarray(g.face_index).reshape(-1, 6)
+    np.testing.assert_array_equal(face[b], idx)
+    flags = np.asarray(g.flags)[b]
+    want = np.select([np.isin(typ, (1, 4)), typ == 2], [BUCKET_ABSORBING, BUCKET_MIXED], 0)
+    assert set(np.unique(typ)) <= {1, 2, 3, 4}
+    np.testing.assert_array_equal(flags & (BUCKET_ABSORBING | BUCKET_MIXED), want)
