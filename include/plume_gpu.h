@@ -331,6 +331,29 @@ int plume_get_bucket_involvement(plume_ctx *ctx, uint8_t *state, size_t nbuckets
 int plume_scan_outside_layer(plume_ctx *ctx, int *adapt);
 int plume_adapt_domain(plume_ctx *ctx);
 
+/* The hydrostatic atmosphere of ATMOSPHERE_TYPE 1 (air_prop_hydro,
+ * sph_lib.cc:488-592; constants of parameters.h:902-935). */
+typedef struct PlumeAtmosphere {
+    double Ta0, pa0, Ra, gamma;           /* Ta0_P pa0_P Ra_P gamma_P          */
+    double H1, H2, H3, miu1, miu2;        /* layer heights and lapse rates      */
+    double Ata1, Ate1, Ata2, Atb2, Ata3, Atb3, AtC3, Ate3; /* pressure fit     */
+} PlumeAtmosphere;
+
+/* The pressure-ghost layers that follow an adaptation (add_pressure_ghost,
+ * add_pressure_ghost.cc:37-316; main.cc:265-271), on the device: every NONE
+ * bucket that holds no pressure ghost and has a neighbour whose state is not
+ * NONE is made active and filled with a lattice of spacing
+ * sml_phase2 (edge / spacing points per axis, at corner + spacing/2 + i
+ * spacing; on-ground MIXED buckets above the ground only; UNDERGROUND
+ * buckets none) of pressure ghosts at rest in the hydrostatic air of their
+ * height (initial_air, sph_lib.cc:831-866: mass of the particle's box by the
+ * reference's three-point rule, then the mixture EOS).  The new rows get
+ * keys key_base, key_base + 1, ... (bucket by bucket, x fastest, then the
+ * lattice with z fastest); *added is their number.  Single-run 3D
+ * contexts; PLUME_E_CAPACITY when the table would overflow. */
+int plume_add_pressure_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base,
+                             size_t *added);
+
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):
  * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket

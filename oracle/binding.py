@@ -185,6 +185,14 @@ class OracleRun:
             self.ps = self.ps.take(np.arange(n.value))
         return np.array(dts[:nsteps])
 
+    def append(self, ps):
+        """rows added to the table (particles created outside a step)"""
+        out = ParticleSet(self.ps.n + ps.n)
+        for f in ["key"] + list(DOUBLE_FIELDS) + list(BYTE_FIELDS):
+            getattr(out, f)[:self.ps.n] = getattr(self.ps, f)
+            getattr(out, f)[self.ps.n:] = getattr(ps, f)
+        self.ps = out
+
     def scan_outside_layer(self, binv):
         """scan_outside_layer on the current particles; binv (uint8 per
         bucket) is updated in place; returns the count"""

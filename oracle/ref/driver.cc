@@ -70,7 +70,8 @@ struct Case {
   std::vector<uint64_t> img_key;
   std::vector<double> img_xyz;
   std::vector<uint8_t> binv;  // per-bucket has_involved (optional)
-  int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop
+  int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop,
+                              // 2: then add_pressure_ghost
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -185,11 +186,24 @@ static Particle *make_particle(const Case &c, int i) {
   return p;
 }
 
+// a particle of the case (key pkey(row)) rather than one the reference
+// created during the run
+static bool case_particle(Particle *p, const Case &c) {
+  const unsigned r = p->getKey().key[2];
+  if (r >= (unsigned)c.n) return false;
+  unsigned k[TKEYLENGTH];
+  pkey(r, k);
+  for (int q = 0; q < TKEYLENGTH; q++)
+    if (p->getKey().key[q] != k[q]) return false;
+  return true;
+}
+
 static void dump_state(FILE *fo, THashTable *P, const Case &c, const TimeProps &tp, double dt) {
   std::vector<std::pair<unsigned, Particle *>> rows;
   THTIterator it(P);
   Particle *p;
-  while ((p = (Particle *)it.next())) rows.push_back(std::make_pair(p->getKey().key[2], p));
+  while ((p = (Particle *)it.next()))
+    if (case_particle(p, c)) rows.push_back(std::make_pair(p->getKey().key[2], p));
   std::sort(rows.begin(), rows.end(),
             [](const std::pair<unsigned, Particle *> &a, const std::pair<unsigned, Particle *> &b) {
               return a.first < b.first;
@@ -536,6 +550,8 @@ int main(int argc, char **argv) {
   if (c.adapt_mode) {
     adapt_n = scan_outside_layer(P, BG, 1, 0);
     if (adapt_n) adapt_domain(P, BG, matprops, 1, 0);
+    // the pressure-ghost layers that follow an adaptation (main.cc:265-271)
+    if (adapt_n && c.adapt_mode == 2) add_pressure_ghost(P, BG, simprops, matprops, tp, 1, 0);
     dump_state(fo, P, c, *tp, 0.0);
     ndumped++;
   }
@@ -555,6 +571,54 @@ int main(int argc, char **argv) {
     for (size_t b = 0; b < bucks.size(); b++) {
       uint8_t st = (uint8_t)bucks[b]->get_has_involved();
       fwrite(&st, 1, 1, fo);
+    }
+    // char[4] "PGHO"; int64 n; the particles created during the run (by
+    // add_pressure_ghost), ordered by key: double x, y, z, vx, vy, vz, vsx,
+    // vsy, vsz, m, h, rho, e, p, Y, gamma, c, T, cp (n each), then uint8
+    // phase, bc_type, involved; then uint8 active per bucket
+    std::vector<Particle *> born;
+    THTIterator it(P);
+    Particle *p;
+    while ((p = (Particle *)it.next()))
+      if (!case_particle(p, c)) born.push_back(p);
+    std::sort(born.begin(), born.end(), [](Particle *a, Particle *b) { return a->getKey() < b->getKey(); });
+    fwrite("PGHO", 1, 4, fo);
+    int64_t nn = (int64_t)born.size();
+    fwrite(&nn, 8, 1, fo);
+    std::vector<double> col(born.size());
+    for (int f = 0; f < NF; f++) {
+      for (size_t r = 0; r < born.size(); r++) {
+        Particle *q = born[r];
+        double v = 0;
+        switch (f) {
+        case FX: case FY: case FZ: v = q->get_coords()[f - FX]; break;
+        case FVX: case FVY: case FVZ: v = q->get_vel()[f - FVX]; break;
+        case FSX: case FSY: case FSZ: v = q->get_smoothed_velocity()[f - FSX]; break;
+        case FM: v = q->get_mass(); break;
+        case FH: v = q->get_smlen(); break;
+        case FRHO: v = q->get_density(); break;
+        case FE: v = q->get_energy(); break;
+        case FP: v = q->get_pressure(); break;
+        case FYF: v = q->get_mass_frac(); break;
+        case FG: v = q->get_gamma(); break;
+        case FC: v = q->get_sound_speed(); break;
+        case FT: v = q->get_temperature(); break;
+        case FCP: v = q->get_specific_heat_p(); break;
+        }
+        col[r] = v;
+      }
+      fwrite(col.data(), 8, born.size(), fo);
+    }
+    std::vector<uint8_t> bb(born.size());
+    for (size_t r = 0; r < born.size(); r++) bb[r] = (uint8_t)born[r]->which_phase();
+    fwrite(bb.data(), 1, born.size(), fo);
+    for (size_t r = 0; r < born.size(); r++) bb[r] = (uint8_t)born[r]->get_bc_type();
+    fwrite(bb.data(), 1, born.size(), fo);
+    for (size_t r = 0; r < born.size(); r++) bb[r] = (uint8_t)born[r]->get_involved();
+    fwrite(bb.data(), 1, born.size(), fo);
+    for (size_t b = 0; b < bucks.size(); b++) {
+      uint8_t act = (uint8_t)bucks[b]->is_active();
+      fwrite(&act, 1, 1, fo);
     }
   }
 #endif

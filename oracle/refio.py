@@ -20,8 +20,9 @@ def build_ref(ref_root: str = "/root/reference"):
 
 def write_case(path, case, nsteps, dump_last=False, images=None, binv=None, adapt=False):
     """images: optional (ghost keys, image points (n, 3)) of the wall
-    boundary (3D); binv: optional per-bucket involvement states; adapt: run
-    scan_outside_layer / adapt_domain after the steps (ref3d_adapt)"""
+    boundary (3D); binv: optional per-bucket involvement states; adapt: 1 runs
+    scan_outside_layer / adapt_domain after the steps, 2 also
+    add_pressure_ghost (ref3d_adapt)"""
     o, g, ps = case.options, case.grid, case.particles
     with open(path, "wb") as fp:
         fp.write(b"PLSPHIN1")
@@ -101,6 +102,20 @@ def read_result(path):
         (nbk,) = take("<q")
         st = np.frombuffer(data, np.uint8, nbk, off).copy(); off += nbk
         steps[-1]["adapt"] = (int(na), st)
+    if data[off:off + 4] == b"PGHO":
+        # the particles the reference created during the run (pressure
+        # ghosts of add_pressure_ghost), by key, and bucket activity
+        off += 4
+        (nn,) = take("<q")
+        born = PS(int(nn))
+        for f in DOUBLE_FIELDS:
+            setattr(born, f, np.frombuffer(data, "<f8", nn, off).copy()); off += 8 * nn
+        for f in BYTE_FIELDS:
+            setattr(born, f, np.frombuffer(data, np.uint8, nn, off).copy()); off += nn
+        nbk = len(steps[-1]["adapt"][1])
+        act = np.frombuffer(data, np.uint8, nbk, off).copy(); off += nbk
+        steps[-1]["born"] = born
+        steps[-1]["active"] = act
     return steps, lists
 
 

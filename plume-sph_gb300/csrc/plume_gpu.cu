@@ -690,6 +690,122 @@ __global__ void k_adapt_buckets(const Geo* __restrict__ geo, const uint16_t* __r
   if (bflags) bflags[gb] = f & (uint8_t)~PLUME_BUCKET_ABSORBING;
 }
 
+// ---- add_pressure_ghost (add_pressure_ghost.cc:37-316): pressure-ghost
+// layers around the buckets an adaptation made potentially involved.
+// Hydrostatic air of ATMOSPHERE_TYPE 1 (air_prop_hydro, sph_lib.cc:488-592)
+struct Atm {
+  double Ta0, pa0, Ra, gamma, H1, H2, H3, miu1, miu2, Ata1, Ate1, Ata2, Atb2, Ata3, Atb3, AtC3, Ate3;
+};
+__device__ __forceinline__ double atm_T(const Atm& a, double h) {
+  if (h < 0) return a.Ta0;
+  if (h < a.H1) return a.Ta0 - a.miu1 * h;
+  if (h < a.H2) return a.Ta0 - a.miu1 * a.H1;
+  return a.Ta0 - a.miu1 * a.H1 + a.miu2 * (h - a.H2);
+}
+__device__ __forceinline__ double atm_p(const Atm& a, double h) {
+  if (h < 0) return a.pa0;
+  if (h < a.H1) return a.Ata1 * pow(a.Ta0 - a.miu1 * h, a.Ate1);
+  if (h < a.H2) return a.Ata2 * exp(a.Atb2 * h);
+  return a.AtC3 * pow(a.Atb3 * h + a.Ata3, a.Ate3);
+}
+
+// lattice of a bucket: points per axis (C round of edge / dx) and, in
+// on-ground MIXED buckets, the first z layer above the ground
+struct PgLattice {
+  double lo[3];
+  int n[3], k0;
+};
+__device__ __forceinline__ PgLattice pg_lattice(const Geo& g, int b, double dx, double ground, bool onground) {
+  const int ijk[3] = {b % g.nb[0], (b / g.nb[0]) % g.nb[1], b / (g.nb[0] * g.nb[1])};
+  PgLattice L;
+  for (int a = 0; a < 3; a++) {
+    L.lo[a] = g.mind[a] + ijk[a] * g.del;
+    const double hi = g.mind[a] + (ijk[a] + 1) * g.del;
+    L.n[a] = (int)round((hi - L.lo[a]) / dx);
+  }
+  L.k0 = 0;
+  if (onground)
+    while (L.k0 < L.n[2] && !(L.lo[2] + 0.5 * dx + L.k0 * dx > ground)) L.k0++;
+  return L;
+}
+
+// One thread per bucket: a NONE bucket that holds no pressure ghost and has
+// a neighbour whose state is not NONE is marked and made active; its count
+// is its lattice (none for UNDERGROUND buckets)
+__global__ void k_pg_buckets(const Geo* __restrict__ geo, Dev A, const uint32_t* __restrict__ cs,
+                             const uint8_t* __restrict__ binv, uint8_t* __restrict__ bflags,
+                             const int8_t* __restrict__ bface, int nbk, int explicit_types, double dx,
+                             double ground, uint32_t* __restrict__ cnt, uint8_t* __restrict__ mark) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbk) return;
+  cnt[b] = 0;
+  mark[b] = 0;
+  if (binv[b] != PLUME_BINV_NONE) return;
+  const Geo& g = geo[0];
+  bool has_pg = false;
+  for_bucket_rows(g, cs, b, [&](uint32_t j0, uint32_t j1) {
+    for (uint32_t j = j0; j < j1 && !has_pg; j++) has_pg = A.bc[j] == PLUME_BC_PRESSURE;
+  });
+  if (has_pg) return;
+  if (!any_neighbour(g, b, [&](int nb) { return binv[nb] != PLUME_BINV_NONE; })) return;
+  mark[b] = 1;
+  const uint8_t f = bflags ? bflags[b] : 0;
+  if (bflags) bflags[b] = f & (uint8_t)~PLUME_BUCKET_INACTIVE;
+  const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
+  const int t = btype_of(f, fi, explicit_types);
+  if (t == 1) return;  // UNDERGROUND: none
+  const PgLattice L = pg_lattice(g, b, dx, ground, t == 3 && fi && fi[4] == -1);
+  cnt[b] = (uint32_t)L.n[0] * (uint32_t)L.n[1] * (uint32_t)(L.n[2] - L.k0);
+}
+
+// One block per bucket: its lattice points, k fastest, appended at row
+// base + offs[b]; state of initial_air (sph_lib.cc:831-866) and the EOS
+__global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ mopt, Dev A,
+                          const uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface,
+                          int explicit_types, const uint32_t* __restrict__ cnt,
+                          const unsigned long long* __restrict__ offs, Atm atm, double dx, double ground,
+                          size_t base, unsigned long long key_base) {
+  const int b = blockIdx.x;
+  const uint32_t nq = cnt[b];
+  if (nq == 0) return;
+  const Geo& g = geo[0];
+  const Opt& o = mopt[0];
+  const uint8_t f = bflags ? bflags[b] : 0;
+  const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
+  const int t = btype_of(f, fi, explicit_types);
+  const PgLattice L = pg_lattice(g, b, dx, ground, t == 3 && fi && fi[4] == -1);
+  const uint32_t nk = (uint32_t)(L.n[2] - L.k0);
+  const double dx2 = 0.5 * dx, s2 = 0.5 * dx;
+  for (uint32_t q = threadIdx.x; q < nq; q += blockDim.x) {
+    const uint32_t i = q / ((uint32_t)L.n[1] * nk);
+    const uint32_t j = (q / nk) % (uint32_t)L.n[1];
+    const uint32_t k = (uint32_t)L.k0 + q % nk;
+    const double x = L.lo[0] + dx2 + i * dx;
+    const double y = L.lo[1] + dx2 + j * dx;
+    const double z = L.lo[2] + dx2 + k * dx;
+    const double T = atm_T(atm, z);
+    const double p0 = atm_p(atm, z);
+    const double rho = p0 / (atm.Ra * T);
+    const double e = p0 / (rho * (atm.gamma - 1));
+    const double z1 = z - s2, z2 = z + s2;
+    const double d1 = atm_p(atm, z1) / (atm.Ra * atm_T(atm, z1));
+    const double d2 = atm_p(atm, z2) / (atm.Ra * atm_T(atm, z2));
+    const double vol = ((x + s2) - (x - s2)) * ((y + s2) - (y - s2)) * (z2 - z1);
+    const double mass = vol * (0.1666667 * d1 + 0.6666666 * rho + 0.1666667 * d2);
+    const size_t r = base + offs[b] + q;
+    A.key[r] = key_base + offs[b] + q;
+    A.x[r] = x; A.y[r] = y; A.z[r] = z;
+    A.vx[r] = 0; A.vy[r] = 0; A.vz[r] = 0;
+    A.vsx[r] = 0; A.vsy[r] = 0; A.vsz[r] = 0;
+    A.mass[r] = mass; A.h[r] = dx; A.rho[r] = rho; A.e[r] = e; A.Y[r] = 0;
+    double gam, p, c, temp, cp = 0;
+    eos(o, rho, 0.0, e, gam, p, c, temp, cp, o.lans != 0);
+    A.gam[r] = gam; A.p[r] = p; A.c[r] = c; A.T[r] = temp; A.cp[r] = cp;
+    A.phase[r] = 1; A.bc[r] = PLUME_BC_PRESSURE; A.inv[r] = 0;
+    A.mem[r] = 0; A.bkt[r] = b;
+  }
+}
+
 // adapt_domain, particles of the converted buckets: real (100) and
 // potentially involved (1) -- on-ground MIXED buckets their pressure ghosts,
 // other MIXED buckets those inside the domain (determine_escape), OVERGROUND
@@ -2839,6 +2955,70 @@ int plume_adapt_domain(plume_ctx* ctx) {
                                                              ctx->bflags, ctx->bface, ctx->explicit_types);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
+  return PLUME_OK;
+}
+
+int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
+  if (!ctx || !atm || !added) return PLUME_E_INVALID;
+  *added = 0;
+  if (!ctx->binv) {
+    ctx->err = "add_pressure_ghost: 3D only";
+    return PLUME_E_INVALID;
+  }
+  if (ctx->nmem != 1) {
+    ctx->err = "add_pressure_ghost: single-run contexts only";
+    return PLUME_E_INVALID;
+  }
+  int rc = search(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->st;
+  const int nbk = ctx->nbk;
+  const double dx = ctx->opt.sml_phase2;
+  const double ground = ctx->hgeo[0].lo[2];
+  if (!(dx > 0) || ctx->hgeo[0].del / dx > 1024.0) {
+    ctx->err = "add_pressure_ghost: bucket edge / smoothing length must be in (0, 1024]";
+    return PLUME_E_INVALID;
+  }
+  uint32_t* cnt = nullptr;
+  unsigned long long* offs = nullptr;
+  CK(cudaMalloc(&cnt, 4 * (size_t)nbk));
+  CK(cudaMalloc(&offs, 8 * (size_t)nbk));
+  k_pg_buckets<<<nblocks(nbk), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->cs, ctx->binv, ctx->bflags, ctx->bface,
+                                                 nbk, ctx->explicit_types, dx, ground, cnt, ctx->bmark);
+  CK(cudaGetLastError());
+  std::vector<uint32_t> hc((size_t)nbk);
+  std::vector<unsigned long long> ho((size_t)nbk);
+  CK(cudaMemcpyAsync(hc.data(), cnt, 4 * (size_t)nbk, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  unsigned long long tot = 0;
+  for (int b = 0; b < nbk; b++) {
+    ho[b] = tot;
+    tot += hc[b];
+  }
+  if (ctx->n_alloc + tot > ctx->cap) {
+    cudaFree(cnt);
+    cudaFree(offs);
+    ctx->err = "add_pressure_ghost exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  if (tot) {
+    CK(cudaMemcpyAsync(offs, ho.data(), 8 * (size_t)nbk, cudaMemcpyHostToDevice, st));
+    const Atm a{atm->Ta0,  atm->pa0,  atm->Ra,   atm->gamma, atm->H1,   atm->H2,   atm->H3,   atm->miu1, atm->miu2,
+                atm->Ata1, atm->Ate1, atm->Ata2, atm->Atb2,  atm->Ata3, atm->Atb3, atm->AtC3, atm->Ate3};
+    k_pg_fill<<<nbk, 128, 0, st>>>(ctx->d_geo, ctx->d_opt, ctx->A, ctx->bflags, ctx->bface, ctx->explicit_types, cnt,
+                                  offs, a, dx, ground, ctx->n_alloc, (unsigned long long)key_base);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(st));
+  cudaFree(cnt);
+  cudaFree(offs);
+  ctx->launches += tot ? 2 : 1;
+  if (tot) {
+    rc = set_count(ctx, ctx->n_alloc + (size_t)tot);
+    if (rc) return rc;
+    ctx->pending_dead = true;
+  }
+  *added = (size_t)tot;
   return PLUME_OK;
 }
 

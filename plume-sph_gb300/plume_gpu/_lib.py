@@ -10,7 +10,7 @@ import os
 import subprocess
 import threading
 
-from .abi import PlumeGrid, PlumeInlet, PlumeOptions, PlumeSoA, PlumeStepLog
+from .abi import PlumeAtmosphere, PlumeGrid, PlumeInlet, PlumeOptions, PlumeSoA, PlumeStepLog
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
@@ -99,6 +99,7 @@ def lib():
         L.plume_snapshot_begin.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t]
         L.plume_grid_generate.argtypes = [P(C.c_double), P(C.c_double), C.c_double, C.c_int, P(PlumeGrid),
                                           P(C.c_uint8), P(C.c_int8), C.c_size_t, P(C.c_size_t)]
+        L.plume_add_pressure_ghost.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
         L.plume_snapshot_end.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_double), P(C.c_int)]
         L.plume_set_inlet.argtypes = [C.c_void_p, P(PlumeInlet), C.c_int]
         L.plume_adjoint_backward.argtypes = [C.c_void_p, P(PlumeSoA), C.c_size_t, P(PlumeSoA), C.c_size_t,

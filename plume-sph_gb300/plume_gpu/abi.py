@@ -68,6 +68,41 @@ class PlumeOptions(C.Structure):
     ]
 
 
+class PlumeAtmosphere(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("Ta0", "pa0", "Ra", "gamma", "H1", "H2", "H3", "miu1", "miu2",
+                                          "Ata1", "Ate1", "Ata2", "Atb2", "Ata3", "Atb3", "AtC3", "Ate3")]
+
+
+@dataclass
+class Atmosphere:
+    """The hydrostatic atmosphere of ATMOSPHERE_TYPE 1 (air_prop_hydro,
+    sph_lib.cc:488-592): temperature and the fitted pressure profile, with
+    the values of the 3D section of parameters.h:902-935."""
+    Ta0: float = 265.24
+    pa0: float = 0.831e5
+    Ra: float = 287.0
+    gamma: float = 1.4
+    H1: float = 11000.0
+    H2: float = 20000.0
+    H3: float = 100000.0
+    miu1: float = 6.5 / 1000
+    miu2: float = 2.0 / 1000
+    Ata1: float = 1.561024741e-8
+    Ate1: float = 5.258643795
+    Ata2: float = 1.321758528e+5
+    Atb2: float = -0.16963e-3
+    Ata3: float = 4.7248e+03
+    Atb3: float = 58.5117
+    AtC3: float = 5642.519912
+    Ate3: float = -0.1709059897e-1
+
+    def to_c(self) -> PlumeAtmosphere:
+        a = PlumeAtmosphere()
+        for n, _ in PlumeAtmosphere._fields_:
+            setattr(a, n, float(getattr(self, n)))
+        return a
+
+
 class PlumeGrid(C.Structure):
     _fields_ = [
         ("mindom", C.c_double * 3), ("del_", C.c_double), ("nb", C.c_int * 3),

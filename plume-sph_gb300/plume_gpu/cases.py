@@ -345,7 +345,7 @@ def wall_images(case):
     return keys, img
 
 
-def adapt_scenario(case):
+def adapt_scenario(case, clear_beyond=False):
     """A domain-growth set-up on a plume built by plume_3d: explicit bucket
     types (absorbing buckets below the ground UNDERGROUND, the other
     absorbing ones PRESS_BC), involvement NONE where absorbing and POTENTIAL
@@ -355,7 +355,9 @@ def adapt_scenario(case):
     the domain), and the particles of the layer inside it that sit in the
     outer half of their bucket are marked involved (2).  The scan then finds
     involved particles next to the pressure layer, and adapt_domain converts
-    that layer.  Returns (new case, per-bucket involvement states)."""
+    that layer.  clear_beyond: the particles of the bucket layer outside it
+    are removed, so that add_pressure_ghost refills those buckets after
+    the adaptation.  Returns (new case, per-bucket involvement states)."""
     import dataclasses
     g0 = case.grid
     nb = np.array(g0.nb)
@@ -386,6 +388,8 @@ def adapt_scenario(case):
     ps.involved[layer[pb] & real] = 0
     outer_half = (pos[:, 0] - (mind[0] + b3[:, 0] * g0.del_)) > 0.5 * g0.del_
     ps.involved[inner[pb] & real & outer_half] = 2
+    if clear_beyond:
+        ps = ps.take(np.nonzero(b3[:, 0] != bx_max + 1)[0])
     grid = dataclasses.replace(g0, flags=flags, face_index=np.array(g0.face_index).copy())
     return dataclasses.replace(case, grid=grid, particles=ps, name=case.name + "_adapt"), binv
 

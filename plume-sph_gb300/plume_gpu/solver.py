@@ -202,6 +202,17 @@ class Solver:
     def adapt_domain(self):
         self._check(self.L.plume_adapt_domain(self.ctx), "plume_adapt_domain")
 
+    def add_pressure_ghost(self, key_base: int, atmosphere=None) -> int:
+        """the pressure-ghost layers that follow an adaptation
+        (add_pressure_ghost), on the device; new keys from key_base; returns
+        how many particles were added"""
+        from .abi import Atmosphere
+        a = (atmosphere or Atmosphere()).to_c()
+        n = C.c_size_t()
+        self._check(self.L.plume_add_pressure_ghost(self.ctx, C.byref(a), int(key_base), C.byref(n)),
+                    "plume_add_pressure_ghost")
+        return n.value
+
     # -- output snapshots -----------------------------------------------------
     def snapshot_begin(self, host: ParticleSet):
         """queue a copy of the current particles into host's arrays (the

@@ -143,6 +143,7 @@ def main():
     make_gsph()
     make_gsph_end()
     make_adapt()
+    make_adapt_pg()
     make_csv()
     make_grid()
 
@@ -188,6 +189,27 @@ def make_adapt():
          "out_involved": out.involved, "out_x": out.x}
     d.update(pack("in_", c.particles))
     path = os.path.join(HERE, "adapt_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
+def make_adapt_pg():
+    """adapt_pg_3d.npz: the domain-growth set-up with the bucket layer
+    outside the converted one emptied (cases.adapt_scenario, clear_beyond):
+    one step, scan_outside_layer, adapt_domain, then the reference's
+    add_pressure_ghost.  Stores the input, flags and involvement states, and
+    the particles add_pressure_ghost created (by the reference's key) with
+    every bucket's activity after it."""
+    c = adapt_case()
+    c, binv = cases.adapt_scenario(c, clear_beyond=True)
+    steps, _ = refio.run_ref("ref3d_adapt", c, 1, "/tmp/plume_golden", binv=binv, adapt=2)
+    na, st = steps[-1]["adapt"]
+    d = {"nsteps": 1, "step0": c.step0, "pre_adaptive": 0, "dim": 3,
+         "flags": np.asarray(c.grid.flags, dtype=np.uint8), "binv_in": binv, "binv_out": st,
+         "adapt": np.int64(na), "active": steps[-1]["active"]}
+    d.update(pack("in_", c.particles))
+    d.update(pack("born_", steps[-1]["born"]))
+    path = os.path.join(HERE, "adapt_pg_3d.npz")
     np.savez_compressed(path, **d)
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
@@ -253,6 +275,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--adapt-pg":
+        refio.build_ref()
+        make_adapt_pg()
     elif len(sys.argv) > 1 and sys.argv[1] == "--grid":
         refio.build_ref()
         make_grid()

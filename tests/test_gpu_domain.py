@@ -70,3 +70,93 @@ def test_default_involvement_follows_absorbing_flags():
     st = s.bucket_involvement()
     absorbing = (c.grid.flags & cases.BUCKET_ABSORBING) != 0
     np.testing.assert_array_equal(st, np.where(absorbing, BINV_NONE, BINV_POTENTIAL))
+
+
+def _pg_fixture():
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "adapt_pg_3d.npz")))
+    c, _ = cases.adapt_scenario(adapt_case(), clear_beyond=True)
+    c.particles = unpack(d, "in_")
+    c.grid.flags = np.array(d["flags"], dtype=np.uint8)
+    return c, d
+
+
+def _by_position(ps):
+    return ps.take(np.lexsort((ps.z, ps.y, ps.x)))
+
+
+def test_pressure_ghosts_after_adaptation_match_reference():
+    """one step, scan_outside_layer, adapt_domain and add_pressure_ghost on
+    the device: the new particles are the reference's (matched by position;
+    positions, bc types and flags exact, the air state within 1e-14 of it:
+    CUDA's pow against libm's), their keys the requested range; then two
+    steps on the device and the oracle (which appends the same particles)
+    agree at the FP64 tolerance"""
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    c, d = _pg_fixture()
+    c.options.capacity = c.particles.n + 40000
+    s = Solver(c)
+    s.set_bucket_involvement(d["binv_in"])
+    s.steps(int(d["nsteps"]))
+    assert s.scan_outside_layer() == int(d["adapt"])
+    s.adapt_domain()
+    n0 = s.count()[0]
+    base = 1 << 40
+    added = s.add_pressure_ghost(base)
+    ref = unpack(d, "born_")
+    assert added == ref.n > 1000
+    g = s.download()
+    new = g.take(np.nonzero(g.key >= base)[0])
+    assert new.n == added and g.n == n0 + added
+    np.testing.assert_array_equal(np.sort(new.key), base + np.arange(added, dtype=np.uint64))
+    a, b = _by_position(new), _by_position(ref)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "vsx", "vsy", "vsz", "h", "Y"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in ("mass", "rho", "e", "p", "gamma", "c", "T", "cp"):
+        np.testing.assert_allclose(getattr(a, f), getattr(b, f), rtol=1e-14, atol=0, err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    # the layers in the following steps
+    from oracle.ghosts import add_pressure_ghost
+    o = OracleRun(c)
+    o.steps(1)
+    bi = np.array(d["binv_in"], dtype=np.uint8)
+    o.scan_outside_layer(bi)
+    o.adapt_domain(bi)
+    extra, _ = add_pressure_ghost(c.grid, bi, o.ps, c.options)
+    # the oracle's rows in the device's key order: by position
+    pos = {(x, y, z): k for x, y, z, k in zip(new.x, new.y, new.z, new.key)}
+    extra.key = np.array([pos[(x, y, z)] for x, y, z in zip(extra.x, extra.y, extra.z)], dtype=np.uint64)
+    o.append(extra)
+    s.steps(2)
+    o.steps(2)
+    gs, os_ = s.download().sorted_by_key(), o.ps.sorted_by_key()
+    np.testing.assert_array_equal(gs.key, os_.key)
+    np.testing.assert_array_equal(gs.bc_type, os_.bc_type)
+    for f in DOUBLE_FIELDS:
+        x, y = getattr(gs, f), getattr(os_, f)
+        assert np.abs(x - y).max() <= 1e-10 * max(np.abs(y).max(), 1e-300), f
+
+
+def test_pressure_ghosts_beyond_capacity_are_refused():
+    """a table without room for the new layers: PLUME_E_CAPACITY, and the
+    context keeps its particles"""
+    from plume_gpu import PlumeError
+    c, d = _pg_fixture()
+    s = Solver(c)
+    s.set_bucket_involvement(d["binv_in"])
+    s.steps(int(d["nsteps"]))
+    s.scan_outside_layer()
+    s.adapt_domain()
+    n0 = s.count()[0]
+    with pytest.raises(PlumeError) as e:
+        s.add_pressure_ghost(1 << 40)
+    assert e.value.status == 5
+    assert s.count()[0] == n0
+
+
+def test_pressure_ghosts_need_a_3d_single_run():
+    from plume_gpu import PlumeError
+    case = cases.sod_1d(n_real=200)
+    s = Solver(case)
+    with pytest.raises(PlumeError):
+        s.add_pressure_ghost(1 << 40)

@@ -14,7 +14,7 @@ import pytest
 
 from oracle.binding import OracleRun
 from plume_gpu import cases
-from plume_gpu.abi import BYTE_FIELDS, RIEMANN_ROE
+from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, RIEMANN_ROE
 from _util import GOLDEN, field_errors, golden_case, set_summary, unpack
 
 
@@ -281,3 +281,41 @@ def test_bucket_grid_matches_reference_preprocessor(name):
     want = np.select([np.isin(typ, (1, 4)), typ == 2], [BUCKET_ABSORBING, BUCKET_MIXED], 0)
     assert set(np.unique(typ)) <= {1, 2, 3, 4}
     np.testing.assert_array_equal(flags & (BUCKET_ABSORBING | BUCKET_MIXED), want)
+
+
+def _adapt_pg_fixture():
+    from _util import adapt_case
+    d = dict(np.load(os.path.join(GOLDEN, "adapt_pg_3d.npz")))
+    c, binv = cases.adapt_scenario(adapt_case(), clear_beyond=True)
+    c.particles = unpack(d, "in_")
+    c.grid.flags = np.array(d["flags"], dtype=np.uint8)
+    np.testing.assert_array_equal(binv, d["binv_in"])
+    return c, d
+
+
+def _by_position(ps):
+    return ps.take(np.lexsort((ps.z, ps.y, ps.x)))
+
+
+def test_oracle_pressure_ghosts_after_adaptation_match_reference():
+    """one step, scan_outside_layer, adapt_domain, then add_pressure_ghost:
+    the oracle's new pressure ghosts (oracle/ghosts.py) are the reference's,
+    field for field and bit for bit (matched by position: the reference's
+    keys are Hilbert keys of the creation step)"""
+    from oracle.ghosts import add_pressure_ghost
+    c, d = _adapt_pg_fixture()
+    o = OracleRun(c)
+    o.steps(int(d["nsteps"]))
+    binv = np.array(d["binv_in"], dtype=np.uint8)
+    assert o.scan_outside_layer(binv) == int(d["adapt"]) > 0
+    o.adapt_domain(binv)
+    np.testing.assert_array_equal(binv, d["binv_out"])
+    new, marked = add_pressure_ghost(c.grid, binv, o.ps, c.options)
+    ref = unpack(d, "born_")
+    assert new.n == ref.n > 1000
+    a, b = _by_position(new), _by_position(ref)
+    for f in DOUBLE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    assert np.all(d["active"] == 1) and len(marked) > 0
