@@ -354,6 +354,14 @@ typedef struct PlumeAtmosphere {
 int plume_add_pressure_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base,
                              size_t *added);
 
+/* The wall-ghost layers of a grown domain (add_wall_ghost,
+ * add_wall_ghost.cc:44-293; main.cc:279), on the device: every on-ground
+ * MIXED bucket (bottom face below the ground) that holds particles but no
+ * wall ghost gets wall ghosts (bc 2) on its lattice points below the ground
+ * plane, and the bucket below it is made active and filled whole; lattice,
+ * state, keys and errors as plume_add_pressure_ghost. */
+int plume_add_wall_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base, size_t *added);
+
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):
  * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket

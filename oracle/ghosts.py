@@ -1,10 +1,12 @@
-"""Pressure-ghost layers after a domain adaptation -- TEST INFRASTRUCTURE.
+"""Ghost layers after a domain adaptation -- TEST INFRASTRUCTURE.
 
 A numpy restatement of the reference's add_pressure_ghost
-(src/plume/add_pressure_ghost.cc:37-316) with initial_air
+(src/plume/add_pressure_ghost.cc:37-316) and add_wall_ghost
+(src/plume/add_wall_ghost.cc:44-293) with initial_air
 (src/plume/sph_lib.cc:831-866), air_prop_hydro (:543-592) and
 Particle::update_second_var (src/datstr/particle.cc:528-604), used by the
-tests only, as the checker of the device's plume_add_pressure_ghost.
+tests only, as the checker of the device's plume_add_pressure_ghost and
+plume_add_wall_ghost.
 
 For every bucket whose involvement state is NONE, that holds no pressure
 ghost and that has a neighbour (of the 26 inside the grid) whose state is
@@ -20,6 +22,11 @@ mass of its dx^3 box by the reference's three-point rule in z with the
 coefficients as written there (0.1666667, 0.6666666, 0.1666667); then the
 mixture EOS sets gamma, p, c, T and cp.
 
+add_wall_ghost: every on-ground MIXED bucket (bottom face below the
+ground) that holds particles but no wall ghost gets wall ghosts (bc 2) on
+the lattice points below the ground plane, and the bucket below it is made
+active and gets its whole lattice; same air state.
+
 Rows come out bucket by bucket in linear bucket order (x fastest), then by
 lattice index (i, j, k), k fastest.
 """
@@ -30,7 +37,7 @@ import math
 import numpy as np
 
 from .binding import ParticleSet  # noqa: F401  (sets sys.path)
-from plume_gpu.abi import (BC_PRESSURE, BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_PRESS_BC,
+from plume_gpu.abi import (BC_PRESSURE, BC_WALL, BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_PRESS_BC,
                            BUCKET_UNDERGROUND, Atmosphere, ParticleSet as PS)
 
 OVERGROUND, MIXED, UNDERGROUND, PRESS_BC = 3, 2, 1, 4
@@ -137,8 +144,7 @@ def add_pressure_ghost(grid, binv, ps, opt, atm: Atmosphere | None = None):
             continue
         lo = np.array([mind[0] + i * d, mind[1] + j * d, mind[2] + k * d])
         hi = np.array([mind[0] + (i + 1) * d, mind[1] + (j + 1) * d, mind[2] + (k + 1) * d])
-        # C round: halves away from zero (the quotients are positive)
-        n3 = [int(math.floor((hi[a] - lo[a]) / dx + 0.5)) for a in range(3)]
+        n3 = _lattice(lo, hi, dx)
         onground = typ[b] == MIXED and face[b, 4] == -1
         for qi in range(n3[0]):
             for qj in range(n3[1]):
@@ -147,6 +153,64 @@ def add_pressure_ghost(grid, binv, ps, opt, atm: Atmosphere | None = None):
                     if onground and not (c[2] > ground):
                         continue
                     rows.append(c)
+    return _air_particles(rows, BC_PRESSURE, dx, opt, atm), np.array(marked, dtype=np.int64)
+
+
+def _lattice(lo, hi, dx):
+    # C round: halves away from zero (the quotients are positive)
+    return [int(math.floor((hi[a] - lo[a]) / dx + 0.5)) for a in range(3)]
+
+
+def add_wall_ghost(grid, ps, opt, atm: Atmosphere | None = None):
+    """(new particles, buckets below that were marked active)"""
+    atm = atm or Atmosphere()
+    nb = np.array(grid.nb)
+    mind = np.array(grid.mindom, dtype=np.float64)
+    d = float(grid.del_)
+    flags = np.asarray(grid.flags, dtype=np.uint8)
+    face = np.asarray(grid.face_index, dtype=np.int8).reshape(-1, 6)
+    typ = bucket_types(flags, face)
+    pos = np.stack([ps.x, ps.y, ps.z], axis=1)
+    b3 = np.clip(np.floor((pos - mind) / d).astype(np.int64), 0, nb - 1)
+    pb = (b3[:, 2] * nb[1] + b3[:, 1]) * nb[0] + b3[:, 0]
+    count = np.bincount(pb, minlength=len(flags))
+    has_wg = np.zeros(len(flags), dtype=bool)
+    has_wg[pb[ps.bc_type == BC_WALL]] = True
+    dx = float(opt.sml_phase2)
+    dx2 = 0.5 * dx
+    ground = float(grid.domain_lo[2])
+    rows, marked = [], []
+
+    def corners(b):
+        i, j, k = b % nb[0], (b // nb[0]) % nb[1], b // (nb[0] * nb[1])
+        lo = np.array([mind[0] + i * d, mind[1] + j * d, mind[2] + k * d])
+        hi = np.array([mind[0] + (i + 1) * d, mind[1] + (j + 1) * d, mind[2] + (k + 1) * d])
+        return lo, hi
+    for b in range(len(flags)):
+        if not (typ[b] == MIXED and face[b, 4] == -1 and count[b] > 0 and not has_wg[b]):
+            continue
+        lo, hi = corners(b)
+        n3 = _lattice(lo, hi, dx)
+        for qi in range(n3[0]):
+            for qj in range(n3[1]):
+                for qk in range(n3[2]):
+                    c = (lo[0] + dx2 + qi * dx, lo[1] + dx2 + qj * dx, lo[2] + dx2 + qk * dx)
+                    if c[2] < ground:
+                        rows.append(c)
+        down = b - nb[0] * nb[1]
+        marked.append(down)
+        lo, hi = corners(down)
+        n3 = _lattice(lo, hi, dx)
+        for qi in range(n3[0]):
+            for qj in range(n3[1]):
+                for qk in range(n3[2]):
+                    rows.append((lo[0] + dx2 + qi * dx, lo[1] + dx2 + qj * dx, lo[2] + dx2 + qk * dx))
+    return _air_particles(rows, BC_WALL, dx, opt, atm), np.array(marked, dtype=np.int64)
+
+
+def _air_particles(rows, bc, dx, opt, atm):
+    """particles at rest at the given points with the state of initial_air
+    and the mixture EOS (Particle::update_second_var with Y = 0)"""
     n = len(rows)
     out = PS(n)
     if n:
@@ -154,7 +218,7 @@ def add_pressure_ghost(grid, binv, ps, opt, atm: Atmosphere | None = None):
         out.x, out.y, out.z = xyz[:, 0].copy(), xyz[:, 1].copy(), xyz[:, 2].copy()
     out.h[:] = dx
     out.phase[:] = 1
-    out.bc_type[:] = BC_PRESSURE
+    out.bc_type[:] = bc
     for r in range(n):
         rho, e, p, m = air_state(atm, out.x[r], out.y[r], out.z[r], dx)
         out.rho[r], out.e[r], out.mass[r] = rho, e, m
@@ -165,4 +229,4 @@ def add_pressure_ghost(grid, binv, ps, opt, atm: Atmosphere | None = None):
         out.c[r] = np.sqrt(out.gamma[r] * out.p[r] / rho)
         out.T[r] = e / cvm
         out.cp[r] = cvm if opt.lans else 0.0
-    return out, np.array(marked, dtype=np.int64)
+    return out

@@ -709,13 +709,15 @@ __device__ __forceinline__ double atm_p(const Atm& a, double h) {
   return a.AtC3 * pow(a.Atb3 * h + a.Ata3, a.Ate3);
 }
 
-// lattice of a bucket: points per axis (C round of edge / dx) and, in
-// on-ground MIXED buckets, the first z layer above the ground
+// lattice of a bucket: points per axis (C round of edge / dx) at corner +
+// dx/2 + i dx, restricted to the z layers [k0, k1)
 struct PgLattice {
   double lo[3];
-  int n[3], k0;
+  int n[3], k0, k1;
+  __device__ __forceinline__ uint32_t count() const { return (uint32_t)n[0] * (uint32_t)n[1] * (uint32_t)(k1 - k0); }
+  __device__ __forceinline__ double zk(int k, double dx) const { return lo[2] + 0.5 * dx + k * dx; }
 };
-__device__ __forceinline__ PgLattice pg_lattice(const Geo& g, int b, double dx, double ground, bool onground) {
+__device__ __forceinline__ PgLattice pg_lattice(const Geo& g, int b, double dx) {
   const int ijk[3] = {b % g.nb[0], (b / g.nb[0]) % g.nb[1], b / (g.nb[0] * g.nb[1])};
   PgLattice L;
   for (int a = 0; a < 3; a++) {
@@ -724,65 +726,113 @@ __device__ __forceinline__ PgLattice pg_lattice(const Geo& g, int b, double dx, 
     L.n[a] = (int)round((hi - L.lo[a]) / dx);
   }
   L.k0 = 0;
-  if (onground)
-    while (L.k0 < L.n[2] && !(L.lo[2] + 0.5 * dx + L.k0 * dx > ground)) L.k0++;
+  L.k1 = L.n[2];
   return L;
 }
-
-// One thread per bucket: a NONE bucket that holds no pressure ghost and has
-// a neighbour whose state is not NONE is marked and made active; its count
-// is its lattice (none for UNDERGROUND buckets)
-__global__ void k_pg_buckets(const Geo* __restrict__ geo, Dev A, const uint32_t* __restrict__ cs,
-                             const uint8_t* __restrict__ binv, uint8_t* __restrict__ bflags,
-                             const int8_t* __restrict__ bface, int nbk, int explicit_types, double dx,
-                             double ground, uint32_t* __restrict__ cnt, uint8_t* __restrict__ mark) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbk) return;
-  cnt[b] = 0;
-  mark[b] = 0;
-  if (binv[b] != PLUME_BINV_NONE) return;
-  const Geo& g = geo[0];
-  bool has_pg = false;
-  for_bucket_rows(g, cs, b, [&](uint32_t j0, uint32_t j1) {
-    for (uint32_t j = j0; j < j1 && !has_pg; j++) has_pg = A.bc[j] == PLUME_BC_PRESSURE;
-  });
-  if (has_pg) return;
-  if (!any_neighbour(g, b, [&](int nb) { return binv[nb] != PLUME_BINV_NONE; })) return;
-  mark[b] = 1;
-  const uint8_t f = bflags ? bflags[b] : 0;
-  if (bflags) bflags[b] = f & (uint8_t)~PLUME_BUCKET_INACTIVE;
-  const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
-  const int t = btype_of(f, fi, explicit_types);
-  if (t == 1) return;  // UNDERGROUND: none
-  const PgLattice L = pg_lattice(g, b, dx, ground, t == 3 && fi && fi[4] == -1);
-  cnt[b] = (uint32_t)L.n[0] * (uint32_t)L.n[1] * (uint32_t)(L.n[2] - L.k0);
+// points above the ground plane only (add_pressure_ghost.cc:165)
+__device__ __forceinline__ void pg_above(PgLattice& L, double dx, double ground) {
+  while (L.k0 < L.k1 && !(L.zk(L.k0, dx) > ground)) L.k0++;
+}
+// points below the ground plane only (add_wall_ghost.cc:165)
+__device__ __forceinline__ void pg_below(PgLattice& L, double dx, double ground) {
+  int k = 0;
+  while (k < L.n[2] && L.zk(k, dx) < ground) k++;
+  L.k1 = k;
 }
 
-// One block per bucket: its lattice points, k fastest, appended at row
-// base + offs[b]; state of initial_air (sph_lib.cc:831-866) and the EOS
+// The lattices a bucket fills.  kind 0, add_pressure_ghost
+// (add_pressure_ghost.cc:107-300): a NONE bucket that holds no pressure
+// ghost and has a neighbour whose state is not NONE is made active and fills
+// its lattice (on-ground MIXED: above the ground; UNDERGROUND: nothing).
+// kind 1, add_wall_ghost (add_wall_ghost.cc:124-285): an on-ground MIXED
+// bucket that holds particles but no wall ghost fills its lattice below the
+// ground, and the bucket below it is made active and filled whole.
+// Returns the number of lattices (0..2).
+__device__ __forceinline__ int pg_select(const Geo& g, const Dev& A, const uint32_t* __restrict__ cs,
+                                         const uint8_t* __restrict__ binv, const uint8_t* __restrict__ bflags,
+                                         const int8_t* __restrict__ bface, int explicit_types, int kind, int b,
+                                         double dx, double ground, PgLattice* L, int* activate) {
+  *activate = -1;
+  const uint8_t f = bflags ? bflags[b] : 0;
+  const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
+  const int t = btype_of(f, fi, explicit_types);
+  const bool onground = t == 3 && fi && fi[4] == -1;
+  const uint8_t ghost = kind == 0 ? PLUME_BC_PRESSURE : PLUME_BC_WALL;
+  if (kind == 0 && binv[b] != PLUME_BINV_NONE) return 0;
+  if (kind == 1 && !onground) return 0;
+  bool has = false;
+  uint32_t rows = 0;
+  for_bucket_rows(g, cs, b, [&](uint32_t j0, uint32_t j1) {
+    rows += j1 - j0;
+    for (uint32_t j = j0; j < j1 && !has; j++) has = A.bc[j] == ghost;
+  });
+  if (has) return 0;
+  if (kind == 0) {
+    if (!any_neighbour(g, b, [&](int nb) { return binv[nb] != PLUME_BINV_NONE; })) return 0;
+    *activate = b;
+    if (t == 1) return 0;  // UNDERGROUND: none
+    L[0] = pg_lattice(g, b, dx);
+    if (onground) pg_above(L[0], dx, ground);
+    return 1;
+  }
+  if (rows == 0) return 0;
+  L[0] = pg_lattice(g, b, dx);
+  pg_below(L[0], dx, ground);
+  const int down = b - g.nb[0] * g.nb[1];
+  if (down < 0) return 1;
+  *activate = down;
+  L[1] = pg_lattice(g, down, dx);
+  return 2;
+}
+
+// One thread per bucket: the count of its lattices; buckets to make active
+__global__ void k_pg_buckets(const Geo* __restrict__ geo, Dev A, const uint32_t* __restrict__ cs,
+                             const uint8_t* __restrict__ binv, uint8_t* __restrict__ bflags,
+                             const int8_t* __restrict__ bface, int nbk, int explicit_types, int kind, double dx,
+                             double ground, uint32_t* __restrict__ cnt) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbk) return;
+  PgLattice L[2];
+  int act;
+  const int nl = pg_select(geo[0], A, cs, binv, bflags, bface, explicit_types, kind, b, dx, ground, L, &act);
+  uint32_t c = 0;
+  for (int q = 0; q < nl; q++) c += L[q].count();
+  cnt[b] = c;
+  // the activated bucket is b itself (kind 0) or the one below an on-ground
+  // bucket (kind 1), which no other bucket activates; selection reads no
+  // activity bit, so the order of the writes does not matter
+  if (act >= 0 && bflags) bflags[act] &= (uint8_t)~PLUME_BUCKET_INACTIVE;
+}
+
+// One block per bucket: its points, lattice by lattice, k fastest, appended
+// at row base + offs[b]; state of initial_air (sph_lib.cc:831-866) and the EOS
 __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ mopt, Dev A,
-                          const uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface,
-                          int explicit_types, const uint32_t* __restrict__ cnt,
-                          const unsigned long long* __restrict__ offs, Atm atm, double dx, double ground,
-                          size_t base, unsigned long long key_base) {
+                          const uint32_t* __restrict__ cs, const uint8_t* __restrict__ binv,
+                          const uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface, int explicit_types,
+                          int kind, const uint32_t* __restrict__ cnt, const unsigned long long* __restrict__ offs,
+                          Atm atm, double dx, double ground, size_t base, unsigned long long key_base) {
   const int b = blockIdx.x;
   const uint32_t nq = cnt[b];
   if (nq == 0) return;
   const Geo& g = geo[0];
   const Opt& o = mopt[0];
-  const uint8_t f = bflags ? bflags[b] : 0;
-  const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
-  const int t = btype_of(f, fi, explicit_types);
-  const PgLattice L = pg_lattice(g, b, dx, ground, t == 3 && fi && fi[4] == -1);
-  const uint32_t nk = (uint32_t)(L.n[2] - L.k0);
+  PgLattice L[2];
+  int act;
+  const int nl = pg_select(g, A, cs, binv, bflags, bface, explicit_types, kind, b, dx, ground, L, &act);
+  const uint32_t c0 = nl > 0 ? L[0].count() : 0;
   const double dx2 = 0.5 * dx, s2 = 0.5 * dx;
+  const uint8_t bc = kind == 0 ? PLUME_BC_PRESSURE : PLUME_BC_WALL;
   for (uint32_t q = threadIdx.x; q < nq; q += blockDim.x) {
-    const uint32_t i = q / ((uint32_t)L.n[1] * nk);
-    const uint32_t j = (q / nk) % (uint32_t)L.n[1];
-    const uint32_t k = (uint32_t)L.k0 + q % nk;
-    const double x = L.lo[0] + dx2 + i * dx;
-    const double y = L.lo[1] + dx2 + j * dx;
-    const double z = L.lo[2] + dx2 + k * dx;
+    const bool second = q >= c0;
+    const PgLattice& M = second ? L[1] : L[0];
+    const uint32_t u = second ? q - c0 : q;
+    const uint32_t nk = (uint32_t)(M.k1 - M.k0);
+    const uint32_t i = u / ((uint32_t)M.n[1] * nk);
+    const uint32_t j = (u / nk) % (uint32_t)M.n[1];
+    const uint32_t k = (uint32_t)M.k0 + u % nk;
+    const double x = M.lo[0] + dx2 + i * dx;
+    const double y = M.lo[1] + dx2 + j * dx;
+    const double z = M.lo[2] + dx2 + k * dx;
     const double T = atm_T(atm, z);
     const double p0 = atm_p(atm, z);
     const double rho = p0 / (atm.Ra * T);
@@ -801,8 +851,8 @@ __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ m
     double gam, p, c, temp, cp = 0;
     eos(o, rho, 0.0, e, gam, p, c, temp, cp, o.lans != 0);
     A.gam[r] = gam; A.p[r] = p; A.c[r] = c; A.T[r] = temp; A.cp[r] = cp;
-    A.phase[r] = 1; A.bc[r] = PLUME_BC_PRESSURE; A.inv[r] = 0;
-    A.mem[r] = 0; A.bkt[r] = b;
+    A.phase[r] = 1; A.bc[r] = bc; A.inv[r] = 0;
+    A.mem[r] = 0; A.bkt[r] = second ? b - g.nb[0] * g.nb[1] : b;
   }
 }
 
@@ -2958,33 +3008,35 @@ int plume_adapt_domain(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
-int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
+// kind 0: add_pressure_ghost, kind 1: add_wall_ghost
+static int add_ghost_layers(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added, int kind) {
+  const char* name = kind == 0 ? "add_pressure_ghost" : "add_wall_ghost";
   if (!ctx || !atm || !added) return PLUME_E_INVALID;
   *added = 0;
   if (!ctx->binv) {
-    ctx->err = "add_pressure_ghost: 3D only";
+    ctx->err = std::string(name) + ": 3D only";
     return PLUME_E_INVALID;
   }
   if (ctx->nmem != 1) {
-    ctx->err = "add_pressure_ghost: single-run contexts only";
+    ctx->err = std::string(name) + ": single-run contexts only";
+    return PLUME_E_INVALID;
+  }
+  const double dx = ctx->opt.sml_phase2;
+  const double ground = ctx->hgeo[0].lo[2];
+  if (!(dx > 0) || ctx->hgeo[0].del / dx > 1024.0) {
+    ctx->err = std::string(name) + ": bucket edge / smoothing length must be in (0, 1024]";
     return PLUME_E_INVALID;
   }
   int rc = search(ctx);
   if (rc) return rc;
   cudaStream_t st = ctx->st;
   const int nbk = ctx->nbk;
-  const double dx = ctx->opt.sml_phase2;
-  const double ground = ctx->hgeo[0].lo[2];
-  if (!(dx > 0) || ctx->hgeo[0].del / dx > 1024.0) {
-    ctx->err = "add_pressure_ghost: bucket edge / smoothing length must be in (0, 1024]";
-    return PLUME_E_INVALID;
-  }
   uint32_t* cnt = nullptr;
   unsigned long long* offs = nullptr;
   CK(cudaMalloc(&cnt, 4 * (size_t)nbk));
   CK(cudaMalloc(&offs, 8 * (size_t)nbk));
   k_pg_buckets<<<nblocks(nbk), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->cs, ctx->binv, ctx->bflags, ctx->bface,
-                                                 nbk, ctx->explicit_types, dx, ground, cnt, ctx->bmark);
+                                                 nbk, ctx->explicit_types, kind, dx, ground, cnt);
   CK(cudaGetLastError());
   std::vector<uint32_t> hc((size_t)nbk);
   std::vector<unsigned long long> ho((size_t)nbk);
@@ -2998,15 +3050,16 @@ int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_
   if (ctx->n_alloc + tot > ctx->cap) {
     cudaFree(cnt);
     cudaFree(offs);
-    ctx->err = "add_pressure_ghost exceeds capacity";
+    ctx->err = std::string(name) + " exceeds capacity";
     return PLUME_E_CAPACITY;
   }
   if (tot) {
     CK(cudaMemcpyAsync(offs, ho.data(), 8 * (size_t)nbk, cudaMemcpyHostToDevice, st));
     const Atm a{atm->Ta0,  atm->pa0,  atm->Ra,   atm->gamma, atm->H1,   atm->H2,   atm->H3,   atm->miu1, atm->miu2,
                 atm->Ata1, atm->Ate1, atm->Ata2, atm->Atb2,  atm->Ata3, atm->Atb3, atm->AtC3, atm->Ate3};
-    k_pg_fill<<<nbk, 128, 0, st>>>(ctx->d_geo, ctx->d_opt, ctx->A, ctx->bflags, ctx->bface, ctx->explicit_types, cnt,
-                                  offs, a, dx, ground, ctx->n_alloc, (unsigned long long)key_base);
+    k_pg_fill<<<nbk, 128, 0, st>>>(ctx->d_geo, ctx->d_opt, ctx->A, ctx->cs, ctx->binv, ctx->bflags, ctx->bface,
+                                  ctx->explicit_types, kind, cnt, offs, a, dx, ground, ctx->n_alloc,
+                                  (unsigned long long)key_base);
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(st));
@@ -3020,6 +3073,14 @@ int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_
   }
   *added = (size_t)tot;
   return PLUME_OK;
+}
+
+int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
+  return add_ghost_layers(ctx, atm, key_base, added, 0);
+}
+
+int plume_add_wall_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
+  return add_ghost_layers(ctx, atm, key_base, added, 1);
 }
 
 // ---------------------------------------------------------------- GSPH

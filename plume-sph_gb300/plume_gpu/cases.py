@@ -394,6 +394,37 @@ def adapt_scenario(case, clear_beyond=False):
     return dataclasses.replace(case, grid=grid, particles=ps, name=case.name + "_adapt"), binv
 
 
+def wall_scenario(case):
+    """A wall-ghost set-up on a plume built by plume_3d: in the on-ground
+    MIXED buckets of the column of buckets second from the -x side of the
+    original domain, the wall ghosts are removed, and so is every particle
+    of the buckets below them, so that add_wall_ghost refills both.
+    Returns (new case, per-bucket involvement states: NONE where absorbing,
+    POTENTIAL elsewhere)."""
+    import dataclasses
+    g = case.grid
+    nb = np.array(g.nb)
+    flags = np.asarray(g.flags, dtype=np.uint8)
+    face = np.asarray(g.face_index, dtype=np.int8).reshape(-1, 6)
+    idx = np.arange(len(flags))
+    bx, by, bz = idx % nb[0], (idx // nb[0]) % nb[1], idx // (nb[0] * nb[1])
+    onground = ((flags & BUCKET_MIXED) != 0) & (face[:, 4] == -1)
+    col = int(bx[onground & (face[:, 0] == -1) & (face[:, 1] == 0)].min()) + 1
+    target = onground & (bx == col)
+    below = np.zeros(len(flags), dtype=bool)
+    for b in idx[target]:
+        if bz[b] > 0:
+            below[b - nb[0] * nb[1]] = True
+    ps = case.particles
+    pos = np.stack([ps.x, ps.y, ps.z], axis=1)
+    b3 = np.clip(np.floor((pos - np.array(g.mindom)) / g.del_).astype(np.int64), 0, nb - 1)
+    pb = (b3[:, 2] * nb[1] + b3[:, 1]) * nb[0] + b3[:, 0]
+    drop = (target[pb] & (ps.bc_type == BC_WALL)) | below[pb]
+    ps = ps.take(np.nonzero(~drop)[0])
+    binv = np.where((flags & BUCKET_ABSORBING) != 0, BINV_NONE, BINV_POTENTIAL).astype(np.uint8)
+    return dataclasses.replace(case, particles=ps, name=case.name + "_walls"), binv
+
+
 def inlet(case):
     """The eruption inlet of add_new_erupt (setup_erupt.cc:389-673) for a
     plume built by plume_3d: the duct's particle columns (spacing vent_dx,

@@ -213,6 +213,16 @@ class Solver:
                     "plume_add_pressure_ghost")
         return n.value
 
+    def add_wall_ghost(self, key_base: int, atmosphere=None) -> int:
+        """the wall-ghost layers of a grown domain (add_wall_ghost), on the
+        device; new keys from key_base; returns how many were added"""
+        from .abi import Atmosphere
+        a = (atmosphere or Atmosphere()).to_c()
+        n = C.c_size_t()
+        self._check(self.L.plume_add_wall_ghost(self.ctx, C.byref(a), int(key_base), C.byref(n)),
+                    "plume_add_wall_ghost")
+        return n.value
+
     # -- output snapshots -----------------------------------------------------
     def snapshot_begin(self, host: ParticleSet):
         """queue a copy of the current particles into host's arrays (the

@@ -160,3 +160,45 @@ def test_pressure_ghosts_need_a_3d_single_run():
     s = Solver(case)
     with pytest.raises(PlumeError):
         s.add_pressure_ghost(1 << 40)
+
+
+def test_wall_ghosts_match_reference():
+    """one step, then add_wall_ghost on the device (cases.wall_scenario):
+    the new wall ghosts are the reference's (tests/golden/wall_ghost_3d.npz,
+    matched by position; air state within 1e-14); two further steps agree
+    with the oracle, which appends the same particles"""
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    from oracle.ghosts import add_wall_ghost
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "wall_ghost_3d.npz")))
+    c, _ = cases.wall_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    c.options.capacity = c.particles.n + 10000
+    s = Solver(c)
+    s.steps(int(d["nsteps"]))
+    base = 1 << 41
+    added = s.add_wall_ghost(base)
+    ref = unpack(d, "born_")
+    assert added == ref.n > 1000
+    g = s.download()
+    new = g.take(np.nonzero(g.key >= base)[0])
+    a, b = _by_position(new), _by_position(ref)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "h", "Y"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in ("mass", "rho", "e", "p", "gamma", "c", "T", "cp"):
+        np.testing.assert_allclose(getattr(a, f), getattr(b, f), rtol=1e-14, atol=0, err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    assert s.add_wall_ghost(base + added) == 0  # the buckets hold wall ghosts now
+    o = OracleRun(c)
+    o.steps(1)
+    extra, _ = add_wall_ghost(c.grid, o.ps, c.options)
+    pos = {(x, y, z): k for x, y, z, k in zip(new.x, new.y, new.z, new.key)}
+    extra.key = np.array([pos[(x, y, z)] for x, y, z in zip(extra.x, extra.y, extra.z)], dtype=np.uint64)
+    o.append(extra)
+    s.steps(2)
+    o.steps(2)
+    gs, os_ = s.download().sorted_by_key(), o.ps.sorted_by_key()
+    np.testing.assert_array_equal(gs.key, os_.key)
+    for f in DOUBLE_FIELDS:
+        x, y = getattr(gs, f), getattr(os_, f)
+        assert np.abs(x - y).max() <= 1e-10 * max(np.abs(y).max(), 1e-300), f

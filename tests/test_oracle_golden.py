@@ -319,3 +319,24 @@ def test_oracle_pressure_ghosts_after_adaptation_match_reference():
     for f in BYTE_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
     assert np.all(d["active"] == 1) and len(marked) > 0
+
+
+def test_oracle_wall_ghosts_match_reference():
+    """one step, then add_wall_ghost on cases.wall_scenario: the oracle's
+    new wall ghosts (oracle/ghosts.py) are the reference's, bit for bit"""
+    from _util import adapt_case
+    from oracle.ghosts import add_wall_ghost
+    d = dict(np.load(os.path.join(GOLDEN, "wall_ghost_3d.npz")))
+    c, binv = cases.wall_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    np.testing.assert_array_equal(binv, d["binv_in"])
+    o = OracleRun(c)
+    o.steps(int(d["nsteps"]))
+    new, marked = add_wall_ghost(c.grid, o.ps, c.options)
+    ref = unpack(d, "born_")
+    assert new.n == ref.n > 1000 and len(marked) > 0
+    a, b = _by_position(new), _by_position(ref)
+    for f in DOUBLE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
