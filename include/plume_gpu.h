@@ -436,6 +436,15 @@ int plume_batch_run(plume_ctx *ctx, int max_steps, int graph_steps, int *steps_d
  * reference writes at the end of the last step).  3D, keys unique in the
  * context; the adjoint entry points reject a context with images. */
 int plume_set_wall_images(plume_ctx *ctx, const uint64_t *ghost_keys, const double *image_xyz, size_t n);
+
+/* The image table of search_bnd_images (bnd_image.cc:36-245) for a flat
+ * ground, found on the device from the current particles and installed as
+ * plume_set_wall_images would: every wall ghost (bc 2) of a MIXED bucket
+ * whose own bucket or a neighbour is an on-ground MIXED bucket (bottom face
+ * below the ground plane, top face not) gets the image (x, y, 2 z_ground -
+ * z).  *n = the number of images.  Single-run 3D contexts.  Call it after
+ * the wall ghosts change (plume_add_wall_ghost, plume_append). */
+int plume_search_bnd_images(plume_ctx *ctx, size_t *n);
 int plume_apply_bcond(plume_ctx *ctx);
 
 /* ---------------------------------------------------------------- eruption inlet

@@ -856,6 +856,42 @@ __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ m
   }
 }
 
+// search_bnd_images (bnd_image.cc:36-245) for a flat ground: a wall ghost
+// of a MIXED bucket whose own bucket or one of its 26 neighbours is an
+// on-ground MIXED bucket (bottom face below the ground, top face not,
+// bucket.h:524-527) is mirrored in the ground plane, image = 2 intsct - x
+// with intsct = (x, y, z_ground) (Bucket::calc_intersection_ground for flat
+// ground, bucket.cc:346-354); ghosts farther from the ground than the
+// domain's height are skipped (bnd_image.cc:146-150)
+__global__ void k_find_images(const Geo* __restrict__ geo, Dev A, const int* __restrict__ d_count,
+                              const uint8_t* __restrict__ bflags, const int8_t* __restrict__ bface,
+                              int explicit_types, double zmax_dist, unsigned long long* __restrict__ okey,
+                              double* __restrict__ oxyz, unsigned int* __restrict__ ocount, unsigned int cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count || A.bc[i] != PLUME_BC_WALL) return;
+  const Geo& g = geo[0];
+  const int b = A.bkt[i];
+  auto onground_mixed = [&](int q) {
+    const uint8_t f = bflags ? bflags[q] : 0;
+    const int8_t* fi = bface ? bface + 6 * (size_t)q : nullptr;
+    return btype_of(f, fi, explicit_types) == 3 && fi && fi[4] == -1 && fi[5] == 0;
+  };
+  {
+    const uint8_t f = bflags ? bflags[b] : 0;
+    if (btype_of(f, bface ? bface + 6 * (size_t)b : nullptr, explicit_types) != 3) return;
+  }
+  if (!onground_mixed(b) && !any_neighbour(g, b, onground_mixed)) return;
+  const double zg = g.lo[2];
+  const double z = A.z[i];
+  if (fabs(z - zg) > zmax_dist) return;
+  const unsigned int slot = atomicAdd(ocount, 1u);
+  if (slot >= cap) return;
+  okey[slot] = A.key[i];
+  oxyz[3 * (size_t)slot] = A.x[i];
+  oxyz[3 * (size_t)slot + 1] = A.y[i];
+  oxyz[3 * (size_t)slot + 2] = 2 * zg - z;
+}
+
 // adapt_domain, particles of the converted buckets: real (100) and
 // potentially involved (1) -- on-ground MIXED buckets their pressure ghosts,
 // other MIXED buckets those inside the domain (determine_escape), OVERGROUND
@@ -3152,6 +3188,51 @@ int plume_set_wall_images(plume_ctx* ctx, const uint64_t* ghost_keys, const doub
   if ((size_t)ctx->nmem * n > (size_t)0x7fffffff) return PLUME_E_CAPACITY;
   CK(cudaMalloc(&ctx->bc_map, sizeof(int) * (size_t)ctx->nmem * n));
   ctx->nimg = (int)n;
+  return PLUME_OK;
+}
+
+int plume_search_bnd_images(plume_ctx* ctx, size_t* n_out) {
+  if (!ctx || !n_out) return PLUME_E_INVALID;
+  *n_out = 0;
+  if (ctx->o.dim != 3 || ctx->nmem != 1) {
+    ctx->err = "search_bnd_images: single-run 3D contexts only";
+    return PLUME_E_INVALID;
+  }
+  int rc = search(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->st;
+  const Geo& g = ctx->hgeo[0];
+  const double zmax = g.mind[2] + g.nb[2] * g.del - g.mind[2];  // len_domain in z
+  const unsigned int cap = (unsigned int)std::min<size_t>(ctx->n_alloc ? ctx->n_alloc : 1, 0x7fffffff);
+  unsigned long long* dk = nullptr;
+  double* dx = nullptr;
+  unsigned int* dn = nullptr;
+  CK(cudaMalloc(&dk, 8 * (size_t)cap));
+  CK(cudaMalloc(&dx, 24 * (size_t)cap));
+  CK(cudaMalloc(&dn, sizeof(unsigned int)));
+  CK(cudaMemsetAsync(dn, 0, sizeof(unsigned int), st));
+  const int n = (int)ctx->n_alloc;
+  k_find_images<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->bflags, ctx->bface,
+                                                         ctx->explicit_types, zmax, dk, dx, dn, cap);
+  ctx->launches++;
+  CK(cudaGetLastError());
+  unsigned int cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, dn, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  cnt = std::min(cnt, cap);
+  std::vector<uint64_t> k(cnt);
+  std::vector<double> x(3 * (size_t)cnt);
+  if (cnt) {
+    CK(cudaMemcpyAsync(k.data(), dk, 8 * (size_t)cnt, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(x.data(), dx, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  cudaFree(dk);
+  cudaFree(dx);
+  cudaFree(dn);
+  rc = plume_set_wall_images(ctx, k.data(), x.data(), cnt);
+  if (rc) return rc;
+  *n_out = cnt;
   return PLUME_OK;
 }
 

@@ -223,6 +223,14 @@ class Solver:
                     "plume_add_wall_ghost")
         return n.value
 
+    def search_bnd_images(self) -> int:
+        """the wall-image table of search_bnd_images (flat ground), found on
+        the device from the current wall ghosts and installed; returns the
+        number of images"""
+        n = C.c_size_t()
+        self._check(self.L.plume_search_bnd_images(self.ctx, C.byref(n)), "plume_search_bnd_images")
+        return n.value
+
     # -- output snapshots -----------------------------------------------------
     def snapshot_begin(self, host: ParticleSet):
         """queue a copy of the current particles into host's arrays (the

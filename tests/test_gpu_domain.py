@@ -202,3 +202,39 @@ def test_wall_ghosts_match_reference():
     for f in DOUBLE_FIELDS:
         x, y = getattr(gs, f), getattr(os_, f)
         assert np.abs(x - y).max() <= 1e-10 * max(np.abs(y).max(), 1e-300), f
+
+
+def test_device_image_search_equals_host_table():
+    """plume_search_bnd_images on the wall-boundary plume finds the table of
+    cases.wall_images (the fixture's images): same count, and a run with
+    either table computes the same bits through apply_bcond and two steps"""
+    from _util import golden_case
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    case, d = golden_case("plume_3d_bc")
+    a = Solver(case)
+    a.set_wall_images(d["img_key"], d["img_xyz"])
+    b = Solver(case)
+    assert b.search_bnd_images() == len(d["img_key"]) > 1000
+    for s in (a, b):
+        s.apply_bcond()
+        s.steps(2)
+    ga, gb = a.download().sorted_by_key(), b.download().sorted_by_key()
+    for f in DOUBLE_FIELDS + BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(ga, f), getattr(gb, f), err_msg=f)
+
+
+def test_device_image_search_after_wall_ghosts():
+    """after add_wall_ghost the device search finds the images of the new
+    wall ghosts too: the count of cases.wall_images on the new table"""
+    import dataclasses
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "wall_ghost_3d.npz")))
+    c, _ = cases.wall_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    c.options.capacity = c.particles.n + 10000
+    s = Solver(c)
+    s.steps(1)
+    before = s.search_bnd_images()
+    s.add_wall_ghost(1 << 41)
+    after = s.search_bnd_images()
+    keys, _ = cases.wall_images(dataclasses.replace(c, particles=s.download()))
+    assert after == len(keys) > before
