@@ -362,6 +362,16 @@ int plume_add_pressure_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_
  * state, keys and errors as plume_add_pressure_ghost. */
 int plume_add_wall_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base, size_t *added);
 
+/* The adaptation block of the 3D loop (main.cc:257-295) in one call:
+ * plume_scan_outside_layer; when it asks for it (*adapted != 0),
+ * plume_adapt_domain, plume_add_pressure_ghost, plume_add_wall_ghost (keys
+ * from key_base on, *added in all) and, when wall images are in use,
+ * plume_search_bnd_images and plume_apply_bcond.  (move_data,
+ * shift_brief_buck and update_bgmesh have nothing to do in a one-GPU
+ * table.) */
+int plume_adapt_step(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base, int *adapted,
+                     size_t *added);
+
 /* Per-phase device time of the last plume_step/plume_steps call, summed over
  * its steps, in ms (CUDA events on the context's stream):
  * [0] search (keys, sort, gather, cell table), [1] adaptive h, [2] bucket

@@ -3236,6 +3236,34 @@ int plume_search_bnd_images(plume_ctx* ctx, size_t* n_out) {
   return PLUME_OK;
 }
 
+int plume_adapt_step(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, int* adapted,
+                     size_t* added) {
+  if (!ctx || !atm || !adapted || !added) return PLUME_E_INVALID;
+  *adapted = 0;
+  *added = 0;
+  int a = 0;
+  int rc = plume_scan_outside_layer(ctx, &a);
+  if (rc) return rc;
+  *adapted = a;
+  if (!a) return PLUME_OK;
+  rc = plume_adapt_domain(ctx);
+  if (rc) return rc;
+  size_t n1 = 0, n2 = 0;
+  rc = plume_add_pressure_ghost(ctx, atm, key_base, &n1);
+  if (rc) return rc;
+  rc = plume_add_wall_ghost(ctx, atm, key_base + n1, &n2);
+  if (rc) return rc;
+  *added = n1 + n2;
+  if (ctx->nimg) {  // the wall boundary is in use: new ghosts need images
+    size_t ni = 0;
+    rc = plume_search_bnd_images(ctx, &ni);
+    if (rc) return rc;
+    rc = plume_apply_bcond(ctx);
+    if (rc) return rc;
+  }
+  return PLUME_OK;
+}
+
 int plume_apply_bcond(plume_ctx* ctx) {
   if (!ctx) return PLUME_E_INVALID;
   if (!ctx->nimg) return PLUME_OK;

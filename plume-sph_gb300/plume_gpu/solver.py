@@ -231,6 +231,17 @@ class Solver:
         self._check(self.L.plume_search_bnd_images(self.ctx, C.byref(n)), "plume_search_bnd_images")
         return n.value
 
+    def adapt_step(self, key_base: int, atmosphere=None):
+        """the adaptation block of the 3D loop (scan, adapt_domain, both
+        ghost layers, the image table when wall images are in use);
+        returns (the scan's count, particles added)"""
+        from .abi import Atmosphere
+        a = (atmosphere or Atmosphere()).to_c()
+        ad, n = C.c_int(), C.c_size_t()
+        self._check(self.L.plume_adapt_step(self.ctx, C.byref(a), int(key_base), C.byref(ad), C.byref(n)),
+                    "plume_adapt_step")
+        return ad.value, n.value
+
     # -- output snapshots -----------------------------------------------------
     def snapshot_begin(self, host: ParticleSet):
         """queue a copy of the current particles into host's arrays (the

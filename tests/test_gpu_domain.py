@@ -238,3 +238,35 @@ def test_device_image_search_after_wall_ghosts():
     after = s.search_bnd_images()
     keys, _ = cases.wall_images(dataclasses.replace(c, particles=s.download()))
     assert after == len(keys) > before
+
+
+def test_adapt_step_equals_the_calls_in_order():
+    """plume_adapt_step on the pressure-ghost set-up with wall images in
+    use equals scan, adapt_domain, both ghost layers, the image search and
+    apply_bcond called one by one, bit for bit, through two more steps"""
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    c, d = _pg_fixture()
+    c.options.capacity = c.particles.n + 60000
+    keys, xyz = cases.wall_images(c)
+    runs = []
+    for one_call in (True, False):
+        s = Solver(c)
+        s.set_wall_images(keys, xyz)
+        s.set_bucket_involvement(d["binv_in"])
+        s.steps(1)
+        if one_call:
+            adapted, added = s.adapt_step(1 << 40)
+        else:
+            adapted = s.scan_outside_layer()
+            s.adapt_domain()
+            added = s.add_pressure_ghost(1 << 40)
+            added += s.add_wall_ghost((1 << 40) + added)
+            s.search_bnd_images()
+            s.apply_bcond()
+        assert adapted == int(d["adapt"]) and added >= int(d["born_x"].size)
+        s.steps(2)
+        runs.append((s, s.download().sorted_by_key()))
+    (s, a), (_, b) = runs
+    for f in DOUBLE_FIELDS + BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    np.testing.assert_array_equal(a.key, b.key)
