@@ -362,6 +362,14 @@ int plume_add_pressure_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_
  * state, keys and errors as plume_add_pressure_ghost. */
 int plume_add_wall_ghost(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base, size_t *added);
 
+/* The air of add_air (add_air.cc:490-795, 3D), on the device: every empty
+ * bucket whose involvement state is not NONE is made active; MIXED and
+ * OVERGROUND ones are filled with real air particles (bc 100, potentially
+ * involved) on the lattice of plume_add_pressure_ghost (on-ground MIXED:
+ * above the ground only), PRESS_BC and UNDERGROUND ones stay empty.  State,
+ * keys and errors as plume_add_pressure_ghost. */
+int plume_add_air(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_base, size_t *added);
+
 /* The adaptation block of the 3D loop (main.cc:257-295) in one call:
  * plume_scan_outside_layer; when it asks for it (*adapted != 0),
  * plume_adapt_domain, plume_add_pressure_ghost, plume_add_wall_ghost (keys

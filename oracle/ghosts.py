@@ -37,7 +37,7 @@ import math
 import numpy as np
 
 from .binding import ParticleSet  # noqa: F401  (sets sys.path)
-from plume_gpu.abi import (BC_PRESSURE, BC_WALL, BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_PRESS_BC,
+from plume_gpu.abi import (BC_PRESSURE, BC_REAL, BC_WALL, BUCKET_ABSORBING, BUCKET_MIXED, BUCKET_PRESS_BC,
                            BUCKET_UNDERGROUND, Atmosphere, ParticleSet as PS)
 
 OVERGROUND, MIXED, UNDERGROUND, PRESS_BC = 3, 2, 1, 4
@@ -206,6 +206,51 @@ def add_wall_ghost(grid, ps, opt, atm: Atmosphere | None = None):
                 for qk in range(n3[2]):
                     rows.append((lo[0] + dx2 + qi * dx, lo[1] + dx2 + qj * dx, lo[2] + dx2 + qk * dx))
     return _air_particles(rows, BC_WALL, dx, opt, atm), np.array(marked, dtype=np.int64)
+
+
+def add_air(grid, binv, ps, opt, atm: Atmosphere | None = None):
+    """(new particles, buckets marked active): add_air (add_air.cc:490-795)
+    fills every empty bucket whose involvement state is not NONE -- MIXED
+    buckets on or below the ground above the ground plane only, other MIXED
+    and OVERGROUND buckets whole, PRESS_BC and UNDERGROUND buckets not at
+    all -- with real air (bc 100, potentially involved)"""
+    atm = atm or Atmosphere()
+    nb = np.array(grid.nb)
+    mind = np.array(grid.mindom, dtype=np.float64)
+    d = float(grid.del_)
+    flags = np.asarray(grid.flags, dtype=np.uint8)
+    face = np.asarray(grid.face_index, dtype=np.int8).reshape(-1, 6)
+    typ = bucket_types(flags, face)
+    binv = np.asarray(binv, dtype=np.uint8)
+    pos = np.stack([ps.x, ps.y, ps.z], axis=1)
+    b3 = np.clip(np.floor((pos - mind) / d).astype(np.int64), 0, nb - 1)
+    pb = (b3[:, 2] * nb[1] + b3[:, 1]) * nb[0] + b3[:, 0]
+    count = np.bincount(pb, minlength=len(flags))
+    dx = float(opt.sml_phase2)
+    dx2 = 0.5 * dx
+    ground = float(grid.domain_lo[2])
+    rows, marked = [], []
+    for b in range(len(flags)):
+        if binv[b] == 0 or count[b] > 0:
+            continue
+        marked.append(b)
+        if typ[b] not in (MIXED, OVERGROUND):
+            continue
+        i, j, k = b % nb[0], (b // nb[0]) % nb[1], b // (nb[0] * nb[1])
+        lo = np.array([mind[0] + i * d, mind[1] + j * d, mind[2] + k * d])
+        hi = np.array([mind[0] + (i + 1) * d, mind[1] + (j + 1) * d, mind[2] + (k + 1) * d])
+        n3 = _lattice(lo, hi, dx)
+        onground = typ[b] == MIXED and face[b, 4] == -1
+        for qi in range(n3[0]):
+            for qj in range(n3[1]):
+                for qk in range(n3[2]):
+                    c = (lo[0] + dx2 + qi * dx, lo[1] + dx2 + qj * dx, lo[2] + dx2 + qk * dx)
+                    if onground and not (c[2] > ground):
+                        continue
+                    rows.append(c)
+    out = _air_particles(rows, BC_REAL, dx, opt, atm)
+    out.involved[:] = 1
+    return out, np.array(marked, dtype=np.int64)
 
 
 def _air_particles(rows, bc, dx, opt, atm):

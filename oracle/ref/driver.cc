@@ -71,7 +71,8 @@ struct Case {
   std::vector<double> img_xyz;
   std::vector<uint8_t> binv;  // per-bucket has_involved (optional)
   int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop,
-                              // 2: then add_pressure_ghost, 3: add_wall_ghost alone
+                              // 2: then add_pressure_ghost, 3: add_wall_ghost alone,
+                              // 4: add_air alone
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -547,9 +548,13 @@ int main(int argc, char **argv) {
   // then adapt_domain when it asks for it; the particles after it are an
   // extra dumped record
   int adapt_n = 0;
-  if (c.adapt_mode == 3) {
-    // the wall-ghost layers of add_wall_ghost alone (main.cc:279)
-    add_wall_ghost(P, BG, simprops, matprops, tp, 1, 0);
+  if (c.adapt_mode == 3 || c.adapt_mode == 4) {
+    // the wall-ghost layers of add_wall_ghost alone (main.cc:279), or the
+    // air of add_air in the empty buckets (add_air.cc:490-795)
+    if (c.adapt_mode == 3)
+      add_wall_ghost(P, BG, simprops, matprops, tp, 1, 0);
+    else
+      add_air(P, BG, matprops, simprops, 1, 0);
     dump_state(fo, P, c, *tp, 0.0);
     ndumped++;
   } else if (c.adapt_mode) {

@@ -746,8 +746,8 @@ __device__ __forceinline__ void pg_below(PgLattice& L, double dx, double ground)
 // its lattice (on-ground MIXED: above the ground; UNDERGROUND: nothing).
 // kind 1, add_wall_ghost (add_wall_ghost.cc:124-285): an on-ground MIXED
 // bucket that holds particles but no wall ghost fills its lattice below the
-// ground, and the bucket below it is made active and filled whole.
-// Returns the number of lattices (0..2).
+// ground, and the bucket below it is made active and filled whole.  kind
+// 2, add_air: below.  Returns the number of lattices (0..2).
 __device__ __forceinline__ int pg_select(const Geo& g, const Dev& A, const uint32_t* __restrict__ cs,
                                          const uint8_t* __restrict__ binv, const uint8_t* __restrict__ bflags,
                                          const int8_t* __restrict__ bface, int explicit_types, int kind, int b,
@@ -757,6 +757,17 @@ __device__ __forceinline__ int pg_select(const Geo& g, const Dev& A, const uint3
   const int8_t* fi = bface ? bface + 6 * (size_t)b : nullptr;
   const int t = btype_of(f, fi, explicit_types);
   const bool onground = t == 3 && fi && fi[4] == -1;
+  if (kind == 2) {
+    // add_air (add_air.cc:490-795): an empty bucket whose state is not NONE
+    // is made active; MIXED and OVERGROUND buckets fill their lattice (on
+    // or below the ground: above the ground plane only)
+    if (binv[b] == PLUME_BINV_NONE || bucket_count(g, cs, b) > 0) return 0;
+    *activate = b;
+    if (t != 3 && t != 4) return 0;
+    L[0] = pg_lattice(g, b, dx);
+    if (onground) pg_above(L[0], dx, ground);
+    return 1;
+  }
   const uint8_t ghost = kind == 0 ? PLUME_BC_PRESSURE : PLUME_BC_WALL;
   if (kind == 0 && binv[b] != PLUME_BINV_NONE) return 0;
   if (kind == 1 && !onground) return 0;
@@ -821,7 +832,8 @@ __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ m
   const int nl = pg_select(g, A, cs, binv, bflags, bface, explicit_types, kind, b, dx, ground, L, &act);
   const uint32_t c0 = nl > 0 ? L[0].count() : 0;
   const double dx2 = 0.5 * dx, s2 = 0.5 * dx;
-  const uint8_t bc = kind == 0 ? PLUME_BC_PRESSURE : PLUME_BC_WALL;
+  const uint8_t bc = kind == 0 ? PLUME_BC_PRESSURE : (kind == 1 ? PLUME_BC_WALL : PLUME_BC_REAL);
+  const uint8_t inv = kind == 2 ? 1 : 0;  // add_air: potentially involved
   for (uint32_t q = threadIdx.x; q < nq; q += blockDim.x) {
     const bool second = q >= c0;
     const PgLattice& M = second ? L[1] : L[0];
@@ -851,7 +863,7 @@ __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ m
     double gam, p, c, temp, cp = 0;
     eos(o, rho, 0.0, e, gam, p, c, temp, cp, o.lans != 0);
     A.gam[r] = gam; A.p[r] = p; A.c[r] = c; A.T[r] = temp; A.cp[r] = cp;
-    A.phase[r] = 1; A.bc[r] = bc; A.inv[r] = 0;
+    A.phase[r] = 1; A.bc[r] = bc; A.inv[r] = inv;
     A.mem[r] = 0; A.bkt[r] = second ? b - g.nb[0] * g.nb[1] : b;
   }
 }
@@ -3044,9 +3056,9 @@ int plume_adapt_domain(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
-// kind 0: add_pressure_ghost, kind 1: add_wall_ghost
+// kind 0: add_pressure_ghost, kind 1: add_wall_ghost, kind 2: add_air
 static int add_ghost_layers(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added, int kind) {
-  const char* name = kind == 0 ? "add_pressure_ghost" : "add_wall_ghost";
+  const char* name = kind == 0 ? "add_pressure_ghost" : (kind == 1 ? "add_wall_ghost" : "add_air");
   if (!ctx || !atm || !added) return PLUME_E_INVALID;
   *added = 0;
   if (!ctx->binv) {
@@ -3117,6 +3129,10 @@ int plume_add_pressure_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_
 
 int plume_add_wall_ghost(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
   return add_ghost_layers(ctx, atm, key_base, added, 1);
+}
+
+int plume_add_air(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t key_base, size_t* added) {
+  return add_ghost_layers(ctx, atm, key_base, added, 2);
 }
 
 // ---------------------------------------------------------------- GSPH

@@ -101,6 +101,7 @@ def lib():
                                           P(C.c_uint8), P(C.c_int8), C.c_size_t, P(C.c_size_t)]
         L.plume_add_pressure_ghost.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
         L.plume_add_wall_ghost.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
+        L.plume_add_air.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
         L.plume_search_bnd_images.argtypes = [C.c_void_p, P(C.c_size_t)]
         L.plume_adapt_step.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_int), P(C.c_size_t)]
         L.plume_snapshot_end.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_double), P(C.c_int)]

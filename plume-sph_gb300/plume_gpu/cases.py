@@ -425,6 +425,35 @@ def wall_scenario(case):
     return dataclasses.replace(case, particles=ps, name=case.name + "_walls"), binv
 
 
+def air_scenario(case):
+    """An add_air set-up on a plume built by plume_3d: every particle of a
+    block of buckets is removed -- 2 x 2 buckets across, from the ground
+    up through three layers, in the +x +y quarter next to the vent axis
+    (on-ground MIXED and OVERGROUND buckets) -- so that add_air refills
+    them.  Returns (new case, per-bucket involvement states: NONE where
+    absorbing, POTENTIAL elsewhere)."""
+    import dataclasses
+    g = case.grid
+    nb = np.array(g.nb)
+    flags = np.asarray(g.flags, dtype=np.uint8)
+    face = np.asarray(g.face_index, dtype=np.int8).reshape(-1, 6)
+    idx = np.arange(len(flags))
+    bx, by, bz = idx % nb[0], (idx // nb[0]) % nb[1], idx // (nb[0] * nb[1])
+    mind = np.array(g.mindom)
+    cx = int(np.floor((0.0 - mind[0]) / g.del_)) + 1
+    cy = int(np.floor((0.0 - mind[1]) / g.del_)) + 1
+    k0 = int(bz[(face[:, 4] == -1) & (face[:, 5] == 0)].min())
+    block = ((bx >= cx) & (bx < cx + 2) & (by >= cy) & (by < cy + 2) & (bz >= k0) & (bz < k0 + 3)
+             & ((flags & BUCKET_ABSORBING) == 0))
+    ps = case.particles
+    pos = np.stack([ps.x, ps.y, ps.z], axis=1)
+    b3 = np.clip(np.floor((pos - mind) / g.del_).astype(np.int64), 0, nb - 1)
+    pb = (b3[:, 2] * nb[1] + b3[:, 1]) * nb[0] + b3[:, 0]
+    ps = ps.take(np.nonzero(~block[pb])[0])
+    binv = np.where((flags & BUCKET_ABSORBING) != 0, BINV_NONE, BINV_POTENTIAL).astype(np.uint8)
+    return dataclasses.replace(case, particles=ps, name=case.name + "_air"), binv
+
+
 def inlet(case):
     """The eruption inlet of add_new_erupt (setup_erupt.cc:389-673) for a
     plume built by plume_3d: the duct's particle columns (spacing vent_dx,

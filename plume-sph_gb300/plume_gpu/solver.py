@@ -223,6 +223,15 @@ class Solver:
                     "plume_add_wall_ghost")
         return n.value
 
+    def add_air(self, key_base: int, atmosphere=None) -> int:
+        """the air of add_air in the empty buckets, on the device; new keys
+        from key_base; returns how many particles were added"""
+        from .abi import Atmosphere
+        a = (atmosphere or Atmosphere()).to_c()
+        n = C.c_size_t()
+        self._check(self.L.plume_add_air(self.ctx, C.byref(a), int(key_base), C.byref(n)), "plume_add_air")
+        return n.value
+
     def search_bnd_images(self) -> int:
         """the wall-image table of search_bnd_images (flat ground), found on
         the device from the current wall ghosts and installed; returns the

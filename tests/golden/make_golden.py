@@ -145,6 +145,7 @@ def main():
     make_adapt()
     make_adapt_pg()
     make_wall_ghost()
+    make_air()
     make_csv()
     make_grid()
 
@@ -232,6 +233,22 @@ def make_wall_ghost():
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def make_air():
+    """add_air_3d.npz: cases.air_scenario on the domain-growth plume (seed
+    6): one step, then the reference's add_air.  Stores the input, flags and
+    involvement states, and the particles add_air created."""
+    c, binv = cases.air_scenario(adapt_case())
+    steps, _ = refio.run_ref("ref3d_adapt", c, 1, "/tmp/plume_golden", binv=binv, adapt=4)
+    d = {"nsteps": 1, "step0": c.step0, "pre_adaptive": 0, "dim": 3,
+         "flags": np.asarray(c.grid.flags, dtype=np.uint8), "binv_in": binv,
+         "active": steps[-1]["active"]}
+    d.update(pack("in_", c.particles))
+    d.update(pack("born_", steps[-1]["born"]))
+    path = os.path.join(HERE, "add_air_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 GRID_DOMAINS = (
     # (name, lo, hi, h0, nproc): the 20 km plume domain at 150 m, the 600 m
     # test plume at 50 m, and a ragged domain above 1.5 km (bucket counts
@@ -293,6 +310,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--air":
+        refio.build_ref()
+        make_air()
     elif len(sys.argv) > 1 and sys.argv[1] == "--wall-ghost":
         refio.build_ref()
         make_wall_ghost()

@@ -270,3 +270,47 @@ def test_adapt_step_equals_the_calls_in_order():
     for f in DOUBLE_FIELDS + BYTE_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
     np.testing.assert_array_equal(a.key, b.key)
+
+
+def test_add_air_matches_reference():
+    """one step, then add_air on the device (cases.air_scenario): the new
+    air particles are the reference's (tests/golden/add_air_3d.npz, matched
+    by position; air state within 1e-14); a second call adds nothing; two
+    further steps agree with the oracle, which appends the same particles"""
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    from oracle.ghosts import add_air
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "add_air_3d.npz")))
+    c, binv = cases.air_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    c.options.capacity = c.particles.n + 10000
+    s = Solver(c)
+    s.set_bucket_involvement(binv)
+    s.steps(int(d["nsteps"]))
+    base = 1 << 42
+    added = s.add_air(base)
+    ref = unpack(d, "born_")
+    assert added == ref.n > 1000
+    g = s.download()
+    new = g.take(np.nonzero(g.key >= base)[0])
+    a, b = _by_position(new), _by_position(ref)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "h", "Y"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in ("mass", "rho", "e", "p", "gamma", "c", "T", "cp"):
+        np.testing.assert_allclose(getattr(a, f), getattr(b, f), rtol=1e-14, atol=0, err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    assert s.add_air(base + added) == 0
+    o = OracleRun(c)
+    o.steps(1)
+    extra, _ = add_air(c.grid, binv, o.ps, c.options)
+    pos = {(x, y, z): k for x, y, z, k in zip(new.x, new.y, new.z, new.key)}
+    extra.key = np.array([pos[(x, y, z)] for x, y, z in zip(extra.x, extra.y, extra.z)], dtype=np.uint64)
+    o.append(extra)
+    s.steps(2)
+    o.steps(2)
+    gs, os_ = s.download().sorted_by_key(), o.ps.sorted_by_key()
+    np.testing.assert_array_equal(gs.key, os_.key)
+    np.testing.assert_array_equal(gs.bc_type, os_.bc_type)
+    for f in DOUBLE_FIELDS:
+        x, y = getattr(gs, f), getattr(os_, f)
+        assert np.abs(x - y).max() <= 1e-10 * max(np.abs(y).max(), 1e-300), f

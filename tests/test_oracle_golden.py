@@ -340,3 +340,24 @@ def test_oracle_wall_ghosts_match_reference():
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
     for f in BYTE_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+
+
+def test_oracle_add_air_matches_reference():
+    """one step, then add_air on cases.air_scenario: the oracle's new air
+    particles (oracle/ghosts.py) are the reference's, bit for bit"""
+    from _util import adapt_case
+    from oracle.ghosts import add_air
+    d = dict(np.load(os.path.join(GOLDEN, "add_air_3d.npz")))
+    c, binv = cases.air_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    np.testing.assert_array_equal(binv, d["binv_in"])
+    o = OracleRun(c)
+    o.steps(int(d["nsteps"]))
+    new, marked = add_air(c.grid, binv, o.ps, c.options)
+    ref = unpack(d, "born_")
+    assert new.n == ref.n > 1000 and len(marked) > 0
+    a, b = _by_position(new), _by_position(ref)
+    for f in DOUBLE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
