@@ -1152,6 +1152,15 @@ struct plume_ctx {
   int inlet_reserve = 0;
 };
 
+// device scratch of one call, freed on every return path
+struct ScratchFree {
+  void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+  ~ScratchFree() {
+    for (void* q : p)
+      if (q) cudaFree(q);
+  }
+};
+
 #define CK(call)                                                                      \
   do {                                                                                \
     cudaError_t e_ = (call);                                                          \
@@ -1871,7 +1880,7 @@ int plume_destroy(plume_ctx* ctx) {
   if (ctx->bc_map) cudaFree(ctx->bc_map);
   if (ctx->d_nreal) cudaFree(ctx->d_nreal);
   if (ctx->snap_st) cudaStreamSynchronize(ctx->snap_st);
-  if (ctx->snap_cap) {
+  {  // staging arrays (null when never allocated)
     void* sp[] = {ctx->snap.key, ctx->snap.x, ctx->snap.y, ctx->snap.z, ctx->snap.vx, ctx->snap.vy, ctx->snap.vz,
                   ctx->snap.mass, ctx->snap.h, ctx->snap.rho, ctx->snap.e, ctx->snap.p, ctx->snap.Y,
                   ctx->snap.phase, ctx->snap.bc, ctx->snap.inv};
@@ -3081,8 +3090,11 @@ static int add_ghost_layers(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t
   const int nbk = ctx->nbk;
   uint32_t* cnt = nullptr;
   unsigned long long* offs = nullptr;
+  ScratchFree scratch;
   CK(cudaMalloc(&cnt, 4 * (size_t)nbk));
+  scratch.p[0] = cnt;
   CK(cudaMalloc(&offs, 8 * (size_t)nbk));
+  scratch.p[1] = offs;
   k_pg_buckets<<<nblocks(nbk), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->cs, ctx->binv, ctx->bflags, ctx->bface,
                                                  nbk, ctx->explicit_types, kind, dx, ground, cnt);
   CK(cudaGetLastError());
@@ -3096,8 +3108,6 @@ static int add_ghost_layers(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t
     tot += hc[b];
   }
   if (ctx->n_alloc + tot > ctx->cap) {
-    cudaFree(cnt);
-    cudaFree(offs);
     ctx->err = std::string(name) + " exceeds capacity";
     return PLUME_E_CAPACITY;
   }
@@ -3111,8 +3121,6 @@ static int add_ghost_layers(plume_ctx* ctx, const PlumeAtmosphere* atm, uint64_t
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(st));
-  cudaFree(cnt);
-  cudaFree(offs);
   ctx->launches += tot ? 2 : 1;
   if (tot) {
     rc = set_count(ctx, ctx->n_alloc + (size_t)tot);
@@ -3223,9 +3231,13 @@ int plume_search_bnd_images(plume_ctx* ctx, size_t* n_out) {
   unsigned long long* dk = nullptr;
   double* dx = nullptr;
   unsigned int* dn = nullptr;
+  ScratchFree scratch;
   CK(cudaMalloc(&dk, 8 * (size_t)cap));
+  scratch.p[0] = dk;
   CK(cudaMalloc(&dx, 24 * (size_t)cap));
+  scratch.p[1] = dx;
   CK(cudaMalloc(&dn, sizeof(unsigned int)));
+  scratch.p[2] = dn;
   CK(cudaMemsetAsync(dn, 0, sizeof(unsigned int), st));
   const int n = (int)ctx->n_alloc;
   k_find_images<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->d_geo, ctx->A, ctx->d_count, ctx->bflags, ctx->bface,
@@ -3243,9 +3255,6 @@ int plume_search_bnd_images(plume_ctx* ctx, size_t* n_out) {
     CK(cudaMemcpyAsync(x.data(), dx, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
-  cudaFree(dk);
-  cudaFree(dx);
-  cudaFree(dn);
   rc = plume_set_wall_images(ctx, k.data(), x.data(), cnt);
   if (rc) return rc;
   *n_out = cnt;
