@@ -549,6 +549,33 @@ int plume_grid_generate(const double lo[3], const double hi[3], double h0, int s
                         PlumeGrid *grid, uint8_t *flags, int8_t *face_index, size_t cap,
                         size_t *nbk);
 
+/* ---- the initial vent duct --------------------------------------------
+ * setup_erupt (setup_erupt.cc:44-388; main.cc:156), on the device: the
+ * erupt ghosts of the duct below the vent -- the box [-radius, radius]^2 x
+ * [z_top - depth, z_top] filled with np particles' worth of lattice
+ * (Compute_mass, sph_lib.cc:1024-1040: spacing = cbrt(volume / np), mass =
+ * rho volume / np), points stepped out from the vent axis, kept where
+ * x^2 + y^2 <= radius^2 -- with the state of the erupt-ghost constructor
+ * (particle.cc:210-316: rho, e, vertical speed of the profile
+ * (ERUPT_VELOCITY_PROF 0 uniform u_avg, 1 parabolic 2 u_avg (1 - r^2/R^2)),
+ * Y 1, phase 2, the mixture EOS, then p, c and gamma as given); the
+ * particles other than erupt ghosts inside the duct are removed.  Keys
+ * key_base, key_base + 1, ... (z layer by layer from the top, then the
+ * points in the reference's order); *mass and *sml (may be NULL) return the
+ * duct particles' mass and spacing (simprops mass_of_phase2 /
+ * sml_of_phase2, which the eruption inlet uses). */
+typedef struct PlumeDuct {
+    double x0, y0;              /* vent axis (Pos_v_P)                        */
+    double z_top, depth;        /* Ll_P[2]; EXT_DOM_COF*PARTICLE_DENSITY*h0   */
+    double radius;              /* rv_P                                       */
+    int    np;                  /* num_erupt_particles                        */
+    int    profile;             /* ERUPT_VELOCITY_PROF: 0 uniform, 1 parabolic */
+    double u_avg;               /* Vv0_P                                      */
+    double rho, e, p, gamma, c; /* rhov_P ev0_P pv0_P gamma_v_P sndspd        */
+} PlumeDuct;
+int plume_setup_erupt(plume_ctx *ctx, const PlumeDuct *duct, uint64_t key_base, size_t *added,
+                      size_t *removed, double *mass, double *sml);
+
 /* Library version string "major.minor.patch". */
 const char *plume_version(void);
 

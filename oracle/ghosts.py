@@ -2,7 +2,8 @@
 
 A numpy restatement of the reference's add_pressure_ghost
 (src/plume/add_pressure_ghost.cc:37-316) and add_wall_ghost
-(src/plume/add_wall_ghost.cc:44-293) with initial_air
+(src/plume/add_wall_ghost.cc:44-293), add_air (src/plume/add_air.cc:490-795)
+and setup_erupt (src/plume/setup_erupt.cc:44-388) with initial_air
 (src/plume/sph_lib.cc:831-866), air_prop_hydro (:543-592) and
 Particle::update_second_var (src/datstr/particle.cc:528-604), used by the
 tests only, as the checker of the device's plume_add_pressure_ghost and
@@ -251,6 +252,86 @@ def add_air(grid, binv, ps, opt, atm: Atmosphere | None = None):
     out = _air_particles(rows, BC_REAL, dx, opt, atm)
     out.involved[:] = 1
     return out, np.array(marked, dtype=np.int64)
+
+
+def duct_lattice(duct):
+    """the points of setup_erupt's vent duct (setup_erupt.cc:104-230), in
+    its order: z from the top down, then x from the axis outward (+ side,
+    then - side), then y likewise, keeping x^2 + y^2 <= radius^2; positions
+    accumulated by repeated steps of sml as there.  Returns (points, mass,
+    sml) with mass and sml of Compute_mass (sph_lib.cc:1024-1040)."""
+    r = duct["radius"]
+    rng = [(-r, r), (-r, r), (duct["z_top"] - duct["depth"], duct["z_top"])]
+    dom = [rng[a][1] - rng[a][0] for a in range(3)]
+    vol = 1.0
+    for a in range(3):
+        vol *= dom[a]
+    sml = np.cbrt(vol / duct["np"])
+    mss = duct["rho"] * vol / duct["np"]
+    s2 = 0.5 * sml
+
+    def side(c0, lo, hi):
+        out = []
+        v = c0 + s2
+        while v <= hi:
+            out.append(v)
+            v += sml
+        v = c0 - s2
+        while v >= lo:
+            out.append(v)
+            v -= sml
+        return out
+    xs = side(duct["x0"], -r, r)
+    ys = side(duct["y0"], -r, r)
+    pts = []
+    z = rng[2][1] - s2
+    while z >= rng[2][0]:
+        for x in xs:
+            for y in ys:
+                if x * x + y * y <= r * r:
+                    pts.append((x, y, z))
+        z -= sml
+    return pts, mss, sml
+
+
+def setup_erupt(ps, duct, opt):
+    """(new erupt ghosts, mask of the particles setup_erupt removes): the
+    duct of duct_lattice with the state of the erupt-ghost constructor
+    (particle.cc:210-316: rho, e, vertical velocity of the profile, Y 1,
+    phase 2, the mixture EOS, then p, c and gamma as given), and the
+    particles other than erupt ghosts inside the duct removed
+    (setup_erupt.cc:296-310)"""
+    pts, mss, sml = duct_lattice(duct)
+    r = duct["radius"]
+    zlo, ztop = duct["z_top"] - duct["depth"], duct["z_top"]
+    d2 = ps.x * ps.x + ps.y * ps.y
+    gone = (d2 <= r * r) & (ps.z <= ztop) & (ps.z >= zlo) & (ps.bc_type != 0)
+    n = len(pts)
+    out = PS(n)
+    if n:
+        xyz = np.array(pts)
+        out.x, out.y, out.z = xyz[:, 0].copy(), xyz[:, 1].copy(), xyz[:, 2].copy()
+    out.mass[:] = mss
+    out.h[:] = sml
+    out.rho[:] = duct["rho"]
+    out.e[:] = duct["e"]
+    out.Y[:] = 1.0
+    out.phase[:] = 2
+    out.bc_type[:] = 0
+    for q in range(n):
+        dist = out.x[q] * out.x[q] + out.y[q] * out.y[q]
+        out.vz[q] = duct["u_avg"] if duct["profile"] == 0 else duct["u_avg"] * 2 * (1 - dist / (r * r))
+        # Particle::update_second_var with Y = 1
+        ng = opt.ng0 * 1.0
+        ns = 1.0 - ng
+        na = 1.0 - 1.0
+        cvm = ns * opt.cvs + ng * opt.cvg + na * opt.cva
+        out.T[q] = duct["e"] / cvm
+        out.cp[q] = cvm if opt.lans else 0.0
+    out.p[:] = duct["p"]
+    out.c[:] = duct["c"]
+    out.gamma[:] = duct["gamma"]
+    return out, gone
 
 
 def _air_particles(rows, bc, dx, opt, atm):

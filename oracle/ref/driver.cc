@@ -72,7 +72,7 @@ struct Case {
   std::vector<uint8_t> binv;  // per-bucket has_involved (optional)
   int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop,
                               // 2: then add_pressure_ghost, 3: add_wall_ghost alone,
-                              // 4: add_air alone
+                              // 4: add_air alone, 5: setup_erupt alone
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -548,7 +548,13 @@ int main(int argc, char **argv) {
   // then adapt_domain when it asks for it; the particles after it are an
   // extra dumped record
   int adapt_n = 0;
-  if (c.adapt_mode == 3 || c.adapt_mode == 4) {
+  if (c.adapt_mode == 5) {
+    // the initial vent duct of setup_erupt (setup_erupt.cc:44-388,
+    // main.cc:156): new erupt ghosts, displaced particles removed
+    setup_erupt(0, P, BG, tp, matprops, simprops, 1);
+    dump_state(fo, P, c, *tp, 0.0);
+    ndumped++;
+  } else if (c.adapt_mode == 3 || c.adapt_mode == 4) {
     // the wall-ghost layers of add_wall_ghost alone (main.cc:279), or the
     // air of add_air in the empty buckets (add_air.cc:490-795)
     if (c.adapt_mode == 3)

@@ -868,6 +868,47 @@ __global__ void k_pg_fill(const Geo* __restrict__ geo, const Opt* __restrict__ m
   }
 }
 
+// setup_erupt (setup_erupt.cc:44-388): particles other than erupt ghosts
+// inside the duct (x^2 + y^2 <= r^2, z in [z_bot, z_top]) are removed
+__global__ void k_duct_remove(Dev A, const int* __restrict__ d_count, double r2, double zbot, double ztop,
+                              unsigned int* __restrict__ removed) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *d_count) return;
+  const uint8_t bc = A.bc[i];
+  if (bc == BC_DEAD || bc == PLUME_BC_ERUPT) return;
+  const double x = A.x[i], y = A.y[i], z = A.z[i];
+  if (x * x + y * y <= r2 && z <= ztop && z >= zbot) {
+    A.bc[i] = BC_DEAD;
+    atomicAdd(removed, 1u);
+  }
+}
+
+// the duct's erupt ghosts: point q of z layer iz is (xy[2 q], xy[2 q + 1],
+// zs[iz]); state of the erupt-ghost constructor (particle.cc:210-316)
+__global__ void k_duct_fill(const Opt* __restrict__ mopt, Dev A, const double* __restrict__ xy, int npairs,
+                            const double* __restrict__ zs, int nz, PlumeDuct duct, double mass, double sml,
+                            size_t base, unsigned long long key_base) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npairs * nz) return;
+  const Opt& o = mopt[0];
+  const int iz = t / npairs, q = t % npairs;
+  const double x = xy[2 * q], y = xy[2 * q + 1];
+  const size_t r = base + (size_t)t;
+  A.key[r] = key_base + (unsigned long long)t;
+  A.x[r] = x; A.y[r] = y; A.z[r] = zs[iz];
+  const double dist = x * x + y * y;
+  A.vx[r] = 0; A.vy[r] = 0;
+  A.vz[r] = duct.profile == 0 ? duct.u_avg : duct.u_avg * 2 * (1 - dist / (duct.radius * duct.radius));
+  A.vsx[r] = 0; A.vsy[r] = 0; A.vsz[r] = 0;
+  A.mass[r] = mass; A.h[r] = sml; A.rho[r] = duct.rho; A.e[r] = duct.e; A.Y[r] = 1.0;
+  double gam, p, c, temp, cp = 0;
+  eos(o, duct.rho, 1.0, duct.e, gam, p, c, temp, cp, o.lans != 0);
+  A.T[r] = temp; A.cp[r] = cp;
+  A.p[r] = duct.p; A.c[r] = duct.c; A.gam[r] = duct.gamma;
+  A.phase[r] = 2; A.bc[r] = PLUME_BC_ERUPT; A.inv[r] = 0;
+  A.mem[r] = 0; A.bkt[r] = 0;
+}
+
 // search_bnd_images (bnd_image.cc:36-245) for a flat ground: a wall ghost
 // of a MIXED bucket whose own bucket or one of its 26 neighbours is an
 // on-ground MIXED bucket (bottom face below the ground, top face not,
@@ -3258,6 +3299,85 @@ int plume_search_bnd_images(plume_ctx* ctx, size_t* n_out) {
   rc = plume_set_wall_images(ctx, k.data(), x.data(), cnt);
   if (rc) return rc;
   *n_out = cnt;
+  return PLUME_OK;
+}
+
+int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, size_t* added, size_t* removed,
+                      double* mass_out, double* sml_out) {
+  if (!ctx || !duct || !added || !removed) return PLUME_E_INVALID;
+  *added = *removed = 0;
+  if (ctx->o.dim != 3 || ctx->nmem != 1 || !(duct->radius > 0) || !(duct->depth > 0) || duct->np < 1) {
+    ctx->err = "setup_erupt: single-run 3D contexts, radius, depth > 0, np >= 1";
+    return PLUME_E_INVALID;
+  }
+  // Compute_mass (sph_lib.cc:1024-1040) over the box [-r, r]^2 x [z_top - depth, z_top]
+  const double r = duct->radius;
+  const double lo[3] = {-r, -r, duct->z_top - duct->depth}, hi[3] = {r, r, duct->z_top};
+  double vol = 1.0;
+  for (int a = 0; a < 3; a++) vol *= hi[a] - lo[a];
+  const double sml = cbrt(vol / duct->np);
+  const double mss = duct->rho * vol / duct->np;
+  const double s2 = 0.5 * sml;
+  // the duct lattice (setup_erupt.cc:104-230): axes from the vent axis
+  // outward, + side then - side, positions by repeated steps
+  auto side = [&](double c0, double a0, double a1, std::vector<double>& out) {
+    for (double v = c0 + s2; v <= a1 && out.size() < 100000; v += sml) out.push_back(v);
+    for (double v = c0 - s2; v >= a0 && out.size() < 200000; v -= sml) out.push_back(v);
+  };
+  std::vector<double> xs, ys, zs, xy;
+  side(duct->x0, -r, r, xs);
+  side(duct->y0, -r, r, ys);
+  for (double z = hi[2] - s2; z >= lo[2] && zs.size() < 100000; z -= sml) zs.push_back(z);
+  for (double x : xs)
+    for (double y : ys)
+      if (x * x + y * y <= r * r) {
+        xy.push_back(x);
+        xy.push_back(y);
+      }
+  const int npairs = (int)(xy.size() / 2), nz = (int)zs.size();
+  const size_t nnew = (size_t)npairs * (size_t)nz;
+  int rc = search(ctx);
+  if (rc) return rc;
+  if (ctx->n_alloc + nnew > ctx->cap) {
+    ctx->err = "setup_erupt exceeds capacity";
+    return PLUME_E_CAPACITY;
+  }
+  cudaStream_t st = ctx->st;
+  ScratchFree scratch;
+  double *dxy = nullptr, *dz = nullptr;
+  unsigned int* drem = nullptr;
+  CK(cudaMalloc(&drem, sizeof(unsigned int)));
+  scratch.p[0] = drem;
+  CK(cudaMemsetAsync(drem, 0, sizeof(unsigned int), st));
+  const int n = (int)ctx->n_alloc;
+  k_duct_remove<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, r * r, lo[2], hi[2], drem);
+  CK(cudaGetLastError());
+  ctx->launches++;
+  if (nnew) {
+    CK(cudaMalloc(&dxy, 8 * xy.size()));
+    scratch.p[1] = dxy;
+    CK(cudaMalloc(&dz, 8 * zs.size()));
+    scratch.p[2] = dz;
+    CK(cudaMemcpyAsync(dxy, xy.data(), 8 * xy.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dz, zs.data(), 8 * zs.size(), cudaMemcpyHostToDevice, st));
+    k_duct_fill<<<nblocks(nnew), NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, dxy, npairs, dz, nz, *duct, mss, sml,
+                                                   ctx->n_alloc, (unsigned long long)key_base);
+    CK(cudaGetLastError());
+    ctx->launches++;
+  }
+  unsigned int nrem = 0;
+  CK(cudaMemcpyAsync(&nrem, drem, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (nnew) {
+    rc = set_count(ctx, ctx->n_alloc + nnew);
+    if (rc) return rc;
+  }
+  if (nnew || nrem) ctx->pending_dead = true;
+  if (nrem) ctx->has_dead = true;
+  *added = nnew;
+  *removed = nrem;
+  if (mass_out) *mass_out = mss;
+  if (sml_out) *sml_out = sml;
   return PLUME_OK;
 }
 

@@ -10,7 +10,7 @@ import os
 import subprocess
 import threading
 
-from .abi import PlumeAtmosphere, PlumeGrid, PlumeInlet, PlumeOptions, PlumeSoA, PlumeStepLog
+from .abi import PlumeAtmosphere, PlumeDuct, PlumeGrid, PlumeInlet, PlumeOptions, PlumeSoA, PlumeStepLog
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
@@ -102,6 +102,8 @@ def lib():
         L.plume_add_pressure_ghost.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
         L.plume_add_wall_ghost.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
         L.plume_add_air.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_size_t)]
+        L.plume_setup_erupt.argtypes = [C.c_void_p, P(PlumeDuct), C.c_uint64, P(C.c_size_t), P(C.c_size_t),
+                                        P(C.c_double), P(C.c_double)]
         L.plume_search_bnd_images.argtypes = [C.c_void_p, P(C.c_size_t)]
         L.plume_adapt_step.argtypes = [C.c_void_p, P(PlumeAtmosphere), C.c_uint64, P(C.c_int), P(C.c_size_t)]
         L.plume_snapshot_end.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_double), P(C.c_int)]

@@ -103,6 +103,13 @@ class Atmosphere:
         return a
 
 
+class PlumeDuct(C.Structure):
+    _fields_ = [("x0", C.c_double), ("y0", C.c_double), ("z_top", C.c_double), ("depth", C.c_double),
+                ("radius", C.c_double), ("np", C.c_int), ("profile", C.c_int), ("u_avg", C.c_double),
+                ("rho", C.c_double), ("e", C.c_double), ("p", C.c_double), ("gamma", C.c_double),
+                ("c", C.c_double)]
+
+
 class PlumeGrid(C.Structure):
     _fields_ = [
         ("mindom", C.c_double * 3), ("del_", C.c_double), ("nb", C.c_int * 3),

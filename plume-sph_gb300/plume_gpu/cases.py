@@ -454,6 +454,25 @@ def air_scenario(case):
     return dataclasses.replace(case, particles=ps, name=case.name + "_air"), binv
 
 
+def duct_scenario(case):
+    """A setup_erupt set-up on a plume built by plume_3d: its erupt ghosts
+    (the vent duct) removed, so that setup_erupt builds the duct again.
+    Returns (new case, per-bucket involvement states: NONE where absorbing,
+    POTENTIAL elsewhere) and the duct of the reference's constants
+    (parameters.h: radius rv_P 120 m, 1,080 particles, depth
+    EXT_DOM_COF * PARTICLE_DENSITY smoothing lengths below the ground,
+    parabolic profile of mean speed Vv0_P 75 m/s); the vent state
+    (rho, e, p, gamma, c) is left for the caller."""
+    import dataclasses
+    ps = case.particles
+    ps = ps.take(np.nonzero(ps.bc_type != BC_ERUPT)[0])
+    flags = np.asarray(case.grid.flags, dtype=np.uint8)
+    binv = np.where((flags & BUCKET_ABSORBING) != 0, BINV_NONE, BINV_POTENTIAL).astype(np.uint8)
+    duct = dict(x0=0.0, y0=0.0, z_top=float(case.grid.domain_lo[2]), depth=case.options.sml_phase2 * 1.5 * 8,
+                radius=120.0, np=1080, profile=1, u_avg=75.0)
+    return dataclasses.replace(case, particles=ps, name=case.name + "_duct"), binv, duct
+
+
 def inlet(case):
     """The eruption inlet of add_new_erupt (setup_erupt.cc:389-673) for a
     plume built by plume_3d: the duct's particle columns (spacing vent_dx,

@@ -232,6 +232,16 @@ class Solver:
         self._check(self.L.plume_add_air(self.ctx, C.byref(a), int(key_base), C.byref(n)), "plume_add_air")
         return n.value
 
+    def setup_erupt(self, duct: dict, key_base: int):
+        """the initial vent duct of setup_erupt, on the device (duct: the
+        PlumeDuct fields); returns (added, removed, mass, spacing)"""
+        from .abi import PlumeDuct
+        d = PlumeDuct(**{k: duct[k] for k, _ in PlumeDuct._fields_})
+        na, nr, m, h = C.c_size_t(), C.c_size_t(), C.c_double(), C.c_double()
+        self._check(self.L.plume_setup_erupt(self.ctx, C.byref(d), int(key_base), C.byref(na), C.byref(nr),
+                                             C.byref(m), C.byref(h)), "plume_setup_erupt")
+        return na.value, nr.value, m.value, h.value
+
     def search_bnd_images(self) -> int:
         """the wall-image table of search_bnd_images (flat ground), found on
         the device from the current wall ghosts and installed; returns the

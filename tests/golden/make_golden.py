@@ -146,6 +146,7 @@ def main():
     make_adapt_pg()
     make_wall_ghost()
     make_air()
+    make_duct()
     make_csv()
     make_grid()
 
@@ -249,6 +250,22 @@ def make_air():
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+def make_duct():
+    """setup_erupt_3d.npz: cases.duct_scenario on the domain-growth plume
+    (seed 6): one step, then the reference's setup_erupt.  Stores the input,
+    the particles setup_erupt created, and the keys of the case particles
+    left after it."""
+    c, binv, _ = cases.duct_scenario(adapt_case())
+    steps, _ = refio.run_ref("ref3d_adapt", c, 1, "/tmp/plume_golden", binv=binv, adapt=5)
+    d = {"nsteps": 1, "step0": c.step0, "pre_adaptive": 0, "dim": 3, "binv_in": binv,
+         "kept_key": np.sort(steps[-1]["particles"].key)}
+    d.update(pack("in_", c.particles))
+    d.update(pack("born_", steps[-1]["born"]))
+    path = os.path.join(HERE, "setup_erupt_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 GRID_DOMAINS = (
     # (name, lo, hi, h0, nproc): the 20 km plume domain at 150 m, the 600 m
     # test plume at 50 m, and a ragged domain above 1.5 km (bucket counts
@@ -310,6 +327,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--adapt":
         refio.build_ref()
         make_adapt()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--duct":
+        refio.build_ref()
+        make_duct()
     elif len(sys.argv) > 1 and sys.argv[1] == "--air":
         refio.build_ref()
         make_air()

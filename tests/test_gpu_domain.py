@@ -314,3 +314,49 @@ def test_add_air_matches_reference():
     for f in DOUBLE_FIELDS:
         x, y = getattr(gs, f), getattr(os_, f)
         assert np.abs(x - y).max() <= 1e-10 * max(np.abs(y).max(), 1e-300), f
+
+
+def test_setup_erupt_matches_reference():
+    """one step, then setup_erupt on the device (cases.duct_scenario): the
+    new erupt ghosts are the reference's (tests/golden/setup_erupt_3d.npz,
+    matched by position), the same particles are removed,
+    and two further steps agree with the oracle doing the same"""
+    from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
+    from oracle.ghosts import setup_erupt
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "setup_erupt_3d.npz")))
+    c, binv, duct = cases.duct_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    b = unpack(d, "born_")
+    duct.update(rho=float(b.rho[0]), e=float(b.e[0]), p=float(b.p[0]), gamma=float(b.gamma[0]), c=float(b.c[0]))
+    c.options.capacity = c.particles.n + 5000
+    s = Solver(c)
+    s.steps(int(d["nsteps"]))
+    base = 1 << 43
+    added, removed, mass, sml = s.setup_erupt(duct, base)
+    assert added == b.n > 500 and removed > 0
+    g = s.download()
+    np.testing.assert_array_equal(np.sort(g.key[g.key < base]), d["kept_key"])
+    new = g.take(np.nonzero(g.key >= base)[0])
+    # the spacing is cbrt(volume / np) of the host's libm: equal to the
+    # fixture's (x86) to the last place or one unit off, so positions,
+    # which accumulate it, compare to 1e-13
+    x, y = _by_position(new), _by_position(b)
+    for f in DOUBLE_FIELDS:
+        np.testing.assert_allclose(getattr(x, f), getattr(y, f), rtol=1e-13, atol=1e-12, err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(x, f), getattr(y, f), err_msg=f)
+    assert abs(mass / float(b.mass[0]) - 1) < 1e-15 and abs(sml / float(b.h[0]) - 1) < 1e-15
+    o = OracleRun(c)
+    o.steps(1)
+    extra, gone = setup_erupt(o.ps, duct, c.options)
+    o.ps = o.ps.take(np.nonzero(~gone)[0])
+    pos = {(px, py, pz): k for px, py, pz, k in zip(new.x, new.y, new.z, new.key)}
+    extra.key = np.array([pos[(px, py, pz)] for px, py, pz in zip(extra.x, extra.y, extra.z)], dtype=np.uint64)
+    o.append(extra)
+    s.steps(2)
+    o.steps(2)
+    gs, os_ = s.download().sorted_by_key(), o.ps.sorted_by_key()
+    np.testing.assert_array_equal(gs.key, os_.key)
+    for f in DOUBLE_FIELDS:
+        u, v = getattr(gs, f), getattr(os_, f)
+        assert np.abs(u - v).max() <= 1e-10 * max(np.abs(v).max(), 1e-300), f

@@ -361,3 +361,34 @@ def test_oracle_add_air_matches_reference():
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
     for f in BYTE_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+
+
+def _duct_state(d):
+    """the vent state the reference's erupt ghosts carry (rhov_P, ev0_P,
+    pv0_P, gamma_v_P, sndspd of its build)"""
+    b = unpack(d, "born_")
+    return dict(rho=float(b.rho[0]), e=float(b.e[0]), p=float(b.p[0]), gamma=float(b.gamma[0]),
+                c=float(b.c[0]))
+
+
+def test_oracle_setup_erupt_matches_reference():
+    """one step, then setup_erupt on cases.duct_scenario: the oracle's new
+    erupt ghosts (oracle/ghosts.py) are the reference's bit for bit, and it
+    removes the same particles"""
+    from _util import adapt_case
+    from oracle.ghosts import setup_erupt
+    d = dict(np.load(os.path.join(GOLDEN, "setup_erupt_3d.npz")))
+    c, binv, duct = cases.duct_scenario(adapt_case())
+    c.particles = unpack(d, "in_")
+    duct.update(_duct_state(d))
+    o = OracleRun(c)
+    o.steps(int(d["nsteps"]))
+    new, gone = setup_erupt(o.ps, duct, c.options)
+    ref = unpack(d, "born_")
+    assert new.n == ref.n > 500 and gone.sum() > 0
+    np.testing.assert_array_equal(np.sort(o.ps.key[~gone]), d["kept_key"])
+    a, b = _by_position(new), _by_position(ref)
+    for f in DOUBLE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
