@@ -43,6 +43,9 @@ def test_ctypes_struct_layout_matches_header():
 int main(void) {
   printf("%zu %zu %zu %zu\n", sizeof(PlumeOptions), sizeof(PlumeGrid), sizeof(PlumeSoA), sizeof(PlumeStepLog));
   printf("%zu %zu %zu\n", offsetof(PlumeOptions, capacity), offsetof(PlumeGrid, domain_hi), offsetof(PlumeSoA, involved));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(PlumeAtmosphere), offsetof(PlumeAtmosphere, Ate3), sizeof(PlumeDuct),
+         offsetof(PlumeDuct, u_avg), offsetof(PlumeDuct, c));
+  printf("%zu %zu\n", sizeof(PlumeInlet), offsetof(PlumeOptions, gsph_gradients));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -59,6 +62,13 @@ int main(void) {
     assert sizes[4] == abi.PlumeOptions.capacity.offset
     assert sizes[5] == abi.PlumeGrid.domain_hi.offset
     assert sizes[6] == abi.PlumeSoA.involved.offset
+    assert sizes[7] == C.sizeof(abi.PlumeAtmosphere)
+    assert sizes[8] == abi.PlumeAtmosphere.Ate3.offset
+    assert sizes[9] == C.sizeof(abi.PlumeDuct)
+    assert sizes[10] == abi.PlumeDuct.u_avg.offset
+    assert sizes[11] == abi.PlumeDuct.c.offset
+    assert sizes[12] == C.sizeof(abi.PlumeInlet)
+    assert sizes[13] == abi.PlumeOptions.gsph_gradients.offset
 
 
 def test_read_data_uses_single_precision(tmp_path):
