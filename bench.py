@@ -23,8 +23,22 @@ need_neigh particles x steps / seconds.
             64 small 3D plumes (60 m lattice, 5e4-4e5 air particles each,
             seed 2), mixed and FP64, on a bounded number of steps
 
-`--impl reference` times the reference's CPU path (the oracle port: the
-reference's own build is x86-only and does not travel) on the host cores.
+Timed window.  Config 2 starts from the lattice with h = dx; the first
+adaptive-h pass (step 50, every 50 steps after) raises h to about 1.5 dx,
+which more than triples the pairs per particle, and the 2,000-step run
+spends 97 % of its steps there.  The run therefore steps untimed to just
+before step 100 - K/2 (the plume develops, the inlet injects, h adapts at
+step 50), warms up, and times K steps centred on the second adaptive pass:
+the window holds every phase of the reference loop (dt, search, wall
+boundary, adaptive h once, momentum/energy, density, LANS filter, position,
+inlet) at the smoothing lengths of the bulk of the run.
+
+`--impl reference` times the reference's CPU path on the host cores: the
+oracle port (OpenMP over all cores) on a bounded sample of the same state,
+extrapolated to the whole table.  The reference's own C++ sources are not on
+the GPU machine (they build from the reference tree, which only the build
+container holds); its single-core speed against the port on the same sample
+is measured there and recorded beside the numbers.
 Multi-GPU: replicas only (independent copies per rank).
 """
 from __future__ import annotations
@@ -171,6 +185,38 @@ def pinned_particles(ps):
         setattr(out, f, pin(getattr(ps, f)))
     out._pinned = keep
     return out
+
+
+SML_INTERVAL = 50
+
+
+def timed_window(warmup: int, steps: int, interval: int = SML_INTERVAL):
+    """(untimed preparation steps, first timed step): K timed steps centred on
+    the second adaptive-h pass (step 2 * interval), starting after the first"""
+    first = max(interval + 1, 2 * interval - steps // 2)
+    return first - warmup - 1, first
+
+
+def cpu_state(case):
+    """the CPU sample's state: the workload after one adaptive-h pass (the
+    smoothing lengths of the bulk of the run), computed by the oracle"""
+    import dataclasses
+    from oracle.binding import OracleRun
+    o = OracleRun(case)
+    o.adaptive()
+    return dataclasses.replace(case, particles=o.ps)
+
+
+def density_l1(ref, other):
+    """relative L1 density error of `other` against `ref` over the
+    need_neigh particles present in both (matched by key)"""
+    a, b = ref.sorted_by_key(), other.sorted_by_key()
+    common, ia, ib = np.intersect1d(a.key, b.key, return_indices=True)
+    real = a.need_neigh()[ia] & b.need_neigh()[ib]
+    ra, rb = a.rho[ia][real], b.rho[ib][real]
+    return {"l1": float(np.abs(rb - ra).sum() / np.abs(ra).sum()),
+            "max_rel": float((np.abs(rb - ra) / np.abs(ra)).max()),
+            "particles": int(real.sum())}
 
 
 def cpu_sample(case, budget_s: float = 12.0, nthreads: int = 0):
@@ -372,7 +418,7 @@ def run_reference(args, dist, rank, ws):
     if rank != 0:
         return 0
     from plume_gpu import cases
-    case = small_plume(0) if args.small else cases.plume_config2(seed=0)
+    case = cpu_state(small_plume(0) if args.small else cases.plume_config2(seed=0))
     ncores = os.cpu_count() or 1
     vals = []
     nt = None
@@ -394,8 +440,11 @@ def run_reference(args, dist, rank, ws):
                                          "n_air": int(case.particles.need_neigh().sum()),
                                          "inputs": "host memory"},
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": ncores, "kind": "port",
-                         "sample": f"{nt} air particles per step (neighbour lists + all sweeps), "
-                                   f"remaining per-particle work for all {case.particles.n} particles"},
+                         "sample": f"extrapolated: one step's neighbour lists and sweeps for the first "
+                                   f"{nt} of {int(case.particles.need_neigh().sum())} air particles "
+                                   f"({100.0 * nt / case.particles.need_neigh().sum():.1f} %), per-particle "
+                                   f"work for all {case.particles.n}, on the state after one adaptive-h "
+                                   f"pass; scaled to the whole table"},
         "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -418,6 +467,11 @@ def main():
     ap.add_argument("--no-gsph", action="store_true", help="skip the GSPH leg")
     ap.add_argument("--no-wall-bc", action="store_true",
                     help="leave the wall ghosts' states fixed (no apply_bcond in the step)")
+    ap.add_argument("--no-inlet", action="store_true",
+                    help="no eruption inlet (add_new_erupt) in the step")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="also report the mixed path's density error against FP64 after this "
+                         "many steps (beyond the timed window's end)")
     ap.add_argument("--adjoint-fd", action="store_true",
                     help="also check the adjoint gradient by central differences, relative "
                          "steps 1e-4 and 1e-10 (12 forward solves)")
@@ -444,21 +498,36 @@ def main():
 
     case = make(PREC_MIXED)
     tuning = None
+    import dataclasses
     from plume_gpu.autotune import tune_subcells, with_subcells
     if args.subcells:
         case = with_subcells(case, args.subcells)
     elif not args.no_tune:
+        # tuned at the smoothing lengths of the timed window (after one
+        # adaptive-h pass)
         t0 = time.perf_counter()
-        best, table = tune_subcells(case, candidates=(3, 4, 5, 6), steps=3, warmup=2)
+        best, table = tune_subcells(dataclasses.replace(case, pre_adaptive=True),
+                                    candidates=(3, 4, 5, 6), steps=3, warmup=2)
         tuning = {"subcells": best, "ms_per_step": {str(k): round(v, 3) for k, v in table.items()},
-                  "seconds": time.perf_counter() - t0}
+                  "state": "after one adaptive-h pass", "seconds": time.perf_counter() - t0}
         case = with_subcells(case, best)
     n_air0 = int(case.particles.need_neigh().sum())
     images = None if args.no_wall_bc else cases.wall_images(case)
-    sol = Solver(case)
-    if images is not None:
-        sol.set_wall_images(*images)
-    # warm-up (not timed)
+    inlet = None if args.no_inlet else cases.inlet(case)
+    prep, first = timed_window(args.warmup, args.steps)
+    last = first + args.steps - 1
+
+    def solver(c):
+        s = Solver(c)
+        if images is not None:
+            s.set_wall_images(*images)
+        if inlet is not None:
+            s.set_inlet(inlet)
+        return s
+
+    sol = solver(case)
+    # untimed: the plume develops, h adapts at step 50; then the warm-up
+    sol.steps(prep)
     sol.steps(args.warmup)
     barrier(dist)
     torch.cuda.synchronize()
@@ -472,10 +541,12 @@ def main():
     t_dev = phases["total"] / 1000.0
     t_max = reduce_max(dist, t_dev)
     # particle-steps: need_neigh particles of each step (count at the start
-    # and end of the timed region; the inlet changes it by < 0.1 %)
+    # and end of the timed region; the inlet adds < 0.1 %)
     n_real = 0.5 * (n_real_before + n_real_after)
     value = ws * n_real * args.steps / t_max
     ms_per_step = 1000.0 * t_max / args.steps
+    step_end = sol.time()[1]
+    mixed_end = sol.download() if not args.no_fp64 else None
 
     # dominant kernel: momentum sweep
     peak_hbm, peak_kind = load_peaks()
@@ -526,32 +597,48 @@ def main():
     d2h //= e2e_steps
     sol.close()
 
-    # FP64 path on the same workload (shorter)
+    # FP64 path on the same workload: the same steps from the same inputs
+    # (its last 3 steps timed), and the mixed path's density error against
+    # it at the end of the timed window; --accuracy-steps N (> the window's
+    # end) adds the error after N steps (a separate mixed run to step N)
     fp64 = None
+    accuracy = None
     if not args.no_fp64:
-        c64 = with_subcells(make(PREC_FP64), case.grid.subcells)
-        s64 = Solver(c64)
-        if images is not None:
-            s64.set_wall_images(*images)
-        s64.steps(3)
-        k64 = max(2, min(args.steps, 3))
+        sub = case.grid.subcells
+        s64 = solver(with_subcells(make(PREC_FP64), sub))
+        k64 = 3
+        s64.steps(step_end - k64)
         _, nr0 = s64.count()
         s64.steps(k64)
         ph64 = s64.phase_times()
         _, nr1 = s64.count()
         t64 = reduce_max(dist, ph64["total"] / 1000.0)
         fp64 = {"value": ws * 0.5 * (nr0 + nr1) * k64 / t64, "unit": METRIC, "steps": k64,
+                "timed_steps": [step_end - k64 + 1, step_end],
                 "ms_per_step": 1000.0 * t64 / k64,
                 "momentum_ms": ph64["momentum"] / k64}
-        s64.close()
+        accuracy = [dict(step=step_end, **density_l1(s64.download(), mixed_end))]
+        del mixed_end
+        if args.accuracy_steps > step_end:
+            s64.steps(args.accuracy_steps - step_end)
+            ref = s64.download()
+            s64.close()
+            sm = solver(case)
+            sm.steps(args.accuracy_steps)
+            accuracy.append(dict(step=args.accuracy_steps, **density_l1(ref, sm.download())))
+            sm.close()
+        else:
+            s64.close()
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
             ncpu = os.cpu_count() or 1
-            ntg, tc = cpu_sample(make(PREC_FP64), budget_s=12.0)
+            cs = cpu_state(make(PREC_FP64))
+            ntg, tc = cpu_sample(cs, budget_s=12.0)
             cpu = {"value": ntg / tc, "unit": METRIC, "cores": ncpu, "kind": "port",
-                   "sample": f"one step for {ntg} of {n_air0} air particles (lists + sweeps), "
-                             f"all particles for the per-particle work"}
+                   "sample": f"extrapolated: one step's neighbour lists and sweeps for the first {ntg} of "
+                             f"{n_air0} air particles ({100.0 * ntg / n_air0:.1f} %), per-particle work "
+                             f"for all, on the state after one adaptive-h pass"}
         except Exception as e:  # the oracle is optional on the box
             cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
@@ -592,7 +679,12 @@ def main():
                        "precision": "fp32 pair arithmetic, fp64 positions and updates",
                        "parallelism": f"replicas{ws}", "l2": "working set > L2 (state ~0.6 GB)",
                        "subcells": int(case.grid.subcells), "autotune": tuning,
-                       "wall_images": 0 if images is None else int(len(images[0]))},
+                       "wall_images": 0 if images is None else int(len(images[0])),
+                       "inlet_columns": 0 if inlet is None else int(len(inlet["col_vel"])),
+                       "timed_steps": [first, last],
+                       "window": f"steps {first}-{last} after {prep + args.warmup} untimed steps from the "
+                                 f"lattice (h = dx until the adaptive-h pass of step 50); the window "
+                                 f"holds the adaptive-h pass of step {2 * SML_INTERVAL}"},
             "gpu_launches": launches,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
             "clocks": clk.summary(),
@@ -600,6 +692,7 @@ def main():
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "fp64": fp64,
             "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
+            "l1_density_vs_fp64": accuracy,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak_hbm,
                          "unit": "GB/s", "frac": achieved_gbs / peak_hbm, "traffic": traffic,
                          "kernel": "k_sweep3_list<float,WMom>", "peak_kind": peak_kind,

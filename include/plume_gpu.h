@@ -279,6 +279,14 @@ int plume_set_time(plume_ctx *ctx, double time, int step, int ioutput,
 int plume_neighbor_pairs(plume_ctx *ctx, int mode, uint64_t *key_i,
                          uint64_t *key_j, size_t cap, size_t *n);
 
+/* plume_neighbor_pairs restricted to the need_neigh particles whose keys are
+ * among keys[0..nkeys) (any order): the neighbour vectors of chosen
+ * particles, as the reference reads them from one particle of its table
+ * (THashTable::lookup(key)->get_neighs(), particle.h:538-541), so large
+ * tables can be checked on a sample. */
+int plume_neighbor_pairs_of(plume_ctx *ctx, int mode, const uint64_t *keys, size_t nkeys,
+                            uint64_t *key_i, uint64_t *key_j, size_t cap, size_t *n);
+
 /* ---- output snapshots ---------------------------------------------------
  * The fields that write_h5part writes (h5part_writer.cc:41-275: x, y, z,
  * vx, vy, vz, rho, e, Y, p, phase, bc_type; plus key, mass and h) of the
@@ -386,7 +394,8 @@ int plume_adapt_step(plume_ctx *ctx, const PlumeAtmosphere *atm, uint64_t key_ba
  * max h and per-step neighbour lists, [3] momentum/energy sweep, [4] its commit + EOS, [5] density sweep,
  * [6] its commit + EOS, [7] velocity filter, [8] position update and
  * re-bucketing, [9] dt reduction, [10] total, [11] the momentum pair-sweep
- * kernel alone (inside [3]).  n <= 12 entries. */
+ * kernel alone (inside [3]), [12] eruption inlet (add_new_erupt) and the
+ * step's end, [13] wall boundary (apply_bcond).  n <= 14 entries. */
 int plume_phase_times(plume_ctx *ctx, float *ms, int n);
 
 /* Device kernel launches issued by the last plume_step/plume_steps call. */
@@ -525,10 +534,11 @@ int plume_adjoint_backward(plume_ctx *ctx, const PlumeSoA *final_bar, size_t n_f
  * array of PLUME_NOALLOC_MAX_BLOCKS doubles that every GPU loading the
  * library keeps until exit; n above PLUME_NOALLOC_MAX_BLOCKS *
  * PLUME_NOALLOC_CHUNK returns PLUME_E_CAPACITY.  The first call on a device
- * looks up that array's address; make it before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race.  A sound speed <= 0
- * (or NaN) among those particles gives a NaN dt.  Asynchronous: read dt_out
- * after synchronising the stream. */
+ * looks up that array's address (again after the device's context is
+ * replaced, e.g. by cudaDeviceReset); make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race.  A particle
+ * with h <= 0 or c <= 0 (or NaN) among those particles gives a NaN dt.
+ * Asynchronous: read dt_out after synchronising the stream. */
 #define PLUME_NOALLOC_MAX_BLOCKS 1024
 #define PLUME_NOALLOC_CHUNK      16384
 int plume_timestep_noalloc(const double *h, const double *c, const uint8_t *bc_type,

@@ -47,6 +47,11 @@ def lib():
                                    C.POINTER(PlumeSoA), C.c_size_t, C.c_int,
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_size_t,
                                    C.POINTER(C.c_size_t)]
+        L.oracle_pairs_of.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
+                                      C.POINTER(PlumeSoA), C.c_size_t, C.c_int,
+                                      C.POINTER(C.c_uint64), C.c_size_t,
+                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_size_t,
+                                      C.POINTER(C.c_size_t)]
         L.oracle_sample_step_seconds.argtypes = [C.POINTER(PlumeOptions), C.POINTER(PlumeGrid),
                                                  C.POINTER(PlumeSoA), C.c_size_t, C.c_size_t,
                                                  C.c_int]
@@ -230,6 +235,30 @@ class OracleRun:
         if rc:
             raise RuntimeError(f"oracle_pairs failed: {rc}")
         return ki, kj
+
+
+def _pairs_of(self, keys, mode: int = 0):
+    """pairs() of the need_neigh particles whose keys are in `keys`"""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    kp = keys.ctypes.data_as(C.POINTER(C.c_uint64))
+    s = self.ps.soa()
+    cnt = C.c_size_t(0)
+    L = lib()
+    rc = L.oracle_pairs_of(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n, mode, kp, len(keys),
+                           None, None, 0, C.byref(cnt))
+    if rc:
+        raise RuntimeError(f"oracle_pairs_of failed: {rc}")
+    ki = np.zeros(cnt.value, dtype=np.uint64)
+    kj = np.zeros(cnt.value, dtype=np.uint64)
+    rc = L.oracle_pairs_of(C.byref(self.opt), C.byref(self.grid), C.byref(s), self.ps.n, mode, kp, len(keys),
+                           ki.ctypes.data_as(C.POINTER(C.c_uint64)), kj.ctypes.data_as(C.POINTER(C.c_uint64)),
+                           cnt.value, C.byref(cnt))
+    if rc:
+        raise RuntimeError(f"oracle_pairs_of failed: {rc}")
+    return ki, kj
+
+
+OracleRun.pairs_of = _pairs_of
 
 
 def sample_step_seconds(case, ntarget: int, nthreads: int = 0) -> float:

@@ -14,7 +14,15 @@ from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, ParticleSet as PS
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def build_ref(ref_root: str = "/root/reference"):
+def reference_root() -> str:
+    """the reference source tree: $PLUME_REFERENCE, else a directory named
+    "reference" beside this checkout"""
+    return os.environ.get("PLUME_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                             "reference")
+
+
+def build_ref(ref_root: str | None = None):
+    ref_root = ref_root or reference_root()
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
 
 

@@ -250,19 +250,20 @@ static void lists_free(Lists *L)
  * (neighs.cc:84,117-131).  Particles of one bucket keep index order. */
 static int build_lists_3d_for(const PlumeOptions *o, const PlumeGrid *g,
                               const PlumeSoA *s, size_t n, size_t ntarget,
-                              Lists *L, int nthreads, int all);
+                              Lists *L, int nthreads, int all, const char *tmask);
 static int build_lists_3d(const PlumeOptions *o, const PlumeGrid *g,
                           const PlumeSoA *s, size_t n, size_t ntarget,
                           Lists *L, int nthreads)
 {
-    return build_lists_3d_for(o, g, s, n, ntarget, L, nthreads, 0);
+    return build_lists_3d_for(o, g, s, n, ntarget, L, nthreads, 0, NULL);
 }
 
 /* all: lists for every particle, as search_neighs_consth builds them under
- * USE_GSPH (neighs.cc:76, 136: ghosts need lists for their gradients) */
+ * USE_GSPH (neighs.cc:76, 136: ghosts need lists for their gradients);
+ * tmask (when not NULL): lists only for the targets it marks */
 static int build_lists_3d_for(const PlumeOptions *o, const PlumeGrid *g,
                               const PlumeSoA *s, size_t n, size_t ntarget,
-                              Lists *L, int nthreads, int all)
+                              Lists *L, int nthreads, int all, const char *tmask)
 {
     long nbk = (long)g->nb[0] * g->nb[1] * g->nb[2];
     long *bk = (long *)malloc(sizeof(long) * (n ? n : 1));
@@ -292,6 +293,8 @@ static int build_lists_3d_for(const PlumeOptions *o, const PlumeGrid *g,
         size_t c = 0;
         for (size_t i = 0; i < n && c < nt; i++)
             if (all || need_neigh(s->bc_type[i])) { is_t[i] = 1; c++; }
+        if (tmask)
+            for (size_t i = 0; i < n; i++) is_t[i] = is_t[i] && tmask[i];
     }
     int nbx = g->nb[0], nby = g->nb[1], nbz = g->nb[2];
     /* two passes: count, then fill */
@@ -1454,7 +1457,7 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
         const int recon = gsph && o->gsph_recon != PLUME_RECON_ZEROTH;
         const int need_grad = gsph && (o->gsph_gradients || recon);
         if (D == 3) {
-            rc = build_lists_3d_for(o, g, s, nn, (size_t)-1, &L, nthreads, need_grad);
+            rc = build_lists_3d_for(o, g, s, nn, (size_t)-1, &L, nthreads, need_grad, NULL);
             if (rc) return rc;
             oldb = (long *)malloc(sizeof(long) * (nn ? nn : 1));
             for (size_t i = 0; i < nn; i++) oldb[i] = bucket_of(g, s->x[i], s->y[i], s->z[i]);
@@ -1652,21 +1655,28 @@ int oracle_adapt_domain(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s, 
     return PLUME_OK;
 }
 
-int oracle_pairs(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
-                 size_t n, int mode, uint64_t *key_i, uint64_t *key_j,
-                 size_t cap, size_t *npairs)
+static int cmp_u64(const void *a, const void *b)
+{
+    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return (x > y) - (x < y);
+}
+
+static int pairs_impl(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
+                      size_t n, int mode, const char *tmask, uint64_t *key_i, uint64_t *key_j,
+                      size_t cap, size_t *npairs)
 {
     int rc = check_opts(o, g, s);
     if (rc) return rc;
     const int D = o->dim;
     Lists L = { 0 };
     if (D == 3) {
-        rc = build_lists_3d(o, g, s, n, (size_t)-1, &L, nthreads_of(0));
+        rc = build_lists_3d_for(o, g, s, n, (size_t)-1, &L, nthreads_of(0), 0, tmask);
         if (rc) return rc;
     }
     size_t c = 0;
     for (size_t i = 0; i < n; i++) {
         if (!need_neigh(s->bc_type[i])) continue;
+        if (tmask && !tmask[i]) continue;
         double xi[3];
         coords(s, i, D, xi);
         double hi = s->h[i];
@@ -1689,6 +1699,31 @@ int oracle_pairs(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
     lists_free(&L);
     *npairs = c;
     return PLUME_OK;
+}
+
+int oracle_pairs(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
+                 size_t n, int mode, uint64_t *key_i, uint64_t *key_j,
+                 size_t cap, size_t *npairs)
+{
+    return pairs_impl(o, g, s, n, mode, NULL, key_i, key_j, cap, npairs);
+}
+
+/* oracle_pairs for the need_neigh particles whose keys are in keys[0..nkeys) */
+int oracle_pairs_of(const PlumeOptions *o, const PlumeGrid *g, const PlumeSoA *s,
+                    size_t n, int mode, const uint64_t *keys, size_t nkeys,
+                    uint64_t *key_i, uint64_t *key_j, size_t cap, size_t *npairs)
+{
+    uint64_t *sk = (uint64_t *)malloc(sizeof(uint64_t) * (nkeys ? nkeys : 1));
+    char *tmask = (char *)calloc(n ? n : 1, 1);
+    if (!sk || !tmask) { free(sk); free(tmask); return PLUME_E_INVALID; }
+    if (nkeys) memcpy(sk, keys, sizeof(uint64_t) * nkeys);
+    qsort(sk, nkeys, sizeof(uint64_t), cmp_u64);
+    for (size_t i = 0; i < n; i++)
+        tmask[i] = nkeys && bsearch(&s->key[i], sk, nkeys, sizeof(uint64_t), cmp_u64) != NULL;
+    int rc = pairs_impl(o, g, s, n, mode, tmask, key_i, key_j, cap, npairs);
+    free(sk);
+    free(tmask);
+    return rc;
 }
 
 static double now_s(void)

@@ -81,6 +81,10 @@ int oracle_adapt_domain(const PlumeOptions *opt, const PlumeGrid *grid, PlumeSoA
 int oracle_pairs(const PlumeOptions *opt, const PlumeGrid *grid,
                  const PlumeSoA *s, size_t n, int mode,
                  uint64_t *key_i, uint64_t *key_j, size_t cap, size_t *npairs);
+int oracle_pairs_of(const PlumeOptions *opt, const PlumeGrid *grid,
+                    const PlumeSoA *s, size_t n, int mode,
+                    const uint64_t *keys, size_t nkeys,
+                    uint64_t *key_i, uint64_t *key_j, size_t cap, size_t *npairs);
 
 /* Bounded CPU sample of one step: the neighbour search and the pair sweeps
  * of a step run for the first `ntarget` need_neigh particles only (all

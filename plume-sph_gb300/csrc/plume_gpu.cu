@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <climits>
 
 #include "../../include/plume_gpu.h"
 #include "radix_sort.cuh"
@@ -34,9 +35,10 @@ namespace {
 constexpr int NTHREADS = 128;
 // phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax + lists, 3 momentum,
 // 4 commit_mom, 5 density, 6 commit_dens, 7 velocity, 8 position, 9 dt,
-// 10 total, 11 the momentum pair-sweep kernel alone (part of 3)
-constexpr int NPHASE = 12;
-constexpr int NEV = 12;
+// 10 total, 11 the momentum pair-sweep kernel alone (part of 3), 12 inlet +
+// step end, 13 wall boundary
+constexpr int NPHASE = 14;
+constexpr int NEV = 14;
 
 inline int nblocks(size_t n, int t = NTHREADS) { return (int)((n + t - 1) / t); }
 
@@ -288,11 +290,22 @@ template <int D>
 __global__ void k_pairs(int mode, Opt o, const Geo* __restrict__ geo, Dev A, Work W,
                         const uint32_t* __restrict__ cs_all, const int* __restrict__ d_count,
                         const unsigned long long* __restrict__ offs, unsigned int* __restrict__ cnt,
-                        uint64_t* __restrict__ ki, uint64_t* __restrict__ kj) {
+                        uint64_t* __restrict__ ki, uint64_t* __restrict__ kj,
+                        const uint64_t* __restrict__ sub, int nsub) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = *d_count;
   if (i >= n) return;
-  if (!need_neigh(A.bc[i])) {
+  bool want = need_neigh(A.bc[i]);
+  if (want && sub) {  // only the particles whose keys are in the sorted subset
+    const uint64_t k = A.key[i];
+    int lo = 0, hi = nsub;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (sub[mid] < k) lo = mid + 1; else hi = mid;
+    }
+    want = lo < nsub && sub[lo] == k;
+  }
+  if (!want) {
     if (!offs) cnt[i] = 0;
     return;
   }
@@ -1550,6 +1563,7 @@ static int step_async(plume_ctx* ctx) {
   record_ev(ctx, 1);
   int rc = search(ctx);
   if (rc) return rc;
+  record_ev(ctx, 13);
   if (ctx->nimg) apply_bc(ctx);
   record_ev(ctx, 2);
   ctx->host_step++;
@@ -1566,6 +1580,7 @@ static int step_async(plume_ctx* ctx) {
     if (mixed) launch_sweeps<1, float, true>(ctx, adaptive_now); else launch_sweeps<1, double, true>(ctx, adaptive_now);
     k_update_pos<1><<<nblocks(n), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->bflags, ctx->bface, ctx->d_count, ctx->ts);
   }
+  record_ev(ctx, 12);
   if (ctx->inlet_reserve) {  // add_new_erupt (main.cc:416-417)
     cudaMemsetAsync(ctx->inlet_rowctr, 0, sizeof(int), st);
     k_inject<<<nblocks(ctx->inlet.ncol), NTHREADS, 0, st>>>(ctx->inlet, ctx->d_opt, ctx->A, ctx->d_count, ctx->ts,
@@ -1589,13 +1604,20 @@ static int step_async(plume_ctx* ctx) {
   return PLUME_OK;
 }
 
-// events of a step: 0 start, 1 after dt, 2 after search, 3 after adaptive,
-// 4 after hmax, 5 after momentum, 6 after commit, 7 after density, 8 after
-// commit, 9 after velocity, 10 end, 11 before the momentum pair sweep
+// events of a step: 0 start, 1 after dt, 2 after search and wall boundary,
+// 3 after adaptive, 4 after hmax, 5 after momentum, 6 after commit, 7 after
+// density, 8 after commit, 9 after velocity, 10 end, 11 before the momentum
+// pair sweep, 12 after the position update, 13 after search (before the
+// wall boundary).  Phases: 0 search (keys, sort, gather, cell table), 1
+// adaptive h, 2 lists, 3 momentum, 4 commit, 5 density, 6 commit, 7 LANS
+// filter, 8 position update, 9 dt, 10 total, 11 momentum pair sweep alone,
+// 12 inlet (add_new_erupt) and step end, 13 wall boundary (apply_bcond)
 static void accumulate_phases(plume_ctx* ctx, const cudaEvent_t* e) {
   float t[NPHASE];
   cudaEventElapsedTime(&t[9], e[0], e[1]);
-  cudaEventElapsedTime(&t[0], e[1], e[2]);
+  cudaEventElapsedTime(&t[0], e[1], e[13]);
+  cudaEventElapsedTime(&t[13], e[13], e[2]);
+  cudaEventElapsedTime(&t[12], e[12], e[10]);
   cudaEventElapsedTime(&t[1], e[2], e[3]);
   cudaEventElapsedTime(&t[2], e[3], e[4]);
   cudaEventElapsedTime(&t[3], e[4], e[5]);
@@ -1603,7 +1625,7 @@ static void accumulate_phases(plume_ctx* ctx, const cudaEvent_t* e) {
   cudaEventElapsedTime(&t[5], e[6], e[7]);
   cudaEventElapsedTime(&t[6], e[7], e[8]);
   cudaEventElapsedTime(&t[7], e[8], e[9]);
-  cudaEventElapsedTime(&t[8], e[9], e[10]);
+  cudaEventElapsedTime(&t[8], e[9], e[12]);
   cudaEventElapsedTime(&t[10], e[0], e[10]);
   cudaEventElapsedTime(&t[11], e[11], e[5]);
   for (int k = 0; k < NPHASE; k++) ctx->phase_ms[k] += t[k];
@@ -2370,8 +2392,20 @@ int plume_set_time(plume_ctx* ctx, double time, int step, int ioutput, double ne
   return PLUME_OK;
 }
 
-int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* key_j, size_t cap, size_t* n) {
-  if (!ctx || !n || (mode != 0 && mode != 1)) return PLUME_E_INVALID;
+static int neighbor_pairs(plume_ctx* ctx, int mode, const uint64_t* keys, size_t nkeys, uint64_t* key_i,
+                          uint64_t* key_j, size_t cap, size_t* n) {
+  if (!ctx || !n || (mode != 0 && mode != 1) || (nkeys && !keys) || nkeys > (size_t)INT_MAX)
+    return PLUME_E_INVALID;
+  ScratchFree subs;
+  uint64_t* dsub = nullptr;
+  if (keys) {
+    std::vector<uint64_t> sk(keys, keys + nkeys);
+    std::sort(sk.begin(), sk.end());
+    CK(cudaMalloc(&dsub, 8 * (sk.size() ? sk.size() : 1)));
+    subs.p[0] = dsub;
+    if (!sk.empty()) CK(cudaMemcpy(dsub, sk.data(), 8 * sk.size(), cudaMemcpyHostToDevice));
+  }
+  const int nsub = (int)nkeys;
   int rc = search(ctx);
   if (rc) return rc;
   int s = ctx_sync_status(ctx);
@@ -2390,9 +2424,9 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
   cudaStream_t st = ctx->st;
   const int nb = nblocks(np ? np : 1);
   if (ctx->o.dim == 3)
-    k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+    k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr, dsub, nsub);
   else
-    k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr);
+    k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, nullptr, cnt, nullptr, nullptr, dsub, nsub);
   unsigned long long total = 0;
   if (np) {
     k_scan_blocks<<<nbk, 1024, 0, st>>>(cnt, np, offs, sums);
@@ -2407,9 +2441,9 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
     CK(cudaMalloc(&dki, 8 * total));
     CK(cudaMalloc(&dkj, 8 * total));
     if (ctx->o.dim == 3)
-      k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+      k_pairs<3><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj, dsub, nsub);
     else
-      k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj);
+      k_pairs<1><<<nb, NTHREADS, 0, st>>>(mode, ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, offs, cnt, dki, dkj, dsub, nsub);
     CK(cudaMemcpyAsync(key_i, dki, 8 * total, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(key_j, dkj, 8 * total, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -2422,6 +2456,17 @@ int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* ke
   cudaFree(tot);
   CK(cudaGetLastError());
   return PLUME_OK;
+}
+
+int plume_neighbor_pairs(plume_ctx* ctx, int mode, uint64_t* key_i, uint64_t* key_j, size_t cap, size_t* n) {
+  return neighbor_pairs(ctx, mode, nullptr, 0, key_i, key_j, cap, n);
+}
+
+int plume_neighbor_pairs_of(plume_ctx* ctx, int mode, const uint64_t* keys, size_t nkeys, uint64_t* key_i,
+                            uint64_t* key_j, size_t cap, size_t* n) {
+  if (!keys && nkeys) return PLUME_E_INVALID;
+  static const uint64_t none = 0;
+  return neighbor_pairs(ctx, mode, keys ? keys : &none, nkeys, key_i, key_j, cap, n);
 }
 
 // ---------------------------------------------------------------- ensembles
@@ -3318,16 +3363,33 @@ int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, 
   const double sml = cbrt(vol / duct->np);
   const double mss = duct->rho * vol / duct->np;
   const double s2 = 0.5 * sml;
+  int rc = search(ctx);
+  if (rc) return rc;
+  // Upper bounds of the lattice's axis counts, from the extents alone (one
+  // extra point per direction covers the rounding of the repeated steps),
+  // checked against the capacity before any host or device memory is
+  // taken: a large np makes sml tiny and the lattice huge.
+  auto axis_ub = [&](double c0, double a0, double a1) {
+    const double up = floor(fmax(a1 - c0 - s2, -sml) / sml) + 2.0;
+    const double dn = floor(fmax(c0 - s2 - a0, -sml) / sml) + 2.0;
+    return fmax(up, 0.0) + fmax(dn, 0.0);
+  };
+  const double nz_ub = floor(fmax(hi[2] - s2 - lo[2], -sml) / sml) + 2.0;
+  const double ub = axis_ub(duct->x0, -r, r) * axis_ub(duct->y0, -r, r) * fmax(nz_ub, 0.0);
+  if (!(sml > 0) || !(ub == ub) || (double)ctx->n_alloc + ub > (double)ctx->cap || ub > (double)INT_MAX) {
+    ctx->err = "setup_erupt: the duct lattice (np particles) exceeds the context's capacity";
+    return PLUME_E_CAPACITY;
+  }
   // the duct lattice (setup_erupt.cc:104-230): axes from the vent axis
   // outward, + side then - side, positions by repeated steps
   auto side = [&](double c0, double a0, double a1, std::vector<double>& out) {
-    for (double v = c0 + s2; v <= a1 && out.size() < 100000; v += sml) out.push_back(v);
-    for (double v = c0 - s2; v >= a0 && out.size() < 200000; v -= sml) out.push_back(v);
+    for (double v = c0 + s2; v <= a1; v += sml) out.push_back(v);
+    for (double v = c0 - s2; v >= a0; v -= sml) out.push_back(v);
   };
   std::vector<double> xs, ys, zs, xy;
   side(duct->x0, -r, r, xs);
   side(duct->y0, -r, r, ys);
-  for (double z = hi[2] - s2; z >= lo[2] && zs.size() < 100000; z -= sml) zs.push_back(z);
+  for (double z = hi[2] - s2; z >= lo[2]; z -= sml) zs.push_back(z);
   for (double x : xs)
     for (double y : ys)
       if (x * x + y * y <= r * r) {
@@ -3336,8 +3398,6 @@ int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, 
       }
   const int npairs = (int)(xy.size() / 2), nz = (int)zs.size();
   const size_t nnew = (size_t)npairs * (size_t)nz;
-  int rc = search(ctx);
-  if (rc) return rc;
   if (ctx->n_alloc + nnew > ctx->cap) {
     ctx->err = "setup_erupt exceeds capacity";
     return PLUME_E_CAPACITY;
@@ -3346,13 +3406,10 @@ int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, 
   ScratchFree scratch;
   double *dxy = nullptr, *dz = nullptr;
   unsigned int* drem = nullptr;
+  // every scratch buffer is allocated and filled before the removal kernel
+  // marks particles dead, so a failure leaves the table untouched
   CK(cudaMalloc(&drem, sizeof(unsigned int)));
   scratch.p[0] = drem;
-  CK(cudaMemsetAsync(drem, 0, sizeof(unsigned int), st));
-  const int n = (int)ctx->n_alloc;
-  k_duct_remove<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, r * r, lo[2], hi[2], drem);
-  CK(cudaGetLastError());
-  ctx->launches++;
   if (nnew) {
     CK(cudaMalloc(&dxy, 8 * xy.size()));
     scratch.p[1] = dxy;
@@ -3360,6 +3417,17 @@ int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, 
     scratch.p[2] = dz;
     CK(cudaMemcpyAsync(dxy, xy.data(), 8 * xy.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dz, zs.data(), 8 * zs.size(), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemsetAsync(drem, 0, sizeof(unsigned int), st));
+  const int n = (int)ctx->n_alloc;
+  k_duct_remove<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, r * r, lo[2], hi[2], drem);
+  // from here on the table may hold dead rows: the next search compacts them
+  const bool had_dead = ctx->has_dead;
+  ctx->pending_dead = true;
+  ctx->has_dead = true;
+  CK(cudaGetLastError());
+  ctx->launches++;
+  if (nnew) {
     k_duct_fill<<<nblocks(nnew), NTHREADS, 0, st>>>(ctx->d_opt, ctx->A, dxy, npairs, dz, nz, *duct, mss, sml,
                                                    ctx->n_alloc, (unsigned long long)key_base);
     CK(cudaGetLastError());
@@ -3372,8 +3440,7 @@ int plume_setup_erupt(plume_ctx* ctx, const PlumeDuct* duct, uint64_t key_base, 
     rc = set_count(ctx, ctx->n_alloc + nnew);
     if (rc) return rc;
   }
-  if (nnew || nrem) ctx->pending_dead = true;
-  if (nrem) ctx->has_dead = true;
+  ctx->has_dead = had_dead || nrem != 0;
   *added = nnew;
   *removed = nrem;
   if (mass_out) *mass_out = mss;

@@ -74,6 +74,8 @@ def lib():
         L.plume_set_time.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_double]
         L.plume_neighbor_pairs.argtypes = [C.c_void_p, C.c_int, P(C.c_uint64), P(C.c_uint64),
                                            C.c_size_t, P(C.c_size_t)]
+        L.plume_neighbor_pairs_of.argtypes = [C.c_void_p, C.c_int, P(C.c_uint64), C.c_size_t, P(C.c_uint64),
+                                              P(C.c_uint64), C.c_size_t, P(C.c_size_t)]
         L.plume_phase_times.argtypes = [C.c_void_p, P(C.c_float), C.c_int]
         L.plume_launch_count.argtypes = [C.c_void_p, P(C.c_uint64)]
         L.plume_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]

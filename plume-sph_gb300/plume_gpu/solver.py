@@ -335,11 +335,25 @@ class Solver:
             kj.ctypes.data_as(C.POINTER(C.c_uint64)), n.value, C.byref(n)), "plume_neighbor_pairs")
         return ki, kj
 
+    def pairs_of(self, keys, mode: int = 0):
+        """pairs() of the need_neigh particles whose keys are in `keys`"""
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        kp = keys.ctypes.data_as(C.POINTER(C.c_uint64))
+        n = C.c_size_t()
+        self._check(self.L.plume_neighbor_pairs_of(self.ctx, mode, kp, len(keys), None, None, 0, C.byref(n)),
+                    "plume_neighbor_pairs_of")
+        ki = np.zeros(n.value, dtype=np.uint64)
+        kj = np.zeros(n.value, dtype=np.uint64)
+        self._check(self.L.plume_neighbor_pairs_of(
+            self.ctx, mode, kp, len(keys), ki.ctypes.data_as(C.POINTER(C.c_uint64)),
+            kj.ctypes.data_as(C.POINTER(C.c_uint64)), n.value, C.byref(n)), "plume_neighbor_pairs_of")
+        return ki, kj
+
     def phase_times(self):
-        ms = (C.c_float * 12)()
-        self._check(self.L.plume_phase_times(self.ctx, ms, 12), "plume_phase_times")
+        ms = (C.c_float * 14)()
+        self._check(self.L.plume_phase_times(self.ctx, ms, 14), "plume_phase_times")
         names = ["search", "adaptive", "lists", "momentum", "commit_mom", "density", "commit_dens",
-                 "velocity", "position", "dt", "total", "mom_kernel"]
+                 "velocity", "position", "dt", "total", "mom_kernel", "inlet", "wall_bc"]
         return dict(zip(names, list(ms)))
 
     def launches(self) -> int:

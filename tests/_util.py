@@ -103,3 +103,22 @@ def field_errors(a: ParticleSet, b: ParticleSet, fields=DOUBLE_FIELDS):
         scale = max(float(np.abs(y).max()) if y.size else 0.0, 1e-300)
         out[f] = float(np.abs(x - y).max() / scale) if y.size else 0.0
     return out
+
+
+# fields that are positive by construction: their error is bounded per
+# particle (the max-normalised bound would let a small value drift)
+POSITIVE_FIELDS = ("mass", "h", "rho", "e", "p", "c", "T", "gamma", "cp")
+
+
+def particle_rel_errors(a: ParticleSet, b: ParticleSet, fields=POSITIVE_FIELDS):
+    """max over particles of |a_i - b_i| / |b_i| per field (b_i != 0), after
+    matching by key"""
+    a = a.sorted_by_key()
+    b = b.sorted_by_key()
+    assert np.array_equal(a.key, b.key)
+    out = {}
+    for f in fields:
+        x, y = getattr(a, f), getattr(b, f)
+        nz = y != 0
+        out[f] = float((np.abs(x[nz] - y[nz]) / np.abs(y[nz])).max()) if nz.any() else 0.0
+    return out

@@ -26,7 +26,9 @@ state and a summary of the reference's neighbour lists:
                        (make_adapt)
 
 Usage (in a container that has the reference tree):
-  python tests/golden/make_golden.py [--ref /root/reference]
+  python tests/golden/make_golden.py [--ref REFERENCE_TREE]
+(default: $PLUME_REFERENCE, else a directory named "reference" beside this
+checkout)
 """
 from __future__ import annotations
 
@@ -125,7 +127,7 @@ def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     a = ap.parse_args()
     refio.build_ref(a.ref)
     make(cases.sod_1d(n_real=200, kernel=cases.KERNEL_M4), "ref1d_sod", 20,

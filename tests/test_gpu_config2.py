@@ -1,0 +1,124 @@
+"""The full 3D plume workload against the oracle (FP64) and against FP64 (mixed).
+
+The bench reports the 20 x 20 x 20 km plume at 150 m (134^3 = 2,388,148 air
+particles, 3.09 M with ghosts and the vent duct, 85,248 wall images, the
+eruption inlet) on the fine-cell tile the autotuner picks there (5^3 cells
+per bucket).  These tests run that geometry and that tile:
+
+* two FP64 steps across the adaptive-h pass of step 50 (step 51 runs at
+  h ~ 1.5 dx, where a particle's masked neighbour windows come closest to
+  their capacity), GPU vs the oracle: fields within 1e-10 (max-normalised,
+  and per particle for the positive fields), byte fields and keys equal
+  (the inlet's particles included);
+* the neighbour sets of both list rules on a sample of 2,500 particles of
+  the state after those steps (random ones plus the ones nearest the vent
+  and the ground), bit-exact against the oracle on identical inputs;
+* the mixed path's relative L1 density error against the FP64 path after
+  the same steps <= 1e-4.
+
+The oracle needs about 25 GB of host memory for the lists at h ~ 1.5 dx
+and a minute or two on 16 cores.
+"""
+import numpy as np
+import pytest
+
+from oracle.binding import OracleRun
+from plume_gpu import PREC_MIXED, Solver, cases
+from plume_gpu.autotune import with_subcells
+from _util import field_errors, particle_rel_errors, set_summary
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+SUBCELLS = 5
+
+
+@pytest.fixture(scope="module")
+def config2():
+    case = with_subcells(cases.plume_config2(seed=0), SUBCELLS)
+    case.step0 = 49  # the next step is 50: adaptive h, then step 51 at h ~ 1.5 dx
+    images = cases.wall_images(case)
+    inlet = cases.inlet(case)
+    return case, images, inlet
+
+
+def _solver(case, images, inlet):
+    s = Solver(case)
+    s.set_wall_images(*images)
+    s.set_inlet(inlet)
+    return s
+
+
+@pytest.fixture(scope="module")
+def fp64_runs(config2):
+    case, images, inlet = config2
+    s = _solver(case, images, inlet)
+    s.steps(2)
+    s.apply_bcond()
+    g = s.download()
+    s.close()
+    o = OracleRun(case)
+    o.set_images(*images)
+    o.set_inlet(inlet)
+    o.apply_bcond()
+    o.steps(2)
+    return g, o.ps
+
+
+def test_config2_fp64_two_steps_across_adaptive_h_match_oracle(config2, fp64_runs):
+    case, _, inlet = config2
+    g, o = fp64_runs
+    assert g.n == o.n
+    err = field_errors(g, o)
+    assert max(err.values()) <= FP64_TOL, err
+    rel = particle_rel_errors(g, o)
+    assert max(rel.values()) <= FP64_TOL, rel
+    a, b = g.sorted_by_key(), o.sorted_by_key()
+    for f in ("phase", "bc_type", "involved"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    assert (a.key >= inlet["key_base"]).sum() == (b.key >= inlet["key_base"]).sum()
+    # the adaptive pass ran: h grew from dx to about 1.5 dx in the air
+    real = b.need_neigh()
+    assert np.median(b.h[real]) > 1.4 * 150.0
+
+
+def test_config2_neighbour_sets_on_a_sample_bit_exact(config2, fp64_runs):
+    case, _, _ = config2
+    _, o = fp64_runs
+    ps = o.sorted_by_key()
+    real = np.nonzero(ps.need_neigh())[0]
+    rng = np.random.default_rng(7)
+    pick = set(rng.choice(real, 2000, replace=False).tolist())
+    r2 = ps.x[real] ** 2 + ps.y[real] ** 2 + ps.z[real] ** 2  # vent and ground nearest first
+    pick.update(real[np.argsort(r2)[:500]].tolist())
+    keys = ps.key[np.array(sorted(pick))]
+    import dataclasses
+    same = dataclasses.replace(case, particles=ps)
+    s = Solver(same)  # identical inputs: the oracle's state after the two steps
+    orc = OracleRun(same)
+    for mode in (0, 1):
+        gk, gc, gh = set_summary(*s.pairs_of(keys, mode))
+        ok, oc, oh = set_summary(*orc.pairs_of(keys, mode))
+        assert len(ok) == len(keys)
+        np.testing.assert_array_equal(gk, ok)
+        np.testing.assert_array_equal(gc, oc)
+        np.testing.assert_array_equal(gh, oh)
+    s.close()
+
+
+def test_config2_mixed_density_error_after_adaptive_h(config2, fp64_runs):
+    case, images, inlet = config2
+    g64, _ = fp64_runs
+    mc = with_subcells(cases.plume_config2(seed=0, precision=PREC_MIXED), SUBCELLS)
+    mc.step0 = case.step0
+    s = _solver(mc, images, inlet)
+    s.steps(2)
+    s.apply_bcond()
+    m = s.download().sorted_by_key()
+    s.close()
+    a = g64.sorted_by_key()
+    assert np.array_equal(a.key, m.key)
+    real = a.need_neigh()
+    l1 = np.abs(m.rho[real] - a.rho[real]).sum() / np.abs(a.rho[real]).sum()
+    print(f"config 2, steps 50-51: mixed vs FP64 relative L1 density {l1:.3e}")
+    assert l1 <= 1e-4, l1
