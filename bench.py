@@ -166,18 +166,19 @@ def barrier(dist):
         dist.barrier()
 
 
-def pinned_particles(ps):
-    """copy of a ParticleSet whose arrays live in pinned host memory"""
+def pinned_particles(ps, extra: int = 0):
+    """copy of a ParticleSet whose arrays live in pinned host memory, with
+    `extra` more rows of room (the table grows when the inlet injects)"""
     import torch
     from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS, ParticleSet
     out = ParticleSet(0)
     keep = []
 
     def pin(a):
-        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)) if a.dtype != np.uint64
-                        else torch.int64, pin_memory=True)
+        t = torch.zeros((a.shape[0] + extra,) + a.shape[1:], dtype=getattr(torch, str(a.dtype))
+                        if a.dtype != np.uint64 else torch.int64, pin_memory=True)
         v = t.numpy().view(a.dtype)
-        v[...] = a
+        v[:a.shape[0]] = a
         keep.append(t)
         return v
     out.key = pin(ps.key)
@@ -574,16 +575,18 @@ def main():
     # e2e: through the C ABI with pinned host buffers, every step
     # upload -> step -> download
     from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
-    host = pinned_particles(sol.download())
-    host.key = host.key  # pinned copy of the whole particle table
-    bytes_per = 8 + 8 * len(DOUBLE_FIELDS) + len(BYTE_FIELDS)
     e2e_steps = max(2, min(args.steps, 5))
+    snap = sol.download()
+    grow = 0 if inlet is None else 4 * len(inlet["col_vel"]) * (e2e_steps + 1)
+    host = pinned_particles(snap, extra=grow)  # pinned copy of the whole particle table
+    n_host = snap.n
+    del snap
+    bytes_per = 8 + 8 * len(DOUBLE_FIELDS) + len(BYTE_FIELDS)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     nrs, h2d, d2h = 0, 0, 0
-    n_host = host.n
     for _ in range(e2e_steps):
-        view = host.take(slice(0, n_host)) if n_host != host.n else host
+        view = host.take(slice(0, n_host))
         sol.upload(view)
         h2d += n_host * bytes_per
         sol.steps(1)

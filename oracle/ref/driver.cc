@@ -72,7 +72,9 @@ struct Case {
   std::vector<uint8_t> binv;  // per-bucket has_involved (optional)
   int adapt_mode = 0;         // 1: scan_outside_layer + adapt_domain after the loop,
                               // 2: then add_pressure_ghost, 3: add_wall_ghost alone,
-                              // 4: add_air alone, 5: setup_erupt alone
+                              // 4: add_air alone, 5: setup_erupt alone,
+                              // 6: setup_erupt before the loop and
+                              //    add_new_erupt in every step
 };
 
 static void rd(FILE *fp, void *p, size_t sz, size_t cnt) {
@@ -459,6 +461,11 @@ int main(int argc, char **argv) {
     }
   }
   for (size_t b = 0; b < bucks.size(); b++) bucks[b]->put_plist(plists[b]);
+#if defined(PLUME_ADJUST_DOMAIN)
+  // mode 6: the initial vent duct of setup_erupt (main.cc:156) before the
+  // loop, and the per-step inlet add_new_erupt in it (main.cc:414-421)
+  if (c.adapt_mode == 6) setup_erupt(0, P, BG, tp, matprops, simprops, 1);
+#endif
   // wall images (the table search_bnd_images builds, bnd_image.cc:35-245):
   // the ghost's key and the image point come from the case, the bucket
   // is the one containing the image
@@ -527,6 +534,9 @@ int main(int argc, char **argv) {
 #endif
     update_pos(P, tp, matprops);
     update_particles_in_bucket(0, P, BG, &lost);
+#if defined(PLUME_ADJUST_DOMAIN)
+    if (c.adapt_mode == 6 && tp->iferupt()) add_new_erupt(0, P, BG, tp, matprops, simprops, dt);  // main.cc:414-421
+#endif
     if (!Image_table.empty()) apply_bcond(0, P, BG, matprops, Image_table);  // main.cc:468
 #endif
     tp->ifoutput();
@@ -563,6 +573,8 @@ int main(int argc, char **argv) {
       add_air(P, BG, matprops, simprops, 1, 0);
     dump_state(fo, P, c, *tp, 0.0);
     ndumped++;
+  } else if (c.adapt_mode == 6) {
+    // the duct and the injected particles are the born record below
   } else if (c.adapt_mode) {
     adapt_n = scan_outside_layer(P, BG, 1, 0);
     if (adapt_n) adapt_domain(P, BG, matprops, 1, 0);

@@ -1141,6 +1141,7 @@ struct plume_ctx {
   // 3D sweep walk: one warp per particle (true) or one thread per particle;
   // default per precision, PLUME_SWEEP=warp|thread overrides
   bool sweep_warp = false;
+  bool list_warp = true;  // mixed list sweeps: one warp per particle (k_sweep3_wl)
   uint32_t *keys = nullptr, *perm = nullptr, *cs = nullptr;
   uint32_t ncells = 0;
   int keybits = 1;
@@ -1376,6 +1377,18 @@ static void launch_gsph(plume_ctx* ctx, int nb) {
                                             ctx->ts, recon ? ctx->grad : nullptr);
 }
 
+// a list sweep: mixed path one warp per particle, FP64 path one thread
+template <typename T, template <typename> class SW, bool MULTI>
+static void launch_list_sweep(plume_ctx* ctx, const Geos<MULTI>& gs, int nb, int nbw, const int* cnt,
+                              const uint32_t* idx) {
+  if (sizeof(T) == 4 && ctx->list_warp)
+    k_sweep3_wl<SW, MULTI><<<nbw, NTHREADS, 0, ctx->st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
+                                                          cnt, idx, ctx->ts, ctx->L);
+  else
+    k_sweep3_list<T, SW, MULTI><<<nb, NTHREADS, 0, ctx->st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
+                                                              cnt, idx, ctx->ts, ctx->L);
+}
+
 template <int D, typename T, bool MULTI>
 static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   const Geos<MULTI> gs{ctx->hgeo[0], ctx->d_geo};
@@ -1459,7 +1472,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
     if (gsph)
       launch_gsph<D, T>(ctx, nb);
     else if (lists)
-      k_sweep3_list<T, WMom, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
+      launch_list_sweep<T, WMom, MULTI>(ctx, gs, nb, nbw, sweep_cnt, sweep_idx);
     else if (ctx->sweep_warp)
       k_sweep3<T, WMom, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
@@ -1487,7 +1500,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
       ctx->launches++;
     }
     if (lists)
-      k_sweep3_list<T, WDens, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
+      launch_list_sweep<T, WDens, MULTI>(ctx, gs, nb, nbw, sweep_cnt, sweep_idx);
     else if (ctx->sweep_warp)
       k_sweep3<T, WDens, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
     else
@@ -1510,7 +1523,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         ctx->launches++;
       }
       if (lists)
-        k_sweep3_list<T, WVel, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, sweep_cnt, sweep_idx, ctx->ts, ctx->L);
+        launch_list_sweep<T, WVel, MULTI>(ctx, gs, nb, nbw, sweep_cnt, sweep_idx);
       else if (ctx->sweep_warp)
         k_sweep3<T, WVel, true, MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27, ctx->d_count, ctx->ts);
       else
@@ -1780,6 +1793,7 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
     if (!strcmp(sw, "warp")) { ctx->sweep_warp = true; ctx->use_lists = false; }
     if (!strcmp(sw, "thread")) { ctx->sweep_warp = false; ctx->use_lists = false; }
     if (!strcmp(sw, "list")) { ctx->sweep_warp = false; ctx->use_lists = true; }
+    if (!strcmp(sw, "list_thread")) { ctx->sweep_warp = false; ctx->use_lists = true; ctx->list_warp = false; }
   }
   if (opt->dim == 3 && ctx->use_lists && capacity > (size_t)NL_JMASK) {
     g_create_error = "capacity above the neighbour-list index range (2^26)";

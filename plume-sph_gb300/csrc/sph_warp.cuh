@@ -903,6 +903,122 @@ __global__ void __launch_bounds__(128, SweepMinBlocks<SW>::v) k_sweep3_list(Opt 
   s.template finish<false>(i, W, ts);
 }
 
+// ------------------------------------------------------------ warp list sweeps
+// Mixed-path list sweeps with one warp per particle.  The particle's
+// windows are taken 32 at a time, one per lane; an inclusive warp scan of
+// the windows' set-bit counts places every listed candidate in a per-warp
+// shared-memory queue (j | bucket-offset code << 26), in the walk's order,
+// and the lanes then take the queue 32 pairs at a time.  Every pair of a
+// batch is a listed candidate (no idle lanes but in a particle's last
+// batch), consecutive lanes hold consecutive candidates of the same rows,
+// so a batch's record loads fall on a few cache lines, and the particle's
+// own fields are loaded once per warp (broadcast).  Each lane keeps its own
+// compensated sums; finish<true> adds the lanes' sums in FP64.  The 27
+// positions of i shifted into the neighbouring buckets are formed once per
+// particle in shared memory; a particle whose windows overflowed walks its
+// rows with ballot compaction (wp_walk).
+constexpr int WL_QUEUE = 32 * 32 + 32;  // one chunk of 32 windows + a batch's remainder
+
+template <typename T>
+struct WLShared {
+  uint32_t q[WP_WARPS][WL_QUEUE];
+  float4 sh[WP_WARPS][27];
+  WBuf<T> wb[WP_WARPS];
+};
+
+template <template <typename> class SW>
+struct SweepMinBlocksW { static constexpr int v = 1; };
+#ifndef PLUME_MINB_WMOM
+#define PLUME_MINB_WMOM 5
+#endif
+#ifndef PLUME_MINB_WDENS
+#define PLUME_MINB_WDENS 7
+#endif
+#ifndef PLUME_MINB_WVEL
+#define PLUME_MINB_WVEL 7
+#endif
+template <>
+struct SweepMinBlocksW<WMom> { static constexpr int v = PLUME_MINB_WMOM; };
+template <>
+struct SweepMinBlocksW<WDens> { static constexpr int v = PLUME_MINB_WDENS; };
+template <>
+struct SweepMinBlocksW<WVel> { static constexpr int v = PLUME_MINB_WVEL; };
+
+template <template <typename> class SW, bool MULTI>
+__global__ void __launch_bounds__(128, SweepMinBlocksW<SW>::v)
+    k_sweep3_wl(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K, const uint32_t* __restrict__ cs_all,
+                const double* __restrict__ hmax_all, const int* __restrict__ d_real,
+                const uint32_t* __restrict__ real_idx, TimeState* ts_all, NList L) {
+  using T = float;
+  __shared__ WLShared<T> S;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * WP_WARPS + wid;
+  if (r >= *d_real) return;  // whole warps leave together
+  const int i = (int)real_idx[r];
+  const int m = geo.member(A, i);  // real_idx holds particles of active members only
+  TimeState* ts = ts_all + m;
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
+  SW<T> s(A, K, o);
+  double xi[3], R;
+  int bi[3];
+  if (!s.setup(i, g, W, hmax, ts, xi, bi, R)) return;  // the same for every lane
+  const uint16_t c = L.cnt[i];
+  if (c == NL_OVERFLOW) {
+    wp_walk<T>(g, cs, xi, bi, R, S.wb[wid], s);
+  } else if (c > 0) {
+    uint32_t* q = S.q[wid];
+    float4* sh = S.sh[wid];
+    if (lane < 27) {
+      bool own;
+      T ox, oy, oz;
+      decode_offsets<T>(T(g.del), lane, own, ox, oy, oz);
+      sh[lane] = make_float4(s.xpos()[0] + ox, s.xpos()[1] + oy, s.xpos()[2] + oz, 0.f);
+    }
+    __syncwarp();
+    auto pair = [&](uint32_t e) {
+      const uint32_t j = e & NL_JMASK;
+      const int code = (int)(e >> 26);
+      const float4 p = sh[code];
+      T dx[3], hj;
+      if (s.template filter<true>(j, code == 13, p.x, p.y, p.z, dx, hj)) s.math(j, dx, hj);
+    };
+    const uint2* ent = L.e + (size_t)i * LCAP;
+    int cnt = 0;  // queued candidates (the same in every lane)
+    for (int w0 = 0; w0 < (int)c; w0 += 32) {
+      const uint2 en = (w0 + lane < (int)c) ? ent[w0 + lane] : make_uint2(0u, 0u);
+      uint32_t mask = en.y;
+      const int pc = __popc(mask);
+      int off = pc;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(WFULL, off, d);
+        if (lane >= d) off += v;
+      }
+      const int tot = __shfl_sync(WFULL, off, 31);
+      int pos = cnt + off - pc;
+      const uint32_t base = en.x & NL_JMASK, codeb = en.x & ~NL_JMASK;
+      while (mask) {
+        q[pos++] = (base + (uint32_t)(__ffs(mask) - 1)) | codeb;
+        mask &= mask - 1;
+      }
+      cnt += tot;
+      __syncwarp();
+      int b = 0;
+      for (; b + 32 <= cnt; b += 32) pair(q[b + lane]);
+      const int rest = cnt - b;  // < 32: moved to the queue's front
+      const uint32_t keep = (lane < rest) ? q[b + lane] : 0u;
+      __syncwarp();
+      if (lane < rest) q[lane] = keep;
+      cnt = rest;
+      __syncwarp();
+    }
+    if (lane < cnt) pair(q[lane]);
+  }
+  s.template finish<true>(i, W, ts);
+}
+
 // compacted indices of the need_neigh particles of the stepping members
 // (sorted order kept)
 __global__ void k_real_flags(Dev A, const int* __restrict__ d_count, int n, const TimeState* __restrict__ ts_all,

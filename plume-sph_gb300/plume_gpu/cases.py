@@ -473,6 +473,59 @@ def duct_scenario(case):
     return dataclasses.replace(case, particles=ps, name=case.name + "_duct"), binv, duct
 
 
+def duct_inlet(duct: dict, born: ParticleSet, key_base: int) -> dict:
+    """The inlet of add_new_erupt (setup_erupt.cc:389-673) for a vent duct
+    that setup_erupt built (setup_erupt.cc:44-388) from the duct description
+    of duct_scenario: the columns of the reference's loops (x from the vent
+    axis + sml/2 outward by repeated steps of sml, + side then - side, y the
+    same inside each, kept where x^2 + y^2 <= radius^2), each with the
+    speed of the velocity profile (profile 1: parabolic_vel, 2 u_avg
+    (1 - r^2 / R^2), sph_lib.cc:1223-1227; 0: uniform_vel), the bottom of
+    the duct (simprops bot = z_top - depth), and the state of the duct's
+    particles (sml_of_phase2, mass_of_phase2, rhov, ev0, pv0, gamma_v,
+    sound speed 340, mass fraction 1)."""
+    sml = float(born.h[0])
+    sml2 = 0.5 * sml
+    rv = float(duct["radius"])
+    rvsq = rv * rv
+    x0, y0 = float(duct["x0"]), float(duct["y0"])
+
+    def speed(rsq):
+        if int(duct["profile"]) == 1:
+            umax = float(duct["u_avg"]) * 2
+            return umax * (1 - (rsq / (rv * rv)))
+        return float(duct["u_avg"])
+
+    xy, vel = [], []
+
+    def row(x):
+        for sgn in (1, -1):
+            y = y0 + sgn * sml2
+            while (y <= rv) if sgn > 0 else (y >= -rv):
+                rsq = 0.0
+                rsq += x * x
+                rsq += y * y
+                if rsq <= rvsq:
+                    xy.append((x, y))
+                    vel.append(speed(rsq))
+                y = y + sml if sgn > 0 else y - sml
+
+    x = x0 + sml2
+    while x <= rv:
+        row(x)
+        x += sml
+    x = x0 - sml2
+    while x >= -rv:
+        row(x)
+        x -= sml
+    i0 = 0
+    return {"col_xy": np.array(xy, dtype=np.float64), "col_vel": np.array(vel, dtype=np.float64),
+            "bot": float(duct["z_top"]) - float(duct["depth"]), "spacing": sml,
+            "mass": float(born.mass[i0]), "h": sml, "rho": float(born.rho[i0]), "e": float(born.e[i0]),
+            "p": float(born.p[i0]), "gamma": float(born.gamma[i0]), "c": float(born.c[i0]), "Y": 1.0,
+            "key_base": int(key_base)}
+
+
 def inlet(case):
     """The eruption inlet of add_new_erupt (setup_erupt.cc:389-673) for a
     plume built by plume_3d: the duct's particle columns (spacing vent_dx,

@@ -122,3 +122,34 @@ def particle_rel_errors(a: ParticleSet, b: ParticleSet, fields=POSITIVE_FIELDS):
         nz = y != 0
         out[f] = float((np.abs(x[nz] - y[nz]) / np.abs(y[nz])).max()) if nz.any() else 0.0
     return out
+
+
+def inlet_fixture():
+    """(case, inlet, fixture) of tests/golden/inlet_3d.npz: the plume of
+    cases.duct_scenario with the particles the reference's setup_erupt kept
+    and the duct it built (keys after the case's), and the inlet of
+    add_new_erupt for that duct (keys after the duct's)"""
+    import dataclasses
+    d = dict(np.load(os.path.join(GOLDEN, "inlet_3d.npz")))
+    c, _, duct = cases.duct_scenario(adapt_case())
+    inp = unpack(d, "in_")
+    kept = inp.take(np.nonzero(np.isin(inp.key, d["kept_key"]))[0])
+    born = unpack(d, "duct_")
+    born.key = np.arange(born.n, dtype=np.uint64) + np.uint64(int(inp.key.max()) + 1)
+    ps = ParticleSet.concat([kept, born])
+    c = dataclasses.replace(c, particles=ps, step0=int(d["step0"]))
+    inl = cases.duct_inlet(duct, born, int(born.key.max()) + 1)
+    return c, inl, d
+
+
+def match_by_position(ours: ParticleSet, ref: ParticleSet, tol: float = 1e-6):
+    """rows of `ours` in the order of `ref`'s rows, matched by nearest
+    position (both sets created with keys of their own)"""
+    from scipy.spatial import cKDTree
+    assert ours.n == ref.n, (ours.n, ref.n)
+    pa = np.stack([ours.x, ours.y, ours.z], axis=1)
+    pb = np.stack([ref.x, ref.y, ref.z], axis=1)
+    dist, idx = cKDTree(pa).query(pb)
+    assert dist.max() <= tol, dist.max()
+    assert len(np.unique(idx)) == ref.n
+    return ours.take(idx)

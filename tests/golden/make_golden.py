@@ -149,6 +149,7 @@ def main():
     make_wall_ghost()
     make_air()
     make_duct()
+    make_inlet()
     make_csv()
     make_grid()
 
@@ -268,6 +269,35 @@ def make_duct():
     print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
 
 
+INLET_STEPS = 6
+
+
+def make_inlet():
+    """inlet_3d.npz: the reference's own add_new_erupt.  cases.duct_scenario
+    on the domain-growth plume (seed 6); the reference's setup_erupt alone
+    gives the duct and the case particles it keeps (mode 5, no step); then
+    setup_erupt before the loop and INLET_STEPS steps with add_new_erupt in
+    each (mode 6).  Stores the input, the duct, the kept keys, the case
+    particles after the steps, the step times, and every particle the run
+    created (duct and inlet) in its final state."""
+    c, binv, duct = cases.duct_scenario(adapt_case())
+    s5, _ = refio.run_ref("ref3d_adapt", c, 0, "/tmp/plume_golden", binv=binv, adapt=5)
+    s6, _ = refio.run_ref("ref3d_adapt", c, INLET_STEPS, "/tmp/plume_golden", binv=binv, adapt=6)
+    d = {"nsteps": INLET_STEPS, "step0": c.step0, "pre_adaptive": 0, "dim": 3, "binv_in": binv,
+         "kept_key": np.sort(s5[-1]["particles"].key),
+         "dt": np.array([r["dt"] for r in s6[:INLET_STEPS]]),
+         "time": np.array([r["time"] for r in s6[:INLET_STEPS]]),
+         "duct": np.array([duct[k] for k in ("x0", "y0", "z_top", "depth", "radius", "np", "profile",
+                                             "u_avg")], dtype=np.float64)}
+    d.update(pack("in_", c.particles))
+    d.update(pack("duct_", s5[-1]["born"]))
+    d.update(pack("out_", s6[INLET_STEPS - 1]["particles"]))
+    d.update(pack("born_", s6[-1]["born"]))
+    path = os.path.join(HERE, "inlet_3d.npz")
+    np.savez_compressed(path, **d)
+    print(f"wrote {path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 GRID_DOMAINS = (
     # (name, lo, hi, h0, nproc): the 20 km plume domain at 150 m, the 600 m
     # test plume at 50 m, and a ragged domain above 1.5 km (bucket counts
@@ -332,6 +362,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--duct":
         refio.build_ref()
         make_duct()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--inlet":
+        refio.build_ref()
+        make_inlet()
     elif len(sys.argv) > 1 and sys.argv[1] == "--air":
         refio.build_ref()
         make_air()

@@ -16,7 +16,7 @@ import pytest
 
 from oracle.binding import OracleRun
 from plume_gpu import PREC_MIXED, Solver, cases
-from plume_gpu.abi import BYTE_FIELDS
+from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
 from _util import field_errors, golden_case, particle_rel_errors, set_summary, unpack
 
 pytestmark = pytest.mark.gpu
@@ -281,4 +281,35 @@ def test_inlet_and_wall_boundary_match_oracle():
     o.steps(6)
     g = s.download()
     assert g.n == o.ps.n and (g.key >= inl["key_base"]).sum() == 24
+    _check_fields(g, o.ps, FP64_TOL)
+
+
+def test_inlet_matches_reference_add_new_erupt():
+    """k_inject against the reference's own add_new_erupt (fixture
+    inlet_3d.npz: the duct setup_erupt built, six steps with the inlet,
+    parabolic inflow profile): per-step dt within 1e-12, the case's
+    particles within 1e-10, the created particles (duct and inlet, matched
+    by position) with the same types and fields within 1e-10; and against
+    the oracle with identical keys"""
+    from _util import inlet_fixture, match_by_position
+    c, inl, d = inlet_fixture()
+    s = Solver(c)
+    s.set_inlet(inl)
+    log = s.steps(int(d["nsteps"]), log=True)
+    np.testing.assert_allclose([r["dt"] for r in log], d["dt"], rtol=1e-12, atol=0)
+    g = s.download()
+    base = int(inl["key_base"]) - unpack(d, "duct_").n
+    case_rows = g.key < np.uint64(base)
+    err = field_errors(g.take(np.nonzero(case_rows)[0]), unpack(d, "out_"))
+    assert max(err.values()) <= FP64_TOL, err
+    ref = unpack(d, "born_")
+    born = match_by_position(g.take(np.nonzero(~case_rows)[0]), ref)
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(born, f), getattr(ref, f), err_msg=f)
+    err = {f: float(np.abs(getattr(born, f) - getattr(ref, f)).max() / max(np.abs(getattr(ref, f)).max(), 1e-300))
+           for f in DOUBLE_FIELDS}
+    assert max(err.values()) <= FP64_TOL, err
+    o = OracleRun(c)
+    o.set_inlet(inl)
+    o.steps(int(d["nsteps"]))
     _check_fields(g, o.ps, FP64_TOL)

@@ -392,3 +392,47 @@ def test_oracle_setup_erupt_matches_reference():
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
     for f in BYTE_FIELDS:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+
+
+def test_oracle_inlet_matches_reference_add_new_erupt():
+    """The reference's own add_new_erupt (setup_erupt.cc:389-673) against
+    the oracle's restatement: the duct that setup_erupt built, then six
+    steps with the inlet in each (main.cc:414-421).  Per-step dt and time
+    within 1e-12 (later 3D steps sum in the reference's re-ordered bucket
+    lists); the case's particles within 1e-10 (max-normalised) and the
+    particles the run created (duct and inlet; matched by position, the
+    reference keys them by Hilbert keys of the creation step) the same count
+    with the same types and fields within 1e-10."""
+    from _util import inlet_fixture, match_by_position
+    c, inl, d = inlet_fixture()
+    o = OracleRun(c)
+    o.set_inlet(inl)
+    dts = o.steps(int(d["nsteps"]))
+    np.testing.assert_allclose(dts, d["dt"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(o.t.time, float(d["time"][-1]), rtol=1e-12, atol=0)
+    base = int(inl["key_base"]) - len(unpack(d, "duct_").key)
+    case_rows = o.ps.key < np.uint64(base)
+    err = field_errors(o.ps.take(np.nonzero(case_rows)[0]), unpack(d, "out_"))
+    assert max(err.values()) <= 1e-10, err
+    ref = unpack(d, "born_")
+    born = match_by_position(o.ps.take(np.nonzero(~case_rows)[0]), ref)
+    injected = int((o.ps.key >= np.uint64(inl["key_base"])).sum())
+    assert injected == ref.n - unpack(d, "duct_").n > 0
+    for f in BYTE_FIELDS:
+        np.testing.assert_array_equal(getattr(born, f), getattr(ref, f), err_msg=f)
+    for f in DOUBLE_FIELDS:
+        x, y = getattr(born, f), getattr(ref, f)
+        scale = max(float(np.abs(y).max()), 1e-300)
+        assert float(np.abs(x - y).max()) <= 1e-10 * scale, f
+
+
+def test_duct_inlet_columns_follow_the_reference_loops():
+    """cases.duct_inlet: one column per duct lattice column of setup_erupt
+    (the same loops), every column inside the vent radius"""
+    from _util import inlet_fixture
+    c, inl, d = inlet_fixture()
+    duct = unpack(d, "duct_")
+    cols = {(float(x), float(y)) for x, y in zip(duct.x, duct.y)}
+    got = {(float(x), float(y)) for x, y in inl["col_xy"]}
+    assert got == cols
+    assert np.all((inl["col_xy"] ** 2).sum(1) <= 120.0 ** 2)
