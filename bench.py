@@ -336,7 +336,7 @@ def ensemble_3d(steps=10, warm=10, members=64, fp64_steps=2):
             "mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
 
 
-def adjoint_leg(steps=300, every=25, n_air=2.0e5, fd_rels=()):
+def adjoint_leg(steps=300, every=25, n_air=2.0e5, fd_rels=(), fd_steps=60, fd_rel=1e-10):
     """Gradient of the plume observable w.r.t. (vent velocity, temperature,
     ash fraction) through the hand-written adjoint on the config-4 geometry
     (60 m lattice) sized for n_air air particles: the time of one FP64
@@ -368,8 +368,21 @@ def adjoint_leg(steps=300, every=25, n_air=2.0e5, fd_rels=()):
     for rel in fd_rels:
         t0 = time.perf_counter()
         gf = adjoint.finite_difference(theta, case, steps, rel=rel, **obj)
-        out["fd"].append({"rel_step": rel, "grad": gf.tolist(),
+        out["fd"].append({"steps": steps, "rel_step": rel, "grad": gf.tolist(),
                           "rel_err": (np.abs(g - gf) / np.maximum(np.abs(g), 1e-300)).tolist(),
+                          "seconds": time.perf_counter() - t0})
+    # the same geometry and objective over fd_steps steps: the adjoint
+    # gradient against central differences with a relative step small enough
+    # to cross none of the forward map's jumps (the Gaussian's box cut-off,
+    # erupt-to-real conversions); over much longer windows the map is
+    # chaotic and no difference step can confirm the gradient
+    if fd_steps:
+        t0 = time.perf_counter()
+        _, gs = adjoint.value_and_grad(theta, case, fd_steps, every, **obj)
+        gf = adjoint.finite_difference(theta, case, fd_steps, rel=fd_rel, **obj)
+        out["fd"].append({"steps": fd_steps, "rel_step": fd_rel, "grad_adjoint": gs.tolist(),
+                          "grad": gf.tolist(),
+                          "rel_err": (np.abs(gs - gf) / np.maximum(np.abs(gs), 1e-300)).tolist(),
                           "seconds": time.perf_counter() - t0})
     return out
 

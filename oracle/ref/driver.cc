@@ -30,6 +30,7 @@
 //   uint64 key_j[len] (list order as stored by the reference); GSPH builds
 //   (USE_GSPH 1) then append the last step's gradients (dump_gradients).
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -508,7 +509,11 @@ int main(int argc, char **argv) {
 #endif
   int lost = 0;
   int ndumped = 0;
+  // ORACLE_STEP_TIMES set: the wall time of every step on stderr (the
+  // reference's single-thread speed, beside the oracle port's)
+  const bool step_times = getenv("ORACLE_STEP_TIMES") != NULL;
   for (int st = 0; c.nsteps < 0 ? !tp->ifend() : st < c.nsteps; st++) {
+    const auto t_step = std::chrono::steady_clock::now();
 #if CODE_DIMENSION == 1
     double dt = timestep(P, tp);
     tp->incrtime(&dt);
@@ -539,6 +544,9 @@ int main(int argc, char **argv) {
 #endif
     if (!Image_table.empty()) apply_bcond(0, P, BG, matprops, Image_table);  // main.cc:468
 #endif
+    if (step_times)
+      fprintf(stderr, "STEP_SECONDS %d %.6f\n", tp->step,
+              std::chrono::duration<double>(std::chrono::steady_clock::now() - t_step).count());
     tp->ifoutput();
     bool last = (c.nsteps < 0) ? tp->ifend() : (st == c.nsteps - 1);
     if (!c.dump_last || last) {

@@ -1141,7 +1141,7 @@ struct plume_ctx {
   // 3D sweep walk: one warp per particle (true) or one thread per particle;
   // default per precision, PLUME_SWEEP=warp|thread overrides
   bool sweep_warp = false;
-  bool list_warp = true;  // mixed list sweeps: one warp per particle (k_sweep3_wl)
+  bool list_warp = false;  // mixed list sweeps: one warp per particle (k_sweep3_wl), opt-in
   uint32_t *keys = nullptr, *perm = nullptr, *cs = nullptr;
   uint32_t ncells = 0;
   int keybits = 1;
@@ -1377,6 +1377,35 @@ static void launch_gsph(plume_ctx* ctx, int nb) {
                                             ctx->ts, recon ? ctx->grad : nullptr);
 }
 
+// The compacted need_neigh particles of the stepping members: in sorted
+// order (the list build's order) and, for single runs, tile by tile (the
+// sweeps' order).  They depend on the particle types and cells only, so
+// they can be formed before the adaptive-h pass.
+template <bool MULTI>
+static void compact_real(plume_ctx* ctx, int n, int nb, bool tiled) {
+  cudaStream_t st = ctx->st;
+  const int ns = n ? n : 1, nsb = (ns + 1023) / 1024;
+  k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->ts, ctx->rflag);
+  k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, ns, ctx->roffs, ctx->rsums);
+  k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
+  k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, ns, ctx->rsums);
+  k_real_scatter<<<nb, NTHREADS, 0, st>>>(ctx->rflag, ctx->roffs, ns, ctx->real_idx, ctx->d_real, ctx->rtot);
+  ctx->launches += 5;
+  if (tiled) {
+    const Geo& g0 = ctx->hgeo[0];
+    const int ntx = (g0.G[0] + TILE_X - 1) / TILE_X, nty = (g0.G[1] + TILE_Y - 1) / TILE_Y;
+    const int nt = ctx->ntiles, ntb = (nt + 1023) / 1024;
+    k_tile_count<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
+                                                   ctx->tcount);
+    k_scan_blocks<<<ntb, 1024, 0, st>>>(ctx->tcount, nt, ctx->toffs, ctx->tsums);
+    k_scan_sums<<<1, 1024, 0, st>>>(ctx->tsums, ntb, ctx->ttot);
+    k_scan_add<<<ntb, 1024, 0, st>>>(ctx->toffs, nt, ctx->tsums);
+    k_tile_fill<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
+                                                  ctx->toffs, ctx->ttot, ctx->real_tile, ctx->d_real_tile);
+    ctx->launches += 5;
+  }
+}
+
 // a list sweep: mixed path one warp per particle, FP64 path one thread
 template <typename T, template <typename> class SW, bool MULTI>
 static void launch_list_sweep(plume_ctx* ctx, const Geos<MULTI>& gs, int nb, int nbw, const int* cnt,
@@ -1396,12 +1425,29 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   const int n = (int)ctx->n_alloc;
   const int nb = nblocks(n);
   AdjRec* rec = ctx->rec;
-  if (adaptive_now || (ctx->capturing && ctx->o.adaptive)) {
+  const bool lists = (D == 3) && ctx->use_lists;
+  // order of the list sweeps: tile by tile for single runs
+  const bool tiled = !MULTI && ctx->ntiles;
+  const uint32_t* sweep_idx = tiled ? ctx->real_tile : ctx->real_idx;
+  const int* sweep_cnt = tiled ? ctx->d_real_tile : ctx->d_real;
+  bool compacted = false;
+  const bool adapt = adaptive_now || (ctx->capturing && ctx->o.adaptive);
+  if (adapt) {
     // a captured step decides on the device (step counter % interval)
-    k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
-                                              ctx->d_hstep, ctx->capturing ? 0 : 1, rec ? rec->hit : nullptr,
-                                              rec ? rec->nit : nullptr, n);
-    ctx->launches++;
+    if (D == 3 && sizeof(T) == 4 && lists && !rec) {
+      // mixed 3D: over the compacted particles, packed records
+      compact_real<MULTI>(ctx, n, nb, tiled);
+      compacted = true;
+      k_pack_adapt<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->o.pgc, ctx->d_count);
+      k_adaptive_mixed<MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, sweep_cnt,
+                                                       sweep_idx, ctx->ts, ctx->d_hstep, ctx->capturing ? 0 : 1);
+      ctx->launches += 2;
+    } else {
+      k_adaptive<D, T><<<nb, NTHREADS, 0, st>>>(ctx->o, ctx->d_geo, ctx->A, ctx->W, ctx->cs, ctx->d_count, ctx->ts,
+                                                ctx->d_hstep, ctx->capturing ? 0 : 1, rec ? rec->hit : nullptr,
+                                                rec ? rec->nit : nullptr, n);
+      ctx->launches++;
+    }
   }
   if (rec) {
     dcopy(rec->h1, ctx->A.h, 8 * (size_t)n, st);
@@ -1416,35 +1462,9 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
   const bool mixed = sizeof(T) == 4;
   const bool gsph = ctx->o.method == PLUME_METHOD_GSPH;
-  const bool lists = (D == 3) && ctx->use_lists;
-  // order of the list sweeps: tile by tile for single runs
-  const bool tiled = !MULTI && ctx->ntiles;
-  const uint32_t* sweep_idx = tiled ? ctx->real_tile : ctx->real_idx;
-  const int* sweep_cnt = tiled ? ctx->d_real_tile : ctx->d_real;
   if constexpr (D == 3) {
     if (lists) {
-      const int ns = n ? n : 1, nsb = (ns + 1023) / 1024;
-      // the list build walks the need_neigh particles in sorted order; the
-      // sweeps of a single run walk them tile by tile
-      k_real_flags<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ns, ctx->ts, ctx->rflag);
-      k_scan_blocks<<<nsb, 1024, 0, st>>>(ctx->rflag, ns, ctx->roffs, ctx->rsums);
-      k_scan_sums<<<1, 1024, 0, st>>>(ctx->rsums, nsb, ctx->rtot);
-      k_scan_add<<<nsb, 1024, 0, st>>>(ctx->roffs, ns, ctx->rsums);
-      k_real_scatter<<<nb, NTHREADS, 0, st>>>(ctx->rflag, ctx->roffs, ns, ctx->real_idx, ctx->d_real, ctx->rtot);
-      ctx->launches += 5;
-      if (tiled) {
-        const Geo& g0 = ctx->hgeo[0];
-        const int ntx = (g0.G[0] + TILE_X - 1) / TILE_X, nty = (g0.G[1] + TILE_Y - 1) / TILE_Y;
-        const int nt = ctx->ntiles, ntb = (nt + 1023) / 1024;
-        k_tile_count<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
-                                                       ctx->tcount);
-        k_scan_blocks<<<ntb, 1024, 0, st>>>(ctx->tcount, nt, ctx->toffs, ctx->tsums);
-        k_scan_sums<<<1, 1024, 0, st>>>(ctx->tsums, ntb, ctx->ttot);
-        k_scan_add<<<ntb, 1024, 0, st>>>(ctx->toffs, nt, ctx->tsums);
-        k_tile_fill<<<nblocks(nt), NTHREADS, 0, st>>>(g0, ctx->A, ctx->cs, ctx->d_count, ctx->ts, ntx, nty, nt,
-                                                      ctx->toffs, ctx->ttot, ctx->real_tile, ctx->d_real_tile);
-        ctx->launches += 5;
-      }
+      if (!compacted) compact_real<MULTI>(ctx, n, nb, tiled);
       if (mixed) {
         k_pack_pos<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
         ctx->launches++;
@@ -1793,7 +1813,7 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
     if (!strcmp(sw, "warp")) { ctx->sweep_warp = true; ctx->use_lists = false; }
     if (!strcmp(sw, "thread")) { ctx->sweep_warp = false; ctx->use_lists = false; }
     if (!strcmp(sw, "list")) { ctx->sweep_warp = false; ctx->use_lists = true; }
-    if (!strcmp(sw, "list_thread")) { ctx->sweep_warp = false; ctx->use_lists = true; ctx->list_warp = false; }
+    if (!strcmp(sw, "list_warp")) { ctx->sweep_warp = false; ctx->use_lists = true; ctx->list_warp = true; }
   }
   if (opt->dim == 3 && ctx->use_lists && capacity > (size_t)NL_JMASK) {
     g_create_error = "capacity above the neighbour-list index range (2^26)";

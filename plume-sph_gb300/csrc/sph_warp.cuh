@@ -1089,6 +1089,83 @@ __global__ void k_tile_fill(Geo g, Dev A, const uint32_t* __restrict__ cs, const
     }
 }
 
+// ------------------------------------------------------------ adaptive h, mixed
+// adaptive_sml (neighs.cc:479-693) on the mixed path: one thread per
+// need_neigh particle of the stepping members, over the compacted (and, for
+// single runs, tile-ordered) index list, candidates from packed FP32 records
+// P = (xr, yr, zr, m or -1 when the particle does not contribute to the
+// density); the kernel support test and the weight on one reciprocal of
+// H* = c_smooth h.  The fixed-point iteration, its stopping rule and the
+// h update are those of k_adaptive (FP64 per particle).
+__global__ void k_pack_adapt(Dev A, Packed K, Work W, int pgc, const int* __restrict__ d_count) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], contr_dens(A.bc[j], pgc) ? (float)A.mass[j] : -1.0f);
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(128) k_adaptive_mixed(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                        const uint32_t* __restrict__ cs_all,
+                                                        const int* __restrict__ d_real,
+                                                        const uint32_t* __restrict__ real_idx, TimeState* ts_all,
+                                                        const int* __restrict__ hstep, int force) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= *d_real) return;
+  if (!force && (*hstep % o.interval) != 0) return;
+  const int i = (int)real_idx[r];
+  const int m = geo.member(A, i);  // real_idx holds particles of active members only
+  TimeState* ts = ts_all + m;
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double xi[3] = {A.x[i], A.y[i], A.z[i]};
+  int bi[3];
+  bucket_coords<3>(g, A.bkt[i], bi);
+  float xs[3];
+  Pos<3, float>::load(A, W, i, xs);
+  const float Lb = float(o.list_factor * W.hlist[i]);
+  const double mi = A.mass[i];
+  double hcur = A.h[i];
+  for (int loop = 0; loop < o.num_loop; loop++) {
+    const double H_old = hcur;
+    const double H_star_d = H_old * o.c_smooth;
+    const float H_star = float(H_star_d);
+    const float supp = float(o.cutoff2) * H_star;
+    const float inv = 1.0f / H_star;
+    const float rn = float(T1_INV_SQRT_PI) * inv;
+    const float r3 = rn * rn * rn;
+    Acc<float> rho_star;
+    const double R = fmin(o.cutoff2, o.ksupport) * H_star_d * (1.0 + 1e-10);
+    for_segments<3, float>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, float ox, float oy, float oz) {
+      const float xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
+      for (uint32_t j = j0; j < j1; j++) {
+        const float4 p = K.P[j];
+        if (p.w < 0.0f) continue;
+        const float dx[3] = {xsh[0] - p.x, xsh[1] - p.y, xsh[2] - p.z};
+        if (!own && !in_box<3, float>(dx, Lb)) continue;
+        if (!in_box<3, float>(dx, supp)) continue;
+        const float si[3] = {dx[0] * inv, dx[1] * inv, dx[2] * inv};
+        float w;
+        if (o.kernel != 1)
+          w = (fabsf(si[0]) > 3.0f || fabsf(si[1]) > 3.0f || fabsf(si[2]) > 3.0f)
+                  ? 0.0f
+                  : r3 * __expf(-(si[0] * si[0] + si[1] * si[1] + si[2] * si[2]));
+        else
+          w = kw<3, float>(o.kernel, si, H_star);
+        rho_star.add(w * p.w);
+      }
+    });
+    const double rs = (double)rho_star.get();
+    const double H_new = o.eta * cbrt(mi / rs);
+    hcur = 1.0 * H_new;
+    if (!(H_new > 0) || !isfinite(H_new)) {
+      set_status(ts, 4);
+      break;
+    }
+    if (fabs((H_new - H_old) / H_old) < o.thresh) break;
+  }
+  A.h[i] = hcur;
+}
+
 // position records for the list build: P (xr, yr, zr, h)
 __global__ void k_pack_pos(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;

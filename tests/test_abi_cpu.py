@@ -156,3 +156,23 @@ def test_plume_ensemble_builder():
     keys = ["dim", "precision", "kernel", "lans", "alpha", "beta", "cutoff2", "list_factor"]
     for k in keys:
         assert len({getattr(c.options, k) for c in cs}) == 1, k
+
+
+def test_reference_side_bridge_compiles_and_round_trips():
+    """plume-sph_gb300/bridge/gpu_bridge.cc, the binding a Plume-SPH build
+    adds to src/plume/, compiled against the reference's own headers
+    (particle.h, thashtab.h, parameters.h) and linked with the reference's
+    particle and hash-table objects and libplume_gpu.so; its self-test packs
+    a table, applies a device-like change (reorder, delete, update, create)
+    and unpacks it without a GPU"""
+    import subprocess
+    sys_ref = os.environ.get("PLUME_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
+    if not os.path.isdir(os.path.join(sys_ref, "src", "datstr")):
+        pytest.skip("the reference tree is not present")
+    plume_gpu.build()
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "bridge", f"REF={sys_ref}"],
+                   check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "bridge", "gpu_bridge_selftest")
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "self-test: ok" in r.stdout
