@@ -483,6 +483,9 @@ def main():
                     help="leave the wall ghosts' states fixed (no apply_bcond in the step)")
     ap.add_argument("--no-inlet", action="store_true",
                     help="no eruption inlet (add_new_erupt) in the step")
+    ap.add_argument("--only-riemann1d", action="store_true",
+                    help="run only the 1D Riemann ensemble leg (--steps timed steps after --warmup) "
+                         "and print its object")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="also report the mixed path's density error against FP64 after this "
                          "many steps (beyond the timed window's end)")
@@ -504,6 +507,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     plume_gpu.build()
+    if args.only_riemann1d:
+        print(json.dumps(ensemble_1d(steps=args.steps, warm=args.warmup)), flush=True)
+        return 0
 
     def make(prec):
         if args.small:

@@ -460,9 +460,24 @@ __global__ void k_bc_map(Dev A, const int* __restrict__ d_count, const uint64_t*
 // coordinates, fields narrowed on the integer pipe, compensated FP32 sums.
 constexpr int BCG = 8;  // threads per image slot (a power of two dividing 32)
 
+// wall-boundary candidate records of the mixed path, written after the
+// step's sort: P (xr, yr, zr, h; -h when the particle is not a real or
+// pressure-ghost particle, contr_image), Q (m, m/rho, e, Y), R (vx, vy, vz)
+__global__ void k_pack_bc(Dev A, Packed K, Work W, const int* __restrict__ d_count) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= *d_count) return;
+  const uint8_t bc = A.bc[j];
+  const bool c = bc == 100 || bc == 99 || bc == 1;
+  const float h = f32_rz(A.h[j]);
+  const float m = f32_rz(A.mass[j]);
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], c ? h : -h);
+  K.Q[j] = make_float4(m, m * __fdividef(1.0f, f32_rz(A.rho[j])), f32_rz(A.e[j]), f32_rz(A.Y[j]));
+  K.R[j] = make_float4(f32_rz(A.vx[j]), f32_rz(A.vy[j]), f32_rz(A.vz[j]), 0.0f);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict__ mopt, const Geo* __restrict__ geo,
-                                                          Dev A, Work W, const uint32_t* __restrict__ cs_all,
+                                                          Dev A, Work W, Packed K, const uint32_t* __restrict__ cs_all,
                                                           const double* __restrict__ h27_all,
                                                           const int* __restrict__ map, int nslots, int nimg,
                                                           const double* __restrict__ ixyz, TimeState* ts_all) {
@@ -529,32 +544,40 @@ __global__ void __launch_bounds__(NTHREADS) k_apply_bcond(const Opt* __restrict_
       const float oy = (float)(bi[1] - by) * delf, oz = (float)(bi[2] - bz) * delf;
       const float ox0 = (float)(bi[0] - bx0) * delf;
       for (uint32_t j = j0; j < j1; j++) {
-        const uint8_t bc = A.bc[j];
-        if (!(bc == 100 || bc == 99 || bc == 1)) continue;
         const int run = (j >= s1) + (j >= s2);
         const bool own = run == own_run;
         if constexpr (MIXED) {
+          // packed records (k_pack_bc); the field records are read only
+          // inside the kernel's support (zero weight outside)
+          const float4 p = K.P[j];
+          if (!(p.w > 0.0f)) continue;
           const float ox = ox0 - (float)run * delf;
-          const float ds[3] = {ir[0] + ox - W.xr[j], ir[1] + oy - W.yr[j], ir[2] + oz - W.zr[j]};
-          const float h = f32_rz(A.h[j]);
-          if (!in_box<3, float>(ds, c2f * h)) continue;
-          const float ih = __fdividef(1.0f, h);
+          const float ds[3] = {ir[0] + ox - p.x, ir[1] + oy - p.y, ir[2] + oz - p.z};
+          if (!in_box<3, float>(ds, c2f * p.w)) continue;
+          const float ih = __fdividef(1.0f, p.w);
           const float sv[3] = {ds[0] * ih, ds[1] * ih, ds[2] * ih};
-          const float w = w_gauss<3, float>(sv, h);
-          const float mw = f32_rz(A.mass[j]) * w;
-          const float mwr = mw * __fdividef(1.0f, f32_rz(A.rho[j]));
+          if (fabsf(sv[0]) > 3.0f || fabsf(sv[1]) > 3.0f || fabsf(sv[2]) > 3.0f) continue;
+          const float4 q = K.Q[j], rv = K.R[j];
+          const float rn = float(T1_INV_SQRT_PI) * ih;
+          const float w = rn * rn * rn * __expf(-(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]));
+          const float mw = q.x * w;
+          const float mwr = q.y * w;
           a0.add(mw);
-          a1.add(mwr * f32_rz(A.vx[j]));
-          a2.add(mwr * f32_rz(A.vy[j]));
-          a3.add(mwr * f32_rz(A.vz[j]));
-          a4.add(mwr * f32_rz(A.e[j]));
-          if (!own) ak.add(mwr * f32_rz(A.Y[j]));
+          a1.add(mwr * rv.x);
+          a2.add(mwr * rv.y);
+          a3.add(mwr * rv.z);
+          a4.add(mwr * q.z);
+          if (!own) ak.add(mwr * q.w);
           aw.add(mwr);
         } else {
+          const uint8_t bc = A.bc[j];
+          if (!(bc == 100 || bc == 99 || bc == 1)) continue;
           const double h = A.h[j];
           const double ds[3] = {refc[0] - A.x[j], refc[1] - A.y[j], refc[2] - A.z[j]};
           if (!in_box<3, double>(ds, o.cutoff2 * h)) continue;
           const double sv[3] = {ds[0] / h, ds[1] / h, ds[2] / h};
+          // zero weight beyond |s_k| = 3 (w_gauss): adds nothing
+          if (fabs(sv[0]) > KCUTOFF || fabs(sv[1]) > KCUTOFF || fabs(sv[2]) > KCUTOFF) continue;
           const double w = w_gauss<3, double>(sv, h);
           const double mj = A.mass[j], rj = A.rho[j];
           a0.add(mj * w);
@@ -1572,14 +1595,17 @@ static void apply_bc(plume_ctx* ctx) {
   const int nslots = ctx->nmem * ctx->nimg;
   cudaMemsetAsync(ctx->bc_map, 0xff, sizeof(int) * (size_t)nslots, st);
   k_bc_map<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->d_count, ctx->img_key, ctx->nimg, ctx->bc_map);
-  if (ctx->opt.precision == PLUME_PREC_MIXED)
-    k_apply_bcond<float><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs,
-                                                               ctx->h27, ctx->bc_map, nslots, ctx->nimg,
+  if (ctx->opt.precision == PLUME_PREC_MIXED) {
+    k_pack_bc<<<nblocks(n ? n : 1), NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
+    k_apply_bcond<float><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->K,
+                                                               ctx->cs, ctx->h27, ctx->bc_map, nslots, ctx->nimg,
                                                                ctx->img_xyz, ctx->ts);
-  else
-    k_apply_bcond<double><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->cs,
-                                                                ctx->h27, ctx->bc_map, nslots, ctx->nimg,
+    ctx->launches++;
+  } else {
+    k_apply_bcond<double><<<nblocks((size_t)nslots * BCG), NTHREADS, 0, st>>>(ctx->d_opt, ctx->d_geo, ctx->A, ctx->W, ctx->K,
+                                                                ctx->cs, ctx->h27, ctx->bc_map, nslots, ctx->nimg,
                                                                 ctx->img_xyz, ctx->ts);
+  }
   ctx->launches += 5;
 }
 

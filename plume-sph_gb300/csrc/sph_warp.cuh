@@ -244,6 +244,44 @@ struct WMom {
   // j-side fields; pVVj = p_j V_j V_j, the reference's pressj * Vj * Vj
   __device__ __forceinline__ void load_j(uint32_t j, T& mj, T& rhoj, T& Vj, T& pVVj, T& cj, T& Tj, T& cpj,
                                          T* vj) const;
+  // A listed candidate of the mixed Gaussian path, in one piece: the four
+  // records of j are loaded together, then the pair arithmetic of math()
+  // runs without branches; a candidate outside the kernel support (or j ==
+  // i) contributes exactly zero through f = 0.  o[] is i's position shifted
+  // into j's bucket.  W = pi^-3/2 ih^3 e^-|s|^2, f = -2 ih W.
+  __device__ __forceinline__ void listed(uint32_t j, float ox, float oy, float oz) {
+    const float4 pj = K.P[j], qj = K.Q[j], rj = K.R[j], sj = K.S[j];
+    const float d0 = ox - pj.x, d1 = oy - pj.y, d2 = oz - pj.z;
+    const float h = 0.5f * (hi + pj.w);
+    const float ih = rcp<float>(h);
+    const float s0 = d0 * ih, s1 = d1 * ih, s2 = d2 * ih;
+    const float dist_sq = d0 * d0 + d1 * d1 + d2 * d2;
+    const float v0 = veli[0] - rj.w, v1 = veli[1] - sj.x, v2 = veli[2] - sj.y;
+    const float sndspdab = 0.5f * (ci + rj.x);
+    const float vrab = d0 * v0 + d1 * v1 + d2 * v2;
+    const float miuab = h * vrab * rcp<float>(dist_sq + ata * h * h);
+    float vis = (vrab < 0.0f) ? (beta * miuab - alpha * sndspdab) * miuab * rcp<float>(0.5f * (rhoi + qj.y)) : 0.0f;
+    const float dotv = v0 * v0 + v1 * v1 + v2 * v2;
+    if (lans) vis -= float(EPS_HALF) * dotv * qj.z;
+    const float mpvsqij = qj.x * (qj.w + pvsqi + vis);
+    const bool in = (j != i) && fabsf(s0) <= 3.0f && fabsf(s1) <= 3.0f && fabsf(s2) <= 3.0f;
+    const float ih2 = ih * ih;
+    const float f = in ? KF * (ih2 * ih2) * __expf(-(s0 * s0 + s1 * s1 + s2 * s2)) : 0.0f;
+    const float gm = mpvsqij * f;
+    rv[0].sub(gm * s0);
+    rv[1].sub(gm * s1);
+    rv[2].sub(gm * s2);
+    float heat_tran = 0.0f;
+    if (lans) {
+      const float Cp_ij = 0.5f * (rj.z + Cp_i);
+      const float dotvr = fabsf(v0 * d0) + fabsf(v1 * d1) + fabsf(v2 * d2);
+      const float kij = 10.0f * float(EPS_HALF) * Cp_ij * dist_sq * dotv *
+                        rcp<float>(float(PRANDTL) * dotvr * h * sndspdab);
+      heat_tran = (dotvr != 0.0f) ? qj.x * qj.z * Vi * kij * (tempi - rj.y) * (f * ih) : 0.0f;
+    }
+    re.add(0.5f * gm * ih * vrab + heat_tran);
+  }
+  static constexpr float KF = float(-2.0 * T1_INV_SQRT_PI * T1_INV_SQRT_PI * T1_INV_SQRT_PI);
   __device__ __forceinline__ void math(uint32_t j, const T* dx, T hj) {
     T mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj[3];
     load_j(j, mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj);
@@ -446,7 +484,38 @@ struct WDens {
     const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
+  // the mixed Gaussian pair of math() with j's density record q = (m, m/rho,
+  // m e/rho, phase) already loaded: W(s, h) = r^3 exp(-s.s), r = 1/(sqrt(pi)
+  // h); the energy-smoothing kernel at h/4 is 64 r^3 exp(-16 s.s), zero once
+  // any |s_k| > 3/4
+  __device__ __forceinline__ void math_q(const float4 q, float d0, float d1, float d2, float hj) {
+    const float hh = 0.5f * (float(hi) + hj);
+    const float ih = rcp<float>(hh);
+    const float s0 = d0 * ih, s1 = d1 * ih, s2 = d2 * ih;
+    const float ax = fabsf(s0), ay = fabsf(s1), az = fabsf(s2);
+    const float qq = s0 * s0 + s1 * s1 + s2 * s2;
+    const float r = float(T1_INV_SQRT_PI) * ih;
+    const float r3 = r * r * r;
+    const float amax = fmaxf(ax, fmaxf(ay, az));
+    if (esm && amax <= 0.75f) {
+      const float w_e = 64.0f * r3 * __expf(-16.0f * qq);
+      wnorm_e.add(w_e * q.y);
+      engr.add(w_e * q.z);
+    }
+    if (amax > 3.0f) return;
+    const float wm = r3 * __expf(-qq) * q.x;
+    if (q.w == 1.0f)
+      rho1.add(wm);
+    else
+      rho2.add(wm);
+  }
   __device__ __forceinline__ void math(uint32_t j, const T* ds, T hj) {
+    if constexpr (sizeof(T) == 4) {
+      if (o.kernel != 1) {
+        math_q(K.Q[j], ds[0], ds[1], ds[2], fabsf(hj));
+        return;
+      }
+    }
     // FP64: the reference's fields; mixed: (m, m/rho, m e/rho, phase)
     T mj, rhoj = 0, ej = 0, mvr = 0, mer = 0, ph;
     if constexpr (sizeof(T) == 8) {
@@ -461,29 +530,6 @@ struct WDens {
     const T ih = rcp<T>(hh);
 #pragma unroll
     for (int k = 0; k < 3; k++) sv[k] = (sizeof(T) == 8) ? ds[k] / hh : ds[k] * ih;
-    if constexpr (sizeof(T) == 4) {
-      if (o.kernel != 1) {
-        // Gaussian, mixed: W(s, h) = r^3 exp(-s.s), r = 1/(sqrt(pi) h); the
-        // energy-smoothing kernel at h/4 is 64 r^3 exp(-16 s.s), zero once
-        // any |s_k| > 3/4
-        const float ax = fabsf(sv[0]), ay = fabsf(sv[1]), az = fabsf(sv[2]);
-        const float q = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2];
-        const float r = float(T1_INV_SQRT_PI) * ih;
-        const float r3 = r * r * r;
-        if (esm && fmaxf(ax, fmaxf(ay, az)) <= 0.75f) {
-          const float w_e = 64.0f * r3 * __expf(-16.0f * q);
-          wnorm_e.add(w_e * mvr);
-          engr.add(w_e * mer);
-        }
-        if (fmaxf(ax, fmaxf(ay, az)) > 3.0f) return;
-        const float wm = r3 * __expf(-q) * mj;
-        if (ph == 1.0f)
-          rho1.add(wm);
-        else
-          rho2.add(wm);
-        return;
-      }
-    }
     if (esm) {
       T s_e[3];
 #pragma unroll
@@ -505,6 +551,15 @@ struct WDens {
       rho2.add(wm);
   }
 };
+
+template <typename T>
+__device__ __forceinline__ void dens_listed(WDens<T>& s, uint32_t j, float ox, float oy, float oz) {
+  // a listed candidate of the mixed Gaussian path: both records loaded
+  // together, then math() (which drops pairs outside the support)
+  const float4 pj = s.K.P[j], qj = s.K.Q[j];
+  if (pj.w < 0.0f) return;  // not contributing
+  s.math_q(qj, ox - pj.x, oy - pj.y, oz - pj.z, pj.w);
+}
 
 // density record: P (xr,yr,zr,+-h: - when not contributing),
 // Q (m, m/rho, m e/rho, phase)
@@ -583,6 +638,19 @@ struct WVel {
       if (!in_box<3, T>(dx, supp)) return false;
     }
     return in_box<3, T>(dx, ks);
+  }
+  // a listed candidate of the mixed Gaussian path: both records loaded
+  // together; outside the support (|s_k| > 3) the weight is zero
+  __device__ __forceinline__ void listed(uint32_t j, float ox, float oy, float oz) {
+    const float4 pj = K.P[j], qj = K.Q[j];
+    if (pj.w < 0.0f) return;  // not contributing
+    const float s0 = (ox - pj.x) * ihi, s1 = (oy - pj.y) * ihi, s2 = (oz - pj.z) * ihi;
+    const bool in = fabsf(s0) <= 3.0f && fabsf(s1) <= 3.0f && fabsf(s2) <= 3.0f;
+    const float mvw = in ? r3 * __expf(-(s0 * s0 + s1 * s1 + s2 * s2)) * qj.x : 0.0f;
+    dv[0].add(mvw * (qj.y - vi[0]));
+    dv[1].add(mvw * (qj.z - vi[1]));
+    dv[2].add(mvw * (qj.w - vi[2]));
+    wnorm.add(mvw);
   }
   __device__ __forceinline__ void math(uint32_t j, const T* ds, T) {
     // FP64: the reference's fields; mixed: (m/rho, vx, vy, vz)
@@ -813,6 +881,17 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
   L.cnt[i] = (cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
 }
 
+// the fused listed pair of each sweep (mixed Gaussian path)
+__device__ __forceinline__ void listed_pair(WMom<float>& s, uint32_t j, float ox, float oy, float oz) {
+  s.listed(j, ox, oy, oz);
+}
+__device__ __forceinline__ void listed_pair(WDens<float>& s, uint32_t j, float ox, float oy, float oz) {
+  dens_listed(s, j, ox, oy, oz);
+}
+__device__ __forceinline__ void listed_pair(WVel<float>& s, uint32_t j, float ox, float oy, float oz) {
+  s.listed(j, ox, oy, oz);
+}
+
 // sweep over the lists (thread per particle, over the compacted need_neigh
 // indices); particles whose list overflowed walk their rows.  The window and
 // Visits the candidates of particle i in the walk's order: the particle's
@@ -840,6 +919,10 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     // listed entries get i's position shifted into the window's bucket
     decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
     ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
+    // mixed Gaussian path: each listed candidate in one branch-free piece
+    // (its records loaded together, zero outside the support)
+    bool fused = false;
+    if constexpr (sizeof(T) == 4) fused = s.o.kernel != 1;
     while (true) {
       if (mask == 0) {  // stored windows are never empty: one step suffices
         if (++q >= c) break;
@@ -850,6 +933,12 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
       }
       const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
       mask &= mask - 1;
+      if constexpr (sizeof(T) == 4) {
+        if (fused) {
+          listed_pair(s, j, ox, oy, oz);
+          continue;
+        }
+      }
       T dx[3], hj;
       if (s.template filter<true>(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
     }
