@@ -82,6 +82,38 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
   }
 }
 
+// The candidates of a particle's stored neighbour list (search_neighs_consth,
+// neighs.cc:84-131: its own bucket, and the particles of the 26 others
+// inside the list box), walked as two regions: A, the rows within RA (the
+// list box, or less when the caller's reach is shorter) clipped to the 27
+// buckets, then B, the fine cells of the own bucket outside A's cells.  Every
+// candidate of the list inside RA comes once; f gets own = true for B.
+template <typename T, class F>
+__device__ __forceinline__ void walk_list_region(const Geo& g, const uint32_t* __restrict__ cs, const double* xi,
+                                                 const int* bi, double RA, F&& f) {
+  for_segments<3, T>(g, cs, xi, bi, RA, f);
+  int lo[3], hi[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const int l = cell_axis(g, a, xi[a] - RA, nullptr, nullptr);
+    const int h = cell_axis(g, a, xi[a] + RA, nullptr, nullptr);
+    lo[a] = max(l, max((bi[a] - 1) * g.s, 0));
+    hi[a] = min(h, min((bi[a] + 2) * g.s - 1, g.G[a] - 1));
+  }
+  const int b0 = bi[0] * g.s, b1 = b0 + g.s - 1;
+  for (int cz = bi[2] * g.s; cz < (bi[2] + 1) * g.s; cz++)
+    for (int cy = bi[1] * g.s; cy < (bi[1] + 1) * g.s; cy++) {
+      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      if (cz >= lo[2] && cz <= hi[2] && cy >= lo[1] && cy <= hi[1]) {
+        // the parts of the own bucket's x-run outside A's cells
+        if (lo[0] > b0) f(cs[rowbase + b0], cs[rowbase + min(lo[0] - 1, b1) + 1], true, T(0), T(0), T(0));
+        if (hi[0] < b1) f(cs[rowbase + max(hi[0] + 1, b0)], cs[rowbase + b1 + 1], true, T(0), T(0), T(0));
+      } else {
+        f(cs[rowbase + b0], cs[rowbase + b1 + 1], true, T(0), T(0), T(0));
+      }
+    }
+}
+
 template <int D>
 __device__ __forceinline__ void bucket_coords(const Geo& g, int b, int* bi) {
   if (D == 1) {
@@ -174,7 +206,7 @@ __global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
     T supp = T(o.cutoff2) * H_star;
     Acc<T> rho_star;
     double R = fmin(o.cutoff2, o.ksupport) * H_star_d * (1.0 + 1e-10);
-    for_segments<D, T>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
+    auto visit = [&](uint32_t j0, uint32_t j1, bool own, T ox, T oy, T oz) {
       T xsh[3] = {xs[0] + ox, D == 3 ? xs[1] + oy : T(0), D == 3 ? xs[2] + oz : T(0)};
       for (uint32_t j = j0; j < j1; j++) {
         if (!contr_dens(A.bc[j], o.pgc)) continue;
@@ -188,7 +220,13 @@ __global__ void k_adaptive(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
         T wght = kw<D, T>(o.kernel, si, H_star);
         rho_star.add(wght * mj);
       }
-    });
+    };
+    // 3D: the list's own bucket plus its list box (the reach beyond the
+    // list box holds no listed candidate)
+    if constexpr (D == 3)
+      walk_list_region<T>(g, cs, xi, bi, fmin(R, o.list_factor * W.hlist[i] * (1.0 + 1e-6)), visit);
+    else
+      for_segments<D, T>(g, cs, xi, bi, R, visit);
     double rs = (double)rho_star.get();
     double H_new = (D == 3) ? o.eta * cbrt(mi / rs) : o.eta * (mi / rs);
     hcur = 1.0 * H_new;

@@ -753,6 +753,23 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geos<MULTI> geo, Dev A, W
 // own exact tests, so the sums are those of the walk; the divergent
 // candidate filtering is paid once per step instead of once per sweep.
 constexpr int LCAP = 160;                 // windows per particle
+#ifndef PLUME_LIST_STREAM
+#define PLUME_LIST_STREAM 1  // list entries stored and loaded evict-first
+#endif
+__device__ __forceinline__ uint2 list_load(const uint2* p) {
+#if PLUME_LIST_STREAM
+  return __ldcs(p);
+#else
+  return *p;
+#endif
+}
+__device__ __forceinline__ void list_store(uint2* p, uint2 v) {
+#if PLUME_LIST_STREAM
+  __stcs(p, v);
+#else
+  *p = v;
+#endif
+}
 constexpr uint16_t NL_OVERFLOW = 0xFFFF;  // particle walks instead
 constexpr uint32_t NL_JMASK = (1u << 26) - 1u;
 
@@ -873,7 +890,9 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
         }
       }
       if (mask) {
-        if (cnt < LCAP) out[cnt] = make_uint2(wb | ((uint32_t)code << 26), mask);
+        // streaming store: the lists are read once per sweep and should not
+        // push the sweeps' particle records out of L2
+        if (cnt < LCAP) list_store(out + cnt, make_uint2(wb | ((uint32_t)code << 26), mask));
         cnt++;
       }
     }
@@ -912,7 +931,8 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     const uint2* ent = L.e + (size_t)i * LCAP;
     const T delT = T(g.del);
     int q = 0;
-    uint2 en = ent[0];
+    // list entries are streamed (evict-first): the particle records stay cached
+    uint2 en = list_load(ent);
     uint32_t mask = en.y;
     bool own;
     T ox, oy, oz;
@@ -926,7 +946,7 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     while (true) {
       if (mask == 0) {  // stored windows are never empty: one step suffices
         if (++q >= c) break;
-        en = ent[q];
+        en = list_load(ent + q);
         mask = en.y;
         decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
         ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
@@ -1224,7 +1244,7 @@ __global__ void __launch_bounds__(128) k_adaptive_mixed(Opt o, Geos<MULTI> geo, 
     const float r3 = rn * rn * rn;
     Acc<float> rho_star;
     const double R = fmin(o.cutoff2, o.ksupport) * H_star_d * (1.0 + 1e-10);
-    for_segments<3, float>(g, cs, xi, bi, R, [&](uint32_t j0, uint32_t j1, bool own, float ox, float oy, float oz) {
+    auto visit = [&](uint32_t j0, uint32_t j1, bool own, float ox, float oy, float oz) {
       const float xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
       for (uint32_t j = j0; j < j1; j++) {
         const float4 p = K.P[j];
@@ -1242,7 +1262,8 @@ __global__ void __launch_bounds__(128) k_adaptive_mixed(Opt o, Geos<MULTI> geo, 
           w = kw<3, float>(o.kernel, si, H_star);
         rho_star.add(w * p.w);
       }
-    });
+    };
+    walk_list_region<float>(g, cs, xi, bi, fmin(R, o.list_factor * W.hlist[i] * (1.0 + 1e-6)), visit);
     const double rs = (double)rho_star.get();
     const double H_new = o.eta * cbrt(mi / rs);
     hcur = 1.0 * H_new;
