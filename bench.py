@@ -265,7 +265,10 @@ def ensemble_1d(steps=400, warm=50, graph=50, members=256):
         e.adaptive_sml()
         e.run(warm, graph_steps=graph)
         st0 = e.member_times()[1]
+        import torch
+        torch.cuda.nvtx.range_push(f"riemann1d_{prec}")  # lets a profiler select these launches
         n = e.run(steps, graph_steps=graph)
+        torch.cuda.nvtx.range_pop()
         t = e.phase_times()["total"] / 1000.0
         _, st1, run1, status = e.member_times()
         ps = float((nreal * (st1 - st0)).sum())
@@ -553,7 +556,9 @@ def main():
     torch.cuda.synchronize()
     _, n_real_before = sol.count()
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed")  # lets a profiler select the timed launches
         log = sol.steps(args.steps, log=False)
+        torch.cuda.nvtx.range_pop()
         phases = sol.phase_times()
     torch.cuda.synchronize()
     launches = sol.launches()
