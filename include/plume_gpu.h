@@ -129,6 +129,16 @@ extern "C" {
 #define PLUME_RIEMANN_ROE   0 /* Roe_RP_Solver, sph_lib.cc:1694-1750 (3D default) */
 #define PLUME_RIEMANN_HLLC  1 /* HLLC_RP_Solver, sph_lib.cc:1753-1908,
                                  HLL_WAVE_SPEED_EVA 0 (1D default)            */
+#define PLUME_RIEMANN_HLLC_MY 2 /* HLLC_RP_Solver_my, sph_lib.cc:1912-2088:
+                                 HLLC for strong shocks, wave speeds by
+                                 PlumeOptions.gsph_wave_speed                 */
+#define PLUME_RIEMANN_VANLEER 3 /* VanLeer_RP_Solver, sph_lib.cc:2094-2210:
+                                 Van Leer's iterative solver on the
+                                 Lagrangian sound speeds (at most
+                                 PLUME_VANLEER_MAX_ITER iterations here; a
+                                 problem that has not converged by then gives
+                                 NaN, which the step reports)                 */
+#define PLUME_VANLEER_MAX_ITER 100
 
 /* ---- GSPH Riemann-problem states (MINI_DERIVATIVE_COND, options.h:156-170,
  *      559-573): zeroth order (the particles' own states) or linear in the
@@ -182,6 +192,11 @@ typedef struct PlumeOptions {
     int    gsph_gradients;      /* 1: calc_gradients every GSPH step, as the
                                    reference does; 0: only when the
                                    reconstruction reads them                  */
+    int    gsph_wave_speed;     /* HLL_WAVE_SPEED_EVA of PLUME_RIEMANN_HLLC_MY
+                                   (options.h:194-206): 2 Davis, 3 Toro --
+                                   the settings the reference runs with (0
+                                   stops it, 1, 4 and 5 do not compile);
+                                   unused by the other solvers                */
 } PlumeOptions;
 
 /* Bucket grid (the background mesh of src/datstr/bucket.h).  Bucket (i,j,k)

@@ -666,6 +666,105 @@ static void roe(double dl, double dr, double pl, double pr, double ul, double ur
     *u_star = ulr - 0.5 * (pr - pl) / clr;
 }
 
+/* HLLC_RP_Solver_my (sph_lib.cc:1912-2088): HLLC for strong shocks on the
+ * velocities relative to the Roe velocity; wave speeds by HLL_WAVE_SPEED_EVA
+ * (2 Davis, 3 Toro); the star region takes p_HLLC and u = sqrt(2 (E*_l -
+ * e*_l)), the outer regions the side's state. */
+static void hllc_my(int wave, double dl, double dr, double pl, double pr, double ul, double ur,
+                    double gl, double gr, double *p_star, double *u_star)
+{
+    double rdl = sqrt(dl), rdr = sqrt(dr);
+    double den = 1.0 / (rdl + rdr);
+    double cl = sqrt(gl * pl / dl), cr = sqrt(gr * pr / dr);
+    double ulr = (ul * rdl + ur * rdr) * den;
+    ul = ul - ulr;
+    ur = ur - ulr;
+    double Sl, Sr;
+    if (wave == 2) {
+        Sl = fmin(ul - cl, ur - cr);
+        Sr = fmax(ul + cl, ur + cr);
+    } else {
+        double plr = (pl * rdl + pr * rdr) * den;
+        double glr = (gl * rdl + gr * rdr) * den;
+        double dlr = (dl * rdl + dr * rdr) * den;
+        double clr = sqrt(glr * plr / dlr);
+        double p_refs = fmax(0.0, 0.5 * (pl + pr) + 0.25 * (ul - ur) * (dr + dl) * clr);
+        double ql = p_refs < pl ? 1.0 : sqrt(1.0 + 0.5 * (gl + 1.0) / gl * (p_refs / pl - 1.0));
+        double qr = p_refs < pr ? 1.0 : sqrt(1.0 + 0.5 * (gr + 1.0) / gr * (p_refs / pr - 1.0));
+        Sl = ul - cl * ql;
+        Sr = ur + cr * qr;
+    }
+    double alf_l = dl * (Sl - ul), alf_r = dr * (Sr - ur);
+    double Sm = (ur * alf_r - ul * alf_l + pl - pr) / (alf_r - alf_l);
+    double p_hllc = (pr * alf_r - pl * alf_l - alf_r * alf_l * (ul - ur)) / (alf_r - alf_l);
+    double dl_star = alf_l / (Sl - Sm);
+    double el_star = p_hllc / (dl_star * (gl - 1.0));
+    double el = pl / (dl * (gl - 1.0));
+    double El_star = el + (Sm - ul) * (Sm + pl / alf_l);
+    double u_hllc = sqrt(2.0 * (El_star - el_star));
+    if (Sl > 0) {
+        *p_star = pl;
+        *u_star = ul;
+    } else if (Sl <= 0 && Sr > 0) {
+        *p_star = p_hllc;
+        *u_star = u_hllc;
+    } else if (Sr <= 0) {
+        *p_star = pr;
+        *u_star = ur;
+    } else {
+        /* a NaN wave speed: the reference leaves p*, u* unset */
+        *p_star = NAN;
+        *u_star = NAN;
+    }
+}
+
+/* VanLeer_RP_Solver (sph_lib.cc:2094-2210): Van Leer's iterative solver on
+ * the Lagrangian sound speeds C = rho c of the particles' own sound speeds:
+ * the acoustic estimate of p*, accepted within 1 % of both pressures, else
+ * iterated with the shock / rarefaction impedances W and slopes Z until p*
+ * moves by less than 1 % (at most PLUME_VANLEER_MAX_ITER iterations, then
+ * NaN; the reference iterates without a limit). */
+static void vanleer(double dl, double dr, double pl, double pr, double ul, double ur, double gl,
+                    double gr, double csl, double csr, double *p_star, double *u_star)
+{
+    double Cl = csl * dl, Cr = csr * dr;
+    double p = (Cl * pr + Cr * pl - Cr * Cl * (ul - ur)) / (Cl + Cr);
+    double md = fabs(p - pl) / pl, md2 = fabs(p - pr) / pr;
+    if (md2 > md) md = md2;
+    if (md < 0.01) {
+        *u_star = 0.5 * (ul + ur);
+        *p_star = p;
+        return;
+    }
+    double G1l = 0.5 * (gl + 1) / gl, G2l = 0.5 * (gl - 1) / gl, G3l = 1.0 - G2l;
+    double G1r = 0.5 * (gr + 1) / gr, G2r = 0.5 * (gr - 1) / gr, G3r = 1.0 - G2r;
+    double Cl2 = Cl * Cl, Cr2 = Cr * Cr;
+    double Zl = 0, Zr = 0, vl = 0, vr = 0, err = 1.0;
+    int it = 0;
+    while (err > 0.01) {
+        if (++it > PLUME_VANLEER_MAX_ITER) {
+            *p_star = NAN;
+            *u_star = NAN;
+            return;
+        }
+        double Rl = p / pl, Rr = p / pr;
+        double Wl = (p >= pl) ? Cl * pow(1.0 + G1l * (p - pl) / pl, 0.5)
+                              : G2l * (1.0 - Rl) / (1.0 - pow(Rl, G2l)) * Cl;
+        double Wr = (p >= pr) ? Cr * pow(1.0 + G1r * (p - pr) / pr, 0.5)
+                              : G2r * (1.0 - Rr) / (1.0 - pow(Rr, G2r)) * Cr;
+        double Wl2 = Wl * Wl, Wr2 = Wr * Wr;
+        Zl = (p >= pl) ? 2.0 * Wl2 / (Wl2 + Cl2) * Wl : Cl * pow(Rl, G3l);
+        Zr = (p >= pr) ? 2.0 * Wr2 / (Wr2 + Cr2) * Wr : Cr * pow(Rr, G3r);
+        vl = ul + (p - pl) / Wl;
+        vr = ur - (p - pr) / Wr;
+        double pn = p - (Zl * Zr * (vl - vr)) / (Zl + Zr);
+        err = fabs(pn - p) / p;
+        p = pn;
+    }
+    *u_star = (Zl * vl + Zr * vr) / (Zl + Zr);
+    *p_star = p;
+}
+
 /* One pair's Riemann problem (Riemann_Solver, sph_lib.cc:2247-2598, USE_GSPH
  * 1, RP_MASS_WEIGHTED 0, SWITCH_OFF_AV_FOR_EXPAN 0, SHEAR_VEL_APP 2): the
  * states projected on e = (x_i - x_j)/|x_i - x_j|; unless the
@@ -769,6 +868,10 @@ static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const d
     double u_star;
     if (o->gsph_solver == PLUME_RIEMANN_HLLC)
         hllc(dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
+    else if (o->gsph_solver == PLUME_RIEMANN_HLLC_MY)
+        hllc_my(o->gsph_wave_speed, dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
+    else if (o->gsph_solver == PLUME_RIEMANN_VANLEER)
+        vanleer(dl, dr, pl, pr, ul, ur, J->gam, I->gam, J->c, I->c, p_star, &u_star);
     else
         roe(dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
     double rdl = sqrt(dl), rdr = sqrt(dr);

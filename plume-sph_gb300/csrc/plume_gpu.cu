@@ -1292,6 +1292,7 @@ static Opt make_opt(const PlumeOptions& p) {
   o.gsph_recon = p.gsph_recon;
   o.gsph_vol = p.gsph_vol;
   o.gsph_mono = p.gsph_mono;
+  o.gsph_wave = p.gsph_wave_speed;
   return o;
 }
 
@@ -1725,7 +1726,8 @@ static bool same_shared_options(const PlumeOptions& a, const PlumeOptions& b) {
          a.alpha == b.alpha && a.beta == b.beta && a.ata == b.ata && a.cutoff2 == b.cutoff2 &&
          a.list_factor == b.list_factor && a.g == b.g && a.method == b.method &&
          a.gsph_solver == b.gsph_solver && a.gsph_recon == b.gsph_recon && a.gsph_vol == b.gsph_vol &&
-         a.gsph_mono == b.gsph_mono && a.gsph_gradients == b.gsph_gradients;
+         a.gsph_mono == b.gsph_mono && a.gsph_gradients == b.gsph_gradients &&
+         a.gsph_wave_speed == b.gsph_wave_speed;
 }
 
 static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem, bool batch, plume_ctx** out) {
@@ -1748,11 +1750,15 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
   }
   if (opt->method == PLUME_METHOD_GSPH) {
     const int r = opt->gsph_recon;
-    if ((opt->gsph_solver != PLUME_RIEMANN_ROE && opt->gsph_solver != PLUME_RIEMANN_HLLC) ||
+    const int sv = opt->gsph_solver;
+    if (!(sv == PLUME_RIEMANN_ROE || sv == PLUME_RIEMANN_HLLC || sv == PLUME_RIEMANN_HLLC_MY ||
+          sv == PLUME_RIEMANN_VANLEER) ||
         !(r == 0 || r == 1 || r == 2 || r == 3 || r == 4 || r == 10) ||
         !(opt->gsph_vol == 0 || opt->gsph_vol == 1 || opt->gsph_vol == 3) ||
-        (opt->gsph_mono != 0 && opt->gsph_mono != 1)) {
-      g_create_error = "GSPH: solver ROE/HLLC, recon 0-4 or 10, vol 0, 1 or 3, mono 0 or 1";
+        (opt->gsph_mono != 0 && opt->gsph_mono != 1) ||
+        (sv == PLUME_RIEMANN_HLLC_MY && opt->gsph_wave_speed != 2 && opt->gsph_wave_speed != 3)) {
+      g_create_error = "GSPH: solver ROE/HLLC/HLLC_MY/VANLEER (HLLC_MY with wave speed 2 or 3), recon 0-4 or 10, "
+                       "vol 0, 1 or 3, mono 0 or 1";
       return PLUME_E_INVALID;
     }
   }

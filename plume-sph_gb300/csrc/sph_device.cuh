@@ -41,6 +41,7 @@ struct Opt {
   // GSPH (USE_GSPH 1): RIEMANN_SOLVER, MINI_DERIVATIVE_COND,
   // GSPH_SPECIFIC_VOL_APP, GSPH_MODIFIED_MONOTONICITY
   int method, gsph_solver, gsph_recon, gsph_vol, gsph_mono;
+  int gsph_wave;  // HLL_WAVE_SPEED_EVA of the HLLC_RP_Solver_my solver
 };
 
 struct Geo {

@@ -10,6 +10,7 @@
 // FP32 Riemann problems, compensated FP32 sums, FP64 update).
 #pragma once
 
+#include "../../include/plume_gpu.h"
 #include "sph_kernels.cuh"
 
 namespace plume {
@@ -206,6 +207,107 @@ __device__ __forceinline__ void rp_hllc(T dl, T dr, T pl, T pr, T ul, T ur, T gl
   }
 }
 
+// HLLC_RP_Solver_my (sph_lib.cc:1912-2088): HLLC for strong shocks on
+// velocities relative to the Roe velocity, with the wave-speed estimate of
+// HLL_WAVE_SPEED_EVA (wave: 2 Davis, 3 Toro, the two the reference runs
+// with); p* = p_HLLC and u* = sqrt(2 (E*_l - e*_l)) in the star region, the
+// side's own state outside it.
+template <typename T>
+__device__ __forceinline__ void rp_hllc_my(int wave, T dl, T dr, T pl, T pr, T ul, T ur, T gl, T gr, T& p_star,
+                                           T& u_star) {
+  const T rdl = sqrt(dl), rdr = sqrt(dr);
+  const T den = T(1) / (rdl + rdr);
+  const T cl = sqrt(gl * pl / dl), cr = sqrt(gr * pr / dr);
+  const T ulr = (ul * rdl + ur * rdr) * den;
+  ul = ul - ulr;
+  ur = ur - ulr;
+  T Sl, Sr;
+  if (wave == 2) {
+    Sl = fmin(ul - cl, ur - cr);
+    Sr = fmax(ul + cl, ur + cr);
+  } else {
+    const T plr = (pl * rdl + pr * rdr) * den;
+    const T glr = (gl * rdl + gr * rdr) * den;
+    const T dlr = (dl * rdl + dr * rdr) * den;
+    const T clr = sqrt(glr * plr / dlr);
+    const T p_refs = fmax(T(0), T(0.5) * (pl + pr) + T(0.25) * (ul - ur) * (dr + dl) * clr);
+    const T ql = p_refs < pl ? T(1) : sqrt(T(1) + T(0.5) * (gl + T(1)) / gl * (p_refs / pl - T(1)));
+    const T qr = p_refs < pr ? T(1) : sqrt(T(1) + T(0.5) * (gr + T(1)) / gr * (p_refs / pr - T(1)));
+    Sl = ul - cl * ql;
+    Sr = ur + cr * qr;
+  }
+  const T alf_l = dl * (Sl - ul), alf_r = dr * (Sr - ur);
+  const T Sm = (ur * alf_r - ul * alf_l + pl - pr) / (alf_r - alf_l);
+  const T p_hllc = (pr * alf_r - pl * alf_l - alf_r * alf_l * (ul - ur)) / (alf_r - alf_l);
+  const T dl_star = alf_l / (Sl - Sm);
+  const T el_star = p_hllc / (dl_star * (gl - T(1)));
+  const T el = pl / (dl * (gl - T(1)));
+  const T El_star = el + (Sm - ul) * (Sm + pl / alf_l);
+  const T u_hllc = sqrt(T(2) * (El_star - el_star));
+  if (Sl > T(0)) {
+    p_star = pl;
+    u_star = ul;
+  } else if (Sl <= T(0) && Sr > T(0)) {
+    p_star = p_hllc;
+    u_star = u_hllc;
+  } else if (Sr <= T(0)) {
+    p_star = pr;
+    u_star = ur;
+  } else {  // NaN wave speeds: the NaN reaches the state and its check
+    p_star = T(NAN);
+    u_star = T(NAN);
+  }
+}
+
+// VanLeer_RP_Solver (sph_lib.cc:2094-2210): Van Leer's iterative solver on
+// the Lagrangian sound speeds C = rho c (c the particles' own sound speeds):
+// the acoustic estimate of p*, accepted when within 1 % of both pressures,
+// else secant-like updates with the shock / rarefaction impedances W and
+// slopes Z until p* moves by less than 1 %.  The reference iterates without
+// a limit; here a problem that has not converged after
+// PLUME_VANLEER_MAX_ITER iterations gives NaN, which the step reports.
+template <typename T>
+__device__ __forceinline__ void rp_vanleer(T dl, T dr, T pl, T pr, T ul, T ur, T gl, T gr, T csl, T csr,
+                                           T& p_star, T& u_star) {
+  const T Cl = csl * dl, Cr = csr * dr;
+  T p = (Cl * pr + Cr * pl - Cr * Cl * (ul - ur)) / (Cl + Cr);
+  T md = fabs(p - pl) / pl;
+  const T md2 = fabs(p - pr) / pr;
+  if (md2 > md) md = md2;
+  if (md < T(0.01)) {
+    u_star = T(0.5) * (ul + ur);
+    p_star = p;
+    return;
+  }
+  const T G1l = T(0.5) * (gl + T(1)) / gl, G2l = T(0.5) * (gl - T(1)) / gl, G3l = T(1) - G2l;
+  const T G1r = T(0.5) * (gr + T(1)) / gr, G2r = T(0.5) * (gr - T(1)) / gr, G3r = T(1) - G2r;
+  const T Cl2 = Cl * Cl, Cr2 = Cr * Cr;
+  T Zl = 0, Zr = 0, vl = 0, vr = 0, err = T(1);
+  int it = 0;
+  while (err > T(0.01)) {
+    if (++it > PLUME_VANLEER_MAX_ITER) {
+      p_star = T(NAN);
+      u_star = T(NAN);
+      return;
+    }
+    const T Rl = p / pl, Rr = p / pr;
+    const T Wl = (p >= pl) ? Cl * pow(T(1) + G1l * (p - pl) / pl, T(0.5))
+                           : G2l * (T(1) - Rl) / (T(1) - pow(Rl, G2l)) * Cl;
+    const T Wr = (p >= pr) ? Cr * pow(T(1) + G1r * (p - pr) / pr, T(0.5))
+                           : G2r * (T(1) - Rr) / (T(1) - pow(Rr, G2r)) * Cr;
+    const T Wl2 = Wl * Wl, Wr2 = Wr * Wr;
+    Zl = (p >= pl) ? T(2) * Wl2 / (Wl2 + Cl2) * Wl : Cl * pow(Rl, G3l);
+    Zr = (p >= pr) ? T(2) * Wr2 / (Wr2 + Cr2) * Wr : Cr * pow(Rr, G3r);
+    vl = ul + (p - pl) / Wl;
+    vr = ur - (p - pr) / Wr;
+    const T pn = p - (Zl * Zr * (vl - vr)) / (Zl + Zr);
+    err = fabs(pn - p) / p;
+    p = pn;
+  }
+  u_star = (Zl * vl + Zr * vr) / (Zl + Zr);
+  p_star = p;
+}
+
 // Riemann_Solver (sph_lib.cc:2247-2598, USE_GSPH 1, RP_MASS_WEIGHTED 0,
 // SWITCH_OFF_AV_FOR_EXPAN 0, SHEAR_VEL_APP 2) for the pair (i = right side,
 // j = left side) at distance vector dx = x_i - x_j: states projected on
@@ -309,6 +411,10 @@ __device__ __forceinline__ void gsph_riemann(const Opt& o, const T* dx, const GS
   T u_star;
   if (o.gsph_solver == 1)
     rp_hllc<T>(dl, dr, pl, pr, ul, ur, J.gam, I.gam, p_star, u_star);
+  else if (o.gsph_solver == 2)
+    rp_hllc_my<T>(o.gsph_wave, dl, dr, pl, pr, ul, ur, J.gam, I.gam, p_star, u_star);
+  else if (o.gsph_solver == 3)
+    rp_vanleer<T>(dl, dr, pl, pr, ul, ur, J.gam, I.gam, J.c, I.c, p_star, u_star);
   else
     rp_roe<T>(dl, dr, pl, pr, ul, ur, J.gam, I.gam, p_star, u_star);
   const T rdl = sqrt(dl), rdr = sqrt(dr);

@@ -38,7 +38,7 @@ BINV_NONE, BINV_POTENTIAL, BINV_INVOLVED, BINV_BOTH = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 KERNEL_GAUSS, KERNEL_M4 = 0, 1
 METHOD_SPH, METHOD_GSPH = 0, 1
-RIEMANN_ROE, RIEMANN_HLLC = 0, 1
+RIEMANN_ROE, RIEMANN_HLLC, RIEMANN_HLLC_MY, RIEMANN_VANLEER = 0, 1, 2, 3
 RECON_NONE, RECON_EACH, RECON_PAIRWISE, RECON_ALL, RECON_ZEROTH, RECON_EACH_SHOCK = 0, 1, 2, 3, 4, 10
 
 # field order of the double arrays (also the order of the oracle case files)
@@ -64,7 +64,7 @@ class PlumeOptions(C.Structure):
         ("max_steps", C.c_int), ("max_per_bucket", C.c_int),
         ("capacity", C.c_size_t),
         ("method", C.c_int), ("gsph_solver", C.c_int), ("gsph_recon", C.c_int), ("gsph_vol", C.c_int),
-        ("gsph_mono", C.c_int), ("gsph_gradients", C.c_int),
+        ("gsph_mono", C.c_int), ("gsph_gradients", C.c_int), ("gsph_wave_speed", C.c_int),
     ]
 
 
@@ -188,6 +188,7 @@ class Options:
     gsph_vol: int = 3
     gsph_mono: int = 1
     gsph_gradients: int = 0
+    gsph_wave_speed: int = 0
 
     def to_c(self) -> PlumeOptions:
         o = PlumeOptions()

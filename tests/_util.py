@@ -52,10 +52,35 @@ def gsph_case(name):
                            vent_dx=25.0, duct_depth=300.0, seed=5, name="gsph_3d")
         c.options.method = cases.METHOD_GSPH
         c.step0 = 48
+    elif name in GSPH_SOLVER_CASES:
+        # the other Riemann solvers on the Sod tube and the 3D cube above
+        base, solver, wave = GSPH_SOLVER_CASES[name]
+        c = gsph_case(base)
+        c.options.gsph_solver = solver
+        c.options.gsph_wave_speed = wave
+        c.name = name
     else:
         raise KeyError(name)
     c.options.gsph_gradients = 1
     return c
+
+
+# fixture name -> (base case, RIEMANN_SOLVER, HLL_WAVE_SPEED_EVA), with the
+# reference build that made it (tests/golden/make_golden.py)
+GSPH_SOLVER_CASES = {
+    "gsph_1d_my2": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 2),
+    "gsph_1d_my3": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 3),
+    "gsph_1d_vl": ("gsph_1d_sod", cases.RIEMANN_VANLEER, 0),
+    "gsph_3d_my3": ("gsph_3d", cases.RIEMANN_HLLC_MY, 3),
+    "gsph_3d_vl": ("gsph_3d", cases.RIEMANN_VANLEER, 0),
+}
+# steps the reference completes on each (the next stops on assert(c > 0))
+GSPH_SOLVER_STEPS = {"gsph_1d_my2": 1, "gsph_1d_my3": 1, "gsph_1d_vl": 7, "gsph_3d_my3": 1, "gsph_3d_vl": 2}
+GSPH_SOLVER_FAILS = {"gsph_1d_my2": True, "gsph_1d_my3": True, "gsph_1d_vl": True, "gsph_3d_my3": True,
+                     "gsph_3d_vl": False}
+GSPH_SOLVER_BUILDS = {"gsph_1d_my2": "ref1d_gsph_my2", "gsph_1d_my3": "ref1d_gsph_my3",
+                      "gsph_1d_vl": "ref1d_gsph_vl", "gsph_3d_my3": "ref3d_gsph_my3",
+                      "gsph_3d_vl": "ref3d_gsph_vl"}
 
 
 def adapt_case():

@@ -114,7 +114,7 @@ def make(case, variant, nsteps, path, sample_lists=64, dump_last=False, perturb_
               "sample_flat": np.concatenate(flat) if flat else np.zeros(0, np.uint64)})
     if o.dim == 3:
         # the lists of the last step were built from the state before it
-        d.update(pack("pre_", steps[-2]["particles"].sorted_by_key()))
+        d.update(pack("pre_", (steps[-2]["particles"] if len(steps) > 1 else case.particles).sorted_by_key()))
     d.update(extra)
     if images is not None:
         d["img_key"] = np.asarray(images[0], dtype=np.uint64)
@@ -176,6 +176,19 @@ def make_gsph():
     make(gsph_case("gsph_1d_sod"), "ref1d_gsph", 20, os.path.join(HERE, "gsph_1d_sod.npz"))
     make(gsph_case("gsph_1d_grad"), "ref1d_gsph_grad", 20, os.path.join(HERE, "gsph_1d_grad.npz"))
     make(gsph_case("gsph_3d"), "ref3d_gsph", 2, os.path.join(HERE, "gsph_3d.npz"))
+    make_gsph_solvers()
+
+
+def make_gsph_solvers():
+    """gsph_1d_my2 / my3 / vl, gsph_3d_my3 / vl: the Sod tube and the 3D cube
+    of gsph_1d_sod / gsph_3d with the reference's other Riemann solvers,
+    HLLC_RP_Solver_my (HLL_WAVE_SPEED_EVA 2 and 3) and VanLeer_RP_Solver,
+    over the steps the reference completes: with HLLC_RP_Solver_my its step
+    2 stops on assert(c > 0) (timestep.cc), with Van Leer's solver the Sod
+    tube's step 9"""
+    from _util import GSPH_SOLVER_BUILDS, GSPH_SOLVER_STEPS
+    for name, build in GSPH_SOLVER_BUILDS.items():
+        make(gsph_case(name), build, GSPH_SOLVER_STEPS[name], os.path.join(HERE, name + ".npz"))
 
 
 def make_adapt():
@@ -362,6 +375,9 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--duct":
         refio.build_ref()
         make_duct()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--gsph-solvers":
+        refio.build_ref()
+        make_gsph_solvers()
     elif len(sys.argv) > 1 and sys.argv[1] == "--inlet":
         refio.build_ref()
         make_inlet()

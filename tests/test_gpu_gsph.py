@@ -202,3 +202,46 @@ def test_gsph_sod_2000_full_run_matches_reference():
         err = np.abs(x - r).sum() / np.abs(r).sum()
         print(f"GSPH sod t=0.2 {f}: L1 gpu-ref {err:.3e}, reference one-ulp floor {floor:.3e}")
         assert err <= 3.0 * floor + 1e-12, (f, err, floor)
+
+
+@pytest.mark.parametrize("name", ["gsph_1d_my2", "gsph_1d_my3", "gsph_1d_vl", "gsph_3d_my3", "gsph_3d_vl"])
+def test_gsph_other_solvers_match_reference(name):
+    """HLLC_RP_Solver_my (HLL_WAVE_SPEED_EVA 2, 3) and VanLeer_RP_Solver on
+    the device against the reference's builds over the steps the reference
+    completes: dt within 1e-12, finite fields within the FP64 tolerance, the
+    same NaN entries (HLLC_RP_Solver_my leaves NaN energies after its first
+    step).  Where the reference then stops (assert(c > 0) of timestep.cc)
+    the device reports an error status within the next two steps."""
+    from plume_gpu.solver import PlumeError
+    from _util import GSPH_SOLVER_FAILS
+    case, d = golden_case(name)
+    s = Solver(case)
+    if case.pre_adaptive:
+        s.adaptive_sml()
+    log = s.steps(int(d["nsteps"]), log=True)
+    np.testing.assert_allclose([r["dt"] for r in log], d["dt"], rtol=1e-12, atol=0)
+    g, ref = s.download().sorted_by_key(), unpack(d, "out_").sorted_by_key()
+    assert np.array_equal(g.key, ref.key)
+    for f in ("x", "y", "z", "vx", "vy", "vz", "rho", "e", "p", "c", "h"):
+        x, y = getattr(g, f), getattr(ref, f)
+        np.testing.assert_array_equal(np.isnan(x), np.isnan(y), err_msg=f)
+        fin = ~np.isnan(y)
+        if fin.any():
+            assert float(np.abs(x[fin] - y[fin]).max()) <= FP64_TOL * max(float(np.abs(y[fin]).max()), 1e-300), f
+    if GSPH_SOLVER_FAILS[name]:
+        with pytest.raises(PlumeError):
+            s.steps(1)
+            s.steps(1)
+    else:
+        s.steps(2)  # the 3D plume goes on with Van Leer's solver
+
+
+def test_gsph_hllc_my_needs_a_wave_speed_the_reference_runs():
+    """HLLC_RP_Solver_my with HLL_WAVE_SPEED_EVA 0 stops the reference's run,
+    and 1, 4, 5 do not compile there: the context refuses them"""
+    from plume_gpu.solver import PlumeError
+    case, _ = golden_case("gsph_1d_my2")
+    for w in (0, 1, 4, 5):
+        case.options.gsph_wave_speed = w
+        with pytest.raises(PlumeError):
+            Solver(case)
