@@ -121,6 +121,15 @@ extern "C" {
 
 /* ---- momentum/energy discretisation (USE_GSPH, options.h:136-142) ------ */
 #define PLUME_METHOD_SPH   0  /* artificial viscosity (mom_engr_update.cc:29-439) */
+#define PLUME_METHOD_GSPH_RCM 2 /* USE_GSPH 2, the random choice method:
+                                 GSPH with the interface at s* = (sp - 1/2)
+                                 |x_i - x_j| and the HLLC problem sampled at
+                                 0.6 (sp - 1/2) |x_i - x_j| against its waves'
+                                 positions S dt, sp the Van der Corput number
+                                 of the step (Generate_VanderCorput,
+                                 sph_lib.cc:2214-2245; HLLC_RP_Solver
+                                 sph_lib.cc:1859-1885; Riemann_Solver
+                                 :2416-2419)                                  */
 #define PLUME_METHOD_GSPH  1  /* Godunov SPH: a Riemann problem per pair
                                  (mom_engr_update.cc:441-1146, SHEAR_VEL_APP 2,
                                  RP_MASS_WEIGHTED 0)                           */

@@ -765,6 +765,61 @@ static void vanleer(double dl, double dr, double pl, double pr, double ul, doubl
     *p_star = p;
 }
 
+/* Generate_VanderCorput (sph_lib.cc:2214-2245): n brought below 65,537 by
+ * steps of 65,536, bits 0..15 of n mirrored about the binary point */
+static double vdc16(unsigned n)
+{
+    while (n > 65536u) n -= 65536u;
+    double v = 0.0, w = 0.5;
+    for (int k = 0; k < 16; k++) {
+        if (n & (1u << k)) v += w;
+        w *= 0.5;
+    }
+    return v;
+}
+
+/* HLLC_RP_Solver under USE_GSPH 2 (sph_lib.cc:1753-1885): the waves of
+ * hllc(), the solution sampled at x = 0.6 (sp - 1/2) dist against the waves'
+ * positions S dt (random choice method) */
+static void hllc_rcm(double dl, double dr, double pl, double pr, double ul, double ur, double gl, double gr,
+                     double sp, double dt, double dist, double *p_star, double *u_star)
+{
+    double rdl = sqrt(dl), rdr = sqrt(dr);
+    double den = 1.0 / (rdl + rdr);
+    double ulr = (ul * rdl + ur * rdr) * den;
+    double plr = (pl * rdl + pr * rdr) * den;
+    double glr = (gl * rdl + gr * rdr) * den;
+    double dlr = (dl * rdl + dr * rdr) * den;
+    double clr = sqrt(glr * plr / dlr);
+    double vl = ul - ulr, vr = ur - ulr;
+    double cl = sqrt(gl * pl / dl), cr = sqrt(gr * pr / dr);
+    double Sl = fmin(vl - cl, -clr);
+    double Sr = fmax(vr + cr, clr);
+    double Sm = (dr * vr * (Sr - vr) - dl * vl * (Sl - vl) + pl - pr) / (dr * (Sr - vr) - dl * (Sl - vl));
+    double ph = dl * (vl - Sl) * (vl - Sm) + pl;
+    double Ml = dl * ul, Mr = dr * ur;
+    double El = dl * (pl / (dl * (gl - 1)) + 0.5 * ul * ul);
+    double Er = dr * (pr / (dr * (gr - 1)) + 0.5 * ur * ur);
+    double xSl = Sl * dt, xSm = Sm * dt, xSr = Sr * dt;
+    double x = (sp - 0.5) * dist * 0.6;
+    if (xSl > x) {
+        *p_star = pl;
+        *u_star = ul;
+    } else if (xSl <= x && xSm > x) {
+        *p_star = Sm / (Sl - Sm) * ((Sl - vl) * Ml + (ph - pl)) + ph;
+        *u_star = (Sm / (Sl - Sm) * ((Sl - vl) * El + ph * Sm - pl * vl) + (Sm + ulr) * ph) / (*p_star);
+    } else if (xSm <= x && xSr > x) {
+        *p_star = Sm / (Sr - Sm) * ((Sr - vr) * Mr + (ph - pr)) + ph;
+        *u_star = (Sm / (Sr - Sm) * ((Sr - vr) * Er + ph * Sm - pr * vr) + (Sm + ulr) * ph) / (*p_star);
+    } else if (xSr <= x) {
+        *p_star = pr;
+        *u_star = ur;
+    } else {
+        *p_star = NAN;
+        *u_star = NAN;
+    }
+}
+
 /* One pair's Riemann problem (Riemann_Solver, sph_lib.cc:2247-2598, USE_GSPH
  * 1, RP_MASS_WEIGHTED 0, SWITCH_OFF_AV_FOR_EXPAN 0, SHEAR_VEL_APP 2): the
  * states projected on e = (x_i - x_j)/|x_i - x_j|; unless the
@@ -783,8 +838,9 @@ typedef struct GsphSide {
 
 static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const double *xj,
                          const GsphSide *I, const GsphSide *J, double dt_half,
-                         double *p_star, double *v_star)
+                         double *p_star, double *v_star, double sp)
 {
+    const int rcm = o->method == PLUME_METHOD_GSPH_RCM;  /* USE_GSPH 2 */
     double dx[3], e[3], dist = 0.0;
     for (int k = 0; k < D; k++) dx[k] = xi[k] - xj[k];
     for (int k = 0; k < D; k++) dist += dx[k] * dx[k];
@@ -839,6 +895,7 @@ static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const d
                          0.25 * hsq * (2.0 * B * Dd + Cc * Cc) + Dd * Dd;
             sij = (0.46875 * h6 * A * B + 0.375 * h4 * (A * Dd + B * Cc) + 0.5 * hsq * Cc * Dd) / Vsq;
         }
+        if (rcm) sij = (sp - 0.5) * dist;
         double delta_i = sij + I->c * dt_half - Si;
         double delta_j = sij - J->c * dt_half - Sj;
         dr = I->rho + drhoi * delta_i;
@@ -866,7 +923,9 @@ static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const d
         }
     }
     double u_star;
-    if (o->gsph_solver == PLUME_RIEMANN_HLLC)
+    if (rcm)
+        hllc_rcm(dl, dr, pl, pr, ul, ur, J->gam, I->gam, sp, 2.0 * dt_half, dist, p_star, &u_star);
+    else if (o->gsph_solver == PLUME_RIEMANN_HLLC)
         hllc(dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
     else if (o->gsph_solver == PLUME_RIEMANN_HLLC_MY)
         hllc_my(o->gsph_wave_speed, dl, dr, pl, pr, ul, ur, J->gam, I->gam, p_star, &u_star);
@@ -895,8 +954,10 @@ static void gsph_riemann(const PlumeOptions *o, int D, const double *xi, const d
  * then v += dt (rhs_v + g e_D), e += dt (rhs_e + v_i,D g), and the commit
  * with the EOS.  grad: the gradients of gsph_gradients or NULL. */
 static int gsph_momentum_pass(const PlumeOptions *o, PlumeSoA *s, size_t n, const Lists *L,
-                              double dt, const double *grad, Work *w, int nthreads)
+                              double dt, const double *grad, Work *w, int nthreads, int step)
 {
+    /* random choice method: the step's sample point (mom_engr_update.cc:513-516) */
+    const double sp = o->method == PLUME_METHOD_GSPH_RCM ? vdc16((unsigned)step) : 0.5;
     const int D = o->dim, NQ = D + 2;
     const double grav = -o->g;
     const double dt_half = 0.5 * dt;
@@ -944,7 +1005,7 @@ static int gsph_momentum_pass(const PlumeOptions *o, PlumeSoA *s, size_t n, cons
                             vel(s, j, D, o->lans, velj);
                             GsphSide J = { s->rho[j], s->p[j], s->c[j], s->gamma[j], s->h[j], velj,
                                            grad ? grad + j * (size_t)(NQ * D) : NULL };
-                            gsph_riemann(o, D, xi, xj, &I, &J, dt_half, &p_star, v_star);
+                            gsph_riemann(o, D, xi, xj, &I, &J, dt_half, &p_star, v_star, sp);
                             for (int k = 0; k < D; k++) velij[k] = veli[k] - velj[k];
                             if (o->lans) tau = eps_mom(velij, Vj, D);
                             if (pass == 0) {
@@ -1556,7 +1617,7 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
         if (dt_log) dt_log[st] = dt;
         Lists L = { 0 };
         long *oldb = NULL;
-        const int gsph = o->method == PLUME_METHOD_GSPH;
+        const int gsph = o->method != PLUME_METHOD_SPH;  /* GSPH or its random choice variant */
         const int recon = gsph && o->gsph_recon != PLUME_RECON_ZEROTH;
         const int need_grad = gsph && (o->gsph_gradients || recon);
         if (D == 3) {
@@ -1578,7 +1639,7 @@ static int steps_impl(const PlumeOptions *o, const PlumeGrid *g, PlumeSoA *s,
             else gsph_gradients(o, s, nn, &L, grad, nthreads);
         }
         if (!rc) {
-            if (gsph) rc = gsph_momentum_pass(o, s, nn, &L, t->dtime, recon ? grad : NULL, &w, nthreads);
+            if (gsph) rc = gsph_momentum_pass(o, s, nn, &L, t->dtime, recon ? grad : NULL, &w, nthreads, t->step);
             else rc = momentum_pass(o, s, nn, &L, t->dtime, &w, nthreads);
         }
         if (!rc && go && st == nsteps - 1) {

@@ -1485,7 +1485,7 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
   k_hmax27<<<nblocks(ctx->nbk, 256), 256, 0, st>>>(ctx->d_geo, ctx->bmember, ctx->nbk, ctx->hb, ctx->h27);
   const int nbw = nblocks(n ? n : 1, WP_WARPS);  // one warp per particle
   const bool mixed = sizeof(T) == 4;
-  const bool gsph = ctx->o.method == PLUME_METHOD_GSPH;
+  const bool gsph = ctx->o.method != PLUME_METHOD_SPH;  // GSPH or its random choice variant
   if constexpr (D == 3) {
     if (lists) {
       if (!compacted) compact_real<MULTI>(ctx, n, nb, tiled);
@@ -1744,11 +1744,11 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
     g_create_error = "dim must be 1 or 3";
     return PLUME_E_INVALID;
   }
-  if (opt->method != PLUME_METHOD_SPH && opt->method != PLUME_METHOD_GSPH) {
-    g_create_error = "method must be PLUME_METHOD_SPH or PLUME_METHOD_GSPH";
+  if (opt->method != PLUME_METHOD_SPH && opt->method != PLUME_METHOD_GSPH && opt->method != PLUME_METHOD_GSPH_RCM) {
+    g_create_error = "method must be PLUME_METHOD_SPH, PLUME_METHOD_GSPH or PLUME_METHOD_GSPH_RCM";
     return PLUME_E_INVALID;
   }
-  if (opt->method == PLUME_METHOD_GSPH) {
+  if (opt->method != PLUME_METHOD_SPH) {
     const int r = opt->gsph_recon;
     const int sv = opt->gsph_solver;
     if (!(sv == PLUME_RIEMANN_ROE || sv == PLUME_RIEMANN_HLLC || sv == PLUME_RIEMANN_HLLC_MY ||
@@ -1901,7 +1901,7 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
         }
       }
     }
-    if (opt->method == PLUME_METHOD_GSPH &&
+    if (opt->method != PLUME_METHOD_SPH &&
         (rc = dev_alloc(ctx, (void**)&ctx->grad, 8 * c * (size_t)((opt->dim + 2) * opt->dim))))
       return fail(rc);
     if (opt->precision == PLUME_PREC_MIXED && opt->dim == 3) {

@@ -207,6 +207,61 @@ __device__ __forceinline__ void rp_hllc(T dl, T dr, T pl, T pr, T ul, T ur, T gl
   }
 }
 
+// Generate_VanderCorput (sph_lib.cc:2214-2245): n brought below 65,537 by
+// steps of 65,536, then its bits 0..15 mirrored about the binary point
+// (bit k weighs 2^-(k+1)); the sample point of the random choice method
+__host__ __device__ inline double vdc16(unsigned n) {
+  while (n > 65536u) n -= 65536u;
+  double v = 0.0, w = 0.5;
+  for (int k = 0; k < 16; k++) {
+    if (n & (1u << k)) v += w;
+    w *= 0.5;
+  }
+  return v;
+}
+
+// HLLC_RP_Solver under USE_GSPH 2 (sph_lib.cc:1753-1885): the waves of
+// rp_hllc, the solution sampled at x = 0.6 (sp - 1/2) |x_i - x_j| against
+// the waves' positions S dt
+template <typename T>
+__device__ __forceinline__ void rp_hllc_rcm(T dl, T dr, T pl, T pr, T ul, T ur, T gl, T gr, T sp, T dt, T dist,
+                                            T& p_star, T& u_star) {
+  const T rdl = sqrt(dl), rdr = sqrt(dr);
+  const T den = T(1) / (rdl + rdr);
+  const T ulr = (ul * rdl + ur * rdr) * den;
+  const T plr = (pl * rdl + pr * rdr) * den;
+  const T glr = (gl * rdl + gr * rdr) * den;
+  const T dlr = (dl * rdl + dr * rdr) * den;
+  const T clr = sqrt(glr * plr / dlr);
+  const T vl = ul - ulr, vr = ur - ulr;
+  const T cl = sqrt(gl * pl / dl), cr = sqrt(gr * pr / dr);
+  const T Sl = fmin(vl - cl, -clr);
+  const T Sr = fmax(vr + cr, clr);
+  const T Sm = (dr * vr * (Sr - vr) - dl * vl * (Sl - vl) + pl - pr) / (dr * (Sr - vr) - dl * (Sl - vl));
+  const T ph = dl * (vl - Sl) * (vl - Sm) + pl;
+  const T Ml = dl * ul, Mr = dr * ur;
+  const T El = dl * (pl / (dl * (gl - T(1))) + T(0.5) * ul * ul);
+  const T Er = dr * (pr / (dr * (gr - T(1))) + T(0.5) * ur * ur);
+  const T xSl = Sl * dt, xSm = Sm * dt, xSr = Sr * dt;
+  const T x = (sp - T(0.5)) * dist * T(0.6);
+  if (xSl > x) {
+    p_star = pl;
+    u_star = ul;
+  } else if (xSl <= x && xSm > x) {
+    p_star = Sm / (Sl - Sm) * ((Sl - vl) * Ml + (ph - pl)) + ph;
+    u_star = (Sm / (Sl - Sm) * ((Sl - vl) * El + ph * Sm - pl * vl) + (Sm + ulr) * ph) / p_star;
+  } else if (xSm <= x && xSr > x) {
+    p_star = Sm / (Sr - Sm) * ((Sr - vr) * Mr + (ph - pr)) + ph;
+    u_star = (Sm / (Sr - Sm) * ((Sr - vr) * Er + ph * Sm - pr * vr) + (Sm + ulr) * ph) / p_star;
+  } else if (xSr <= x) {
+    p_star = pr;
+    u_star = ur;
+  } else {  // NaN wave speeds: the NaN reaches the state and its check
+    p_star = T(NAN);
+    u_star = T(NAN);
+  }
+}
+
 // HLLC_RP_Solver_my (sph_lib.cc:1912-2088): HLLC for strong shocks on
 // velocities relative to the Roe velocity, with the wave-speed estimate of
 // HLL_WAVE_SPEED_EVA (wave: 2 Davis, 3 Toro, the two the reference runs
@@ -320,7 +375,8 @@ __device__ __forceinline__ void rp_vanleer(T dl, T dr, T pl, T pr, T ul, T ur, T
 // transverse velocity.
 template <int D, typename T>
 __device__ __forceinline__ void gsph_riemann(const Opt& o, const T* dx, const GSide<T>& I, const GSide<T>& J,
-                                             T dt_half, T& p_star, T* v_star) {
+                                             T dt_half, T& p_star, T* v_star, T sp = T(0.5)) {
+  const bool rcm = o.method == 2;  // USE_GSPH 2: interface and sampling at sp
   constexpr int NQ = D + 2;
   T dist = 0;
 #pragma unroll
@@ -382,6 +438,7 @@ __device__ __forceinline__ void gsph_riemann(const Opt& o, const T* dx, const GS
                     T(0.25) * hsq * (T(2.0) * Bb * Dd + Cc * Cc) + Dd * Dd;
       sij = (T(0.46875) * h6 * Aa * Bb + T(0.375) * h4 * (Aa * Dd + Bb * Cc) + T(0.5) * hsq * Cc * Dd) / Vsq;
     }
+    if (rcm) sij = (sp - T(0.5)) * dist;
     const T delta_i = sij + I.c * dt_half - Si;
     const T delta_j = sij - J.c * dt_half - Sj;
     dr = I.rho + drhoi * delta_i;
@@ -409,7 +466,9 @@ __device__ __forceinline__ void gsph_riemann(const Opt& o, const T* dx, const GS
     }
   }
   T u_star;
-  if (o.gsph_solver == 1)
+  if (rcm)
+    rp_hllc_rcm<T>(dl, dr, pl, pr, ul, ur, J.gam, I.gam, sp, T(2) * dt_half, dist, p_star, u_star);
+  else if (o.gsph_solver == 1)
     rp_hllc<T>(dl, dr, pl, pr, ul, ur, J.gam, I.gam, p_star, u_star);
   else if (o.gsph_solver == 2)
     rp_hllc_my<T>(o.gsph_wave, dl, dr, pl, pr, ul, ur, J.gam, I.gam, p_star, u_star);
@@ -484,6 +543,8 @@ __global__ void k_gsph_mom(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
   I.g = grad ? grad + (size_t)i * (NQ * D) : nullptr;
   const T tempi = T(A.T[i]), cpi = T(A.cp[i]);
   const T dt_half = T(0.5 * dt);
+  // random choice method: the step's sample point (mom_engr_update.cc:513-516)
+  const T sp = T(o.method == 2 ? vdc16((unsigned)ts->step) : 0.5);
   const double hm = hmax[D == 3 ? b : 0];
   const double R = fmin(o.cutoff2 * hi_d, o.ksupport * 0.5 * (hi_d + hm)) * (1.0 + 1e-10);
   const double grav = -o.g;
@@ -520,7 +581,7 @@ __global__ void k_gsph_mom(Opt o, const Geo* __restrict__ geo, Dev A, Work W, co
       }
       J.g = grad ? grad + (size_t)j * (NQ * D) : nullptr;
       T p_star, v_star[3];
-      gsph_riemann<D, T>(o, dx, I, J, dt_half, p_star, v_star);
+      gsph_riemann<D, T>(o, dx, I, J, dt_half, p_star, v_star, sp);
       T velij[3], tau = 0;
 #pragma unroll
       for (int k = 0; k < D; k++) velij[k] = I.v[k] - J.v[k];

@@ -37,7 +37,7 @@ BUCKET_UNDERGROUND, BUCKET_PRESS_BC = 0x8, 0x10
 BINV_NONE, BINV_POTENTIAL, BINV_INVOLVED, BINV_BOTH = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 KERNEL_GAUSS, KERNEL_M4 = 0, 1
-METHOD_SPH, METHOD_GSPH = 0, 1
+METHOD_SPH, METHOD_GSPH, METHOD_GSPH_RCM = 0, 1, 2
 RIEMANN_ROE, RIEMANN_HLLC, RIEMANN_HLLC_MY, RIEMANN_VANLEER = 0, 1, 2, 3
 RECON_NONE, RECON_EACH, RECON_PAIRWISE, RECON_ALL, RECON_ZEROTH, RECON_EACH_SHOCK = 0, 1, 2, 3, 4, 10
 

@@ -27,7 +27,7 @@ import numpy as np
 from .abi import (BC_ERUPT, BC_NOSAVE_REAL, BC_PRESSURE, BC_REAL, BC_WALL,
                   BINV_NONE, BINV_POTENTIAL, BUCKET_PRESS_BC, BUCKET_UNDERGROUND,
                   BUCKET_ABSORBING, BUCKET_MIXED, KERNEL_GAUSS, KERNEL_M4,
-                  METHOD_GSPH, METHOD_SPH, PREC_FP64, RECON_EACH, RECON_ZEROTH, RIEMANN_HLLC,
+                  METHOD_GSPH, METHOD_GSPH_RCM, METHOD_SPH, PREC_FP64, RECON_EACH, RECON_ZEROTH, RIEMANN_HLLC,
                   RIEMANN_HLLC_MY, RIEMANN_VANLEER,
                   Grid, Options, ParticleSet)
 

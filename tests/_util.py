@@ -54,10 +54,11 @@ def gsph_case(name):
         c.step0 = 48
     elif name in GSPH_SOLVER_CASES:
         # the other Riemann solvers on the Sod tube and the 3D cube above
-        base, solver, wave = GSPH_SOLVER_CASES[name]
+        base, solver, wave, method = GSPH_SOLVER_CASES[name]
         c = gsph_case(base)
         c.options.gsph_solver = solver
         c.options.gsph_wave_speed = wave
+        c.options.method = method
         c.name = name
     else:
         raise KeyError(name)
@@ -68,19 +69,24 @@ def gsph_case(name):
 # fixture name -> (base case, RIEMANN_SOLVER, HLL_WAVE_SPEED_EVA), with the
 # reference build that made it (tests/golden/make_golden.py)
 GSPH_SOLVER_CASES = {
-    "gsph_1d_my2": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 2),
-    "gsph_1d_my3": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 3),
-    "gsph_1d_vl": ("gsph_1d_sod", cases.RIEMANN_VANLEER, 0),
-    "gsph_3d_my3": ("gsph_3d", cases.RIEMANN_HLLC_MY, 3),
-    "gsph_3d_vl": ("gsph_3d", cases.RIEMANN_VANLEER, 0),
+    "gsph_1d_my2": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 2, cases.METHOD_GSPH),
+    "gsph_1d_my3": ("gsph_1d_sod", cases.RIEMANN_HLLC_MY, 3, cases.METHOD_GSPH),
+    "gsph_1d_vl": ("gsph_1d_sod", cases.RIEMANN_VANLEER, 0, cases.METHOD_GSPH),
+    "gsph_3d_my3": ("gsph_3d", cases.RIEMANN_HLLC_MY, 3, cases.METHOD_GSPH),
+    "gsph_3d_vl": ("gsph_3d", cases.RIEMANN_VANLEER, 0, cases.METHOD_GSPH),
+    # the random choice method (USE_GSPH 2) with the bases' solvers set aside
+    "gsph_1d_rcm": ("gsph_1d_sod", cases.RIEMANN_HLLC, 0, cases.METHOD_GSPH_RCM),
+    "gsph_3d_rcm": ("gsph_3d", cases.RIEMANN_HLLC, 0, cases.METHOD_GSPH_RCM),
 }
 # steps the reference completes on each (the next stops on assert(c > 0))
-GSPH_SOLVER_STEPS = {"gsph_1d_my2": 1, "gsph_1d_my3": 1, "gsph_1d_vl": 7, "gsph_3d_my3": 1, "gsph_3d_vl": 2}
+GSPH_SOLVER_STEPS = {"gsph_1d_my2": 1, "gsph_1d_my3": 1, "gsph_1d_vl": 7, "gsph_3d_my3": 1, "gsph_3d_vl": 2,
+                     "gsph_1d_rcm": 20, "gsph_3d_rcm": 2}
 GSPH_SOLVER_FAILS = {"gsph_1d_my2": True, "gsph_1d_my3": True, "gsph_1d_vl": True, "gsph_3d_my3": True,
-                     "gsph_3d_vl": False}
+                     "gsph_3d_vl": False, "gsph_1d_rcm": False, "gsph_3d_rcm": False}
 GSPH_SOLVER_BUILDS = {"gsph_1d_my2": "ref1d_gsph_my2", "gsph_1d_my3": "ref1d_gsph_my3",
                       "gsph_1d_vl": "ref1d_gsph_vl", "gsph_3d_my3": "ref3d_gsph_my3",
-                      "gsph_3d_vl": "ref3d_gsph_vl"}
+                      "gsph_3d_vl": "ref3d_gsph_vl", "gsph_1d_rcm": "ref1d_gsph_rcm",
+                      "gsph_3d_rcm": "ref3d_gsph_rcm"}
 
 
 def adapt_case():

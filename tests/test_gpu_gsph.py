@@ -204,7 +204,8 @@ def test_gsph_sod_2000_full_run_matches_reference():
         assert err <= 3.0 * floor + 1e-12, (f, err, floor)
 
 
-@pytest.mark.parametrize("name", ["gsph_1d_my2", "gsph_1d_my3", "gsph_1d_vl", "gsph_3d_my3", "gsph_3d_vl"])
+@pytest.mark.parametrize("name", ["gsph_1d_my2", "gsph_1d_my3", "gsph_1d_vl", "gsph_3d_my3", "gsph_3d_vl",
+                                  "gsph_1d_rcm", "gsph_3d_rcm"])
 def test_gsph_other_solvers_match_reference(name):
     """HLLC_RP_Solver_my (HLL_WAVE_SPEED_EVA 2, 3) and VanLeer_RP_Solver on
     the device against the reference's builds over the steps the reference

@@ -455,7 +455,8 @@ def _finite_and_nan_match(a, b, tol, fields=DOUBLE_FIELDS):
     return nans
 
 
-@pytest.mark.parametrize("name", ["gsph_1d_my2", "gsph_1d_my3", "gsph_1d_vl", "gsph_3d_my3", "gsph_3d_vl"])
+@pytest.mark.parametrize("name", ["gsph_1d_my2", "gsph_1d_my3", "gsph_1d_vl", "gsph_3d_my3", "gsph_3d_vl",
+                                  "gsph_1d_rcm", "gsph_3d_rcm"])
 def test_oracle_gsph_other_solvers_match_reference(name):
     """HLLC_RP_Solver_my (HLL_WAVE_SPEED_EVA 2, 3) and VanLeer_RP_Solver
     against the reference's own builds over the steps it completes: the
