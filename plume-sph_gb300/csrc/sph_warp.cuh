@@ -754,7 +754,7 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geos<MULTI> geo, Dev A, W
 // candidate filtering is paid once per step instead of once per sweep.
 constexpr int LCAP = 160;                 // windows per particle
 #ifndef PLUME_LIST_STREAM
-#define PLUME_LIST_STREAM 1  // list entries stored and loaded evict-first
+#define PLUME_LIST_STREAM 0  // 1: list entries stored and loaded evict-first (measured slower)
 #endif
 __device__ __forceinline__ uint2 list_load(const uint2* p) {
 #if PLUME_LIST_STREAM
