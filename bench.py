@@ -208,16 +208,22 @@ def cpu_state(case):
     return dataclasses.replace(case, particles=o.ps)
 
 
-def density_l1(ref, other):
+def density_l1(ref, other, jet_radius=2000.0):
     """relative L1 density error of `other` against `ref` over the
-    need_neigh particles present in both (matched by key)"""
+    need_neigh particles present in both (matched by key); also over the
+    particles farther than jet_radius from the vent axis (the ambient
+    atmosphere, outside the jet)"""
     a, b = ref.sorted_by_key(), other.sorted_by_key()
     common, ia, ib = np.intersect1d(a.key, b.key, return_indices=True)
     real = a.need_neigh()[ia] & b.need_neigh()[ib]
     ra, rb = a.rho[ia][real], b.rho[ib][real]
+    far = (a.x[ia][real] ** 2 + a.y[ia][real] ** 2) > jet_radius ** 2
     return {"l1": float(np.abs(rb - ra).sum() / np.abs(ra).sum()),
             "max_rel": float((np.abs(rb - ra) / np.abs(ra)).max()),
-            "particles": int(real.sum())}
+            "particles": int(real.sum()),
+            "l1_beyond_2km_of_the_vent_axis": float(np.abs(rb - ra)[far].sum() / np.abs(ra)[far].sum())
+            if far.any() else None,
+            "particles_within_2km": int((~far).sum())}
 
 
 def cpu_sample(case, budget_s: float = 12.0, nthreads: int = 0):
@@ -489,6 +495,9 @@ def main():
     ap.add_argument("--only-riemann1d", action="store_true",
                     help="run only the 1D Riemann ensemble leg (--steps timed steps after --warmup) "
                          "and print its object")
+    ap.add_argument("--accuracy-control", action="store_true",
+                    help="with --accuracy-steps: also run the FP64 path from positions moved by one FP32 "
+                         "rounding and report its density error against FP64")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="also report the mixed path's density error against FP64 after this "
                          "many steps (beyond the timed window's end)")
@@ -652,8 +661,20 @@ def main():
             s64.close()
             sm = solver(case)
             sm.steps(args.accuracy_steps)
-            accuracy.append(dict(step=args.accuracy_steps, **density_l1(ref, sm.download())))
+            entry = dict(step=args.accuracy_steps, **density_l1(ref, sm.download()))
             sm.close()
+            if args.accuracy_control:
+                # the FP64 path from positions moved by one FP32 rounding
+                # (2^-24 relative): the spread an FP32-size change of the
+                # state alone produces over the same steps
+                cp = with_subcells(make(PREC_FP64), sub)
+                for f in ("x", "y", "z"):
+                    setattr(cp.particles, f, getattr(cp.particles, f) * (1.0 + 2.0 ** -24))
+                sp = solver(cp)
+                sp.steps(args.accuracy_steps)
+                entry["fp64_fp32_perturbed_vs_fp64"] = density_l1(ref, sp.download())
+                sp.close()
+            accuracy.append(entry)
         else:
             s64.close()
     cpu = None

@@ -252,14 +252,32 @@ __global__ void k_hmax_reset(unsigned long long* hb, int nbk) {
 }
 // per-bucket tables cover the buckets of every member (a 1D member has one
 // entry: the maximum over all its particles)
+// Per-bucket maximum h (1D: per member).  Positive doubles order like their
+// bit patterns, so the maximum is an integer atomicMax.  In the sorted order
+// a warp's particles mostly share one bucket (in 1D one member): such a warp
+// reduces by shuffles and makes one atomic, where 32 atomics on one address
+// would serialise; mixed warps fall back to one atomic per particle.
 __global__ void k_hmax(const Geo* __restrict__ geo, Dev A, const int* __restrict__ d_count,
                        unsigned long long* hb, int dim) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *d_count) return;
-  if (A.bc[i] == BC_DEAD) return;
-  double h = A.h[i];
-  const int base = geo[A.mem[i]].bucket_base;
-  atomicMax(&hb[base + (dim == 3 ? A.bkt[i] : 0)], dbits(h));
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool ok = i < *d_count && A.bc[i] != BC_DEAD;
+  unsigned long long v = 0ull;
+  int key = -1;
+  if (ok) {
+    v = dbits(A.h[i]);
+    key = geo[A.mem[i]].bucket_base + (dim == 3 ? A.bkt[i] : 0);
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  if (peers == 0xffffffffu) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && key >= 0) atomicMax(&hb[key], v);
+  } else if (ok) {
+    atomicMax(&hb[key], v);
+  }
 }
 __global__ void k_hmax27(const Geo* __restrict__ geo, const uint16_t* __restrict__ bmember, int nbk_all,
                          const unsigned long long* __restrict__ hb_all, double* __restrict__ h27_all) {

@@ -217,6 +217,50 @@ struct Acc<float> {
   __device__ __forceinline__ float get() const { return s; }
 };
 
+// Cascaded compensated accumulator of the list sweeps: terms are summed in
+// plain arithmetic into a partial (the few pairs of one list window or row
+// segment), and each partial is added to a compensated (Kahan) sum by
+// flush().  FP64: plain.
+template <typename T>
+struct CAcc {
+  T s;
+  __device__ __forceinline__ CAcc() : s(0) {}
+  __device__ __forceinline__ void add(T v) { s += v; }
+  __device__ __forceinline__ void sub(T v) { s -= v; }
+  __device__ __forceinline__ void flush() {}
+  __device__ __forceinline__ T get() { return s; }
+};
+#ifndef PLUME_CASCADE
+#define PLUME_CASCADE 0  // 1: plain partial sums per window, compensated across windows (measured slower)
+#endif
+#if PLUME_CASCADE
+template <>
+struct CAcc<float> {
+  Acc<float> k;
+  float w;
+  __device__ __forceinline__ CAcc() : w(0.f) {}
+  __device__ __forceinline__ void add(float v) { w += v; }
+  __device__ __forceinline__ void sub(float v) { w -= v; }
+  __device__ __forceinline__ void flush() {
+    k.add(w);
+    w = 0.f;
+  }
+  __device__ __forceinline__ float get() {
+    flush();
+    return k.get();
+  }
+};
+#else
+template <>
+struct CAcc<float> {
+  Acc<float> k;
+  __device__ __forceinline__ void add(float v) { k.add(v); }
+  __device__ __forceinline__ void sub(float v) { k.add(-v); }
+  __device__ __forceinline__ void flush() {}
+  __device__ __forceinline__ float get() { return k.get(); }
+};
+#endif
+
 // Particle::update_second_var (particle.cc:528-604), ideal-gas mixture
 __device__ __forceinline__ void eos(const Opt& o, double rho, double Y, double e, double& gam, double& p,
                                     double& c, double& T, double& cp, bool lans) {

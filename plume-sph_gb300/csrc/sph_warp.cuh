@@ -113,6 +113,7 @@ __device__ __forceinline__ void wp_walk(const Geo& g, const uint32_t* __restrict
           if (count >= 32) {
             T d[3] = {B.dx[0][lane], B.dx[1][lane], B.dx[2][lane]};
             s.math(B.j[lane], d, B.dx[3][lane]);
+            if constexpr (sizeof(T) == 4) s.flush();
             __syncwarp();
             const int rest = count - 32;
             if (lane < rest) {
@@ -168,7 +169,10 @@ struct WMom {
   T xs[3], hi, supp, Lb, rhoi, Vi, pvsqi, ci, tempi, Cp_i, veli[3];
   __device__ __forceinline__ const T* xpos() const { return xs; }
   T ks_half, ata, alpha, beta;  // option constants in the sweep's type
-  Acc<T> rv[3], re;
+  CAcc<T> rv[3], re;
+  __device__ __forceinline__ void flush() {
+    rv[0].flush(); rv[1].flush(); rv[2].flush(); re.flush();
+  }
   __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   // i-side set-up; returns false (with the status set) when i is skipped
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState* ts,
@@ -204,6 +208,7 @@ struct WMom {
     ata = T(o.ata);
     alpha = T(o.alpha);
     beta = T(o.beta);
+    heatc = T(0.5 * 10.0 * EPS_HALF / PRANDTL) * Vi;
     return true;
   }
   template <bool WARP>
@@ -273,15 +278,16 @@ struct WMom {
     rv[2].sub(gm * s2);
     float heat_tran = 0.0f;
     if (lans) {
-      const float Cp_ij = 0.5f * (rj.z + Cp_i);
+      // m_j V_j V_i k_ij (T_i - T_j) f/h with k_ij = 10 eps Cp_ij |dx|^2
+      // |v_ij|^2 / (Pr dotvr h c_ab): the constants and V_i in heatc
       const float dotvr = fabsf(v0 * d0) + fabsf(v1 * d1) + fabsf(v2 * d2);
-      const float kij = 10.0f * float(EPS_HALF) * Cp_ij * dist_sq * dotv *
-                        rcp<float>(float(PRANDTL) * dotvr * h * sndspdab);
-      heat_tran = (dotvr != 0.0f) ? qj.x * qj.z * Vi * kij * (tempi - rj.y) * (f * ih) : 0.0f;
+      const float num = heatc * (qj.x * qj.z) * (rj.z + Cp_i) * (dist_sq * dotv) * (tempi - rj.y) * (f * ih);
+      heat_tran = (dotvr != 0.0f) ? num * rcp<float>(dotvr * h * sndspdab) : 0.0f;
     }
     re.add(0.5f * gm * ih * vrab + heat_tran);
   }
   static constexpr float KF = float(-2.0 * T1_INV_SQRT_PI * T1_INV_SQRT_PI * T1_INV_SQRT_PI);
+  T heatc;  // 0.5 * 10 eps / Pr * V_i: the pair-independent factors of the heat term
   __device__ __forceinline__ void math(uint32_t j, const T* dx, T hj) {
     T mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj[3];
     load_j(j, mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj);
@@ -418,8 +424,11 @@ struct WDens {
   int pgc;
   T xs[3], hi, supp, Lb, ks_half;
   __device__ __forceinline__ const T* xpos() const { return xs; }
-  Acc<T> rho1, rho2, wnorm_e, engr;
+  CAcc<T> rho1, rho2, wnorm_e, engr;
   bool esm;
+  __device__ __forceinline__ void flush() {
+    rho1.flush(); rho2.flush(); wnorm_e.flush(); engr.flush();
+  }
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
                                         double* xi, int* bi, double& R) {
@@ -583,7 +592,10 @@ struct WVel {
   T xs[3], hi, supp, ks, Lb, vi[3];
   __device__ __forceinline__ const T* xpos() const { return xs; }
   T ihi, r3;  // 1/h_i and (1/(sqrt(pi) h_i))^3 (mixed Gaussian)
-  Acc<T> dv[3], wnorm;
+  CAcc<T> dv[3], wnorm;
+  __device__ __forceinline__ void flush() {
+    dv[0].flush(); dv[1].flush(); dv[2].flush(); wnorm.flush();
+  }
   __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   double vi_d[3];
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double*, TimeState*,
@@ -736,6 +748,7 @@ __global__ void __launch_bounds__(128) k_sweep3(Opt o, Geos<MULTI> geo, Dev A, W
         T dx[3], hj;
         if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
       }
+      if constexpr (sizeof(T) == 4) s.flush();
     });
     s.template finish<false>(i, W, ts);
   }
@@ -926,6 +939,7 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
         T dx[3], hj;
         if (s.filter(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
       }
+      if constexpr (sizeof(T) == 4) s.flush();  // one partial per row segment
     });
   } else if (c > 0) {
     const uint2* ent = L.e + (size_t)i * LCAP;
@@ -945,6 +959,7 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     if constexpr (sizeof(T) == 4) fused = s.o.kernel != 1;
     while (true) {
       if (mask == 0) {  // stored windows are never empty: one step suffices
+        if constexpr (sizeof(T) == 4) s.flush();  // one partial per window
         if (++q >= c) break;
         en = list_load(ent + q);
         mask = en.y;
@@ -1115,7 +1130,10 @@ __global__ void __launch_bounds__(128, SweepMinBlocksW<SW>::v)
       cnt += tot;
       __syncwarp();
       int b = 0;
-      for (; b + 32 <= cnt; b += 32) pair(q[b + lane]);
+      for (; b + 32 <= cnt; b += 32) {
+        pair(q[b + lane]);
+        s.flush();
+      }
       const int rest = cnt - b;  // < 32: moved to the queue's front
       const uint32_t keep = (lane < rest) ? q[b + lane] : 0u;
       __syncwarp();

@@ -82,7 +82,7 @@ GSPH_SOLVER_CASES = {
 GSPH_SOLVER_STEPS = {"gsph_1d_my2": 1, "gsph_1d_my3": 1, "gsph_1d_vl": 7, "gsph_3d_my3": 1, "gsph_3d_vl": 2,
                      "gsph_1d_rcm": 20, "gsph_3d_rcm": 2}
 GSPH_SOLVER_FAILS = {"gsph_1d_my2": True, "gsph_1d_my3": True, "gsph_1d_vl": True, "gsph_3d_my3": True,
-                     "gsph_3d_vl": False, "gsph_1d_rcm": False, "gsph_3d_rcm": False}
+                     "gsph_3d_vl": True, "gsph_1d_rcm": False, "gsph_3d_rcm": False}
 GSPH_SOLVER_BUILDS = {"gsph_1d_my2": "ref1d_gsph_my2", "gsph_1d_my3": "ref1d_gsph_my3",
                       "gsph_1d_vl": "ref1d_gsph_vl", "gsph_3d_my3": "ref3d_gsph_my3",
                       "gsph_3d_vl": "ref3d_gsph_vl", "gsph_1d_rcm": "ref1d_gsph_rcm",

@@ -211,8 +211,9 @@ def test_gsph_other_solvers_match_reference(name):
     the device against the reference's builds over the steps the reference
     completes: dt within 1e-12, finite fields within the FP64 tolerance, the
     same NaN entries (HLLC_RP_Solver_my leaves NaN energies after its first
-    step).  Where the reference then stops (assert(c > 0) of timestep.cc)
-    the device reports an error status within the next two steps."""
+    step, Van Leer's turns positions NaN at the Sod tube's step 8 and the
+    plume's fourth step).  Where the reference's state turns NaN the device
+    reports an error status within the next two steps."""
     from plume_gpu.solver import PlumeError
     from _util import GSPH_SOLVER_FAILS
     case, d = golden_case(name)
@@ -234,7 +235,7 @@ def test_gsph_other_solvers_match_reference(name):
             s.steps(1)
             s.steps(1)
     else:
-        s.steps(2)  # the 3D plume goes on with Van Leer's solver
+        s.steps(2)  # the random choice method goes on
 
 
 def test_gsph_hllc_my_needs_a_wave_speed_the_reference_runs():

@@ -464,7 +464,8 @@ def test_oracle_gsph_other_solvers_match_reference(name):
     NaN entries.  The reference's HLLC_RP_Solver_my takes u* = sqrt(2 (E*_l -
     e*_l)), NaN where that is negative, so its first step already leaves
     NaN energies (the next step stops on assert(c > 0)); Van Leer's solver
-    runs the 3D plume and leaves the Sod tube with NaN positions at step 8."""
+    leaves NaN positions at the Sod tube's step 8 and the plume's fourth
+    step."""
     from _util import GSPH_SOLVER_CASES
     case, d = golden_case(name)
     assert case.options.gsph_solver == GSPH_SOLVER_CASES[name][1]
