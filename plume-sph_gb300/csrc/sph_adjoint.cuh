@@ -123,6 +123,7 @@ struct AdjIn {
 // formed again for the adjoint of dt.
 struct VMom {
   WMom<double> f;
+  static constexpr bool kListAhead = false;  // the list walk's plain entry loads
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
@@ -366,6 +367,7 @@ struct VMom {
 // W(dx, h_ij/4) / sum (m_j/rho_j) W(dx, h_ij/4).
 struct VDens {
   WDens<double> f;
+  static constexpr bool kListAhead = false;  // the list walk's plain entry loads
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
@@ -443,6 +445,7 @@ struct VDens {
 // v_i) / sum w_j, w_j = (m_j / rho_j) W(dx, h_i).
 struct VVel {
   WVel<double> f;
+  static constexpr bool kListAhead = false;  // the list walk's plain entry loads
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;

@@ -149,6 +149,15 @@ struct JPos<double> {
     h = A.h[j];
   }
 };
+// list sweeps that load the next window's list entry one window ahead
+// (S::kListAhead): on the 134^3 plume at h ~ 1.5 dx the momentum sweep 13.44
+// -> 12.87 ms and the LANS filter 8.02 -> 7.72 ms, while the density sweep
+// (64 registers, no spare one) went 7.87 -> 8.08 ms and keeps the plain load.
+// 0 turns it off everywhere.
+#ifndef PLUME_LIST_AHEAD
+#define PLUME_LIST_AHEAD 1
+#endif
+
 template <>
 struct JPos<float> {
   __device__ __forceinline__ static void get(const Dev&, const Packed& K, uint32_t j, float* x, float& h) {
@@ -173,6 +182,7 @@ struct WMom {
   __device__ __forceinline__ void flush() {
     rv[0].flush(); rv[1].flush(); rv[2].flush(); re.flush();
   }
+  static constexpr bool kListAhead = true;  // the list walk's entry look-ahead
   __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   // i-side set-up; returns false (with the status set) when i is skipped
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState* ts,
@@ -208,7 +218,6 @@ struct WMom {
     ata = T(o.ata);
     alpha = T(o.alpha);
     beta = T(o.beta);
-    heatc = T(0.5 * 10.0 * EPS_HALF / PRANDTL) * Vi;
     return true;
   }
   template <bool WARP>
@@ -279,15 +288,16 @@ struct WMom {
     float heat_tran = 0.0f;
     if (lans) {
       // m_j V_j V_i k_ij (T_i - T_j) f/h with k_ij = 10 eps Cp_ij |dx|^2
-      // |v_ij|^2 / (Pr dotvr h c_ab): the constants and V_i in heatc
+      // |v_ij|^2 / (Pr dotvr h c_ab)
+      const float Cp_ij = 0.5f * (rj.z + Cp_i);
       const float dotvr = fabsf(v0 * d0) + fabsf(v1 * d1) + fabsf(v2 * d2);
-      const float num = heatc * (qj.x * qj.z) * (rj.z + Cp_i) * (dist_sq * dotv) * (tempi - rj.y) * (f * ih);
-      heat_tran = (dotvr != 0.0f) ? num * rcp<float>(dotvr * h * sndspdab) : 0.0f;
+      const float kij = 10.0f * float(EPS_HALF) * Cp_ij * dist_sq * dotv *
+                        rcp<float>(float(PRANDTL) * dotvr * h * sndspdab);
+      heat_tran = (dotvr != 0.0f) ? qj.x * qj.z * Vi * kij * (tempi - rj.y) * (f * ih) : 0.0f;
     }
     re.add(0.5f * gm * ih * vrab + heat_tran);
   }
   static constexpr float KF = float(-2.0 * T1_INV_SQRT_PI * T1_INV_SQRT_PI * T1_INV_SQRT_PI);
-  T heatc;  // 0.5 * 10 eps / Pr * V_i: the pair-independent factors of the heat term
   __device__ __forceinline__ void math(uint32_t j, const T* dx, T hj) {
     T mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj[3];
     load_j(j, mj, rhoj, Vj, pVVj, cj, Tj, cpj, vj);
@@ -429,6 +439,7 @@ struct WDens {
   __device__ __forceinline__ void flush() {
     rho1.flush(); rho2.flush(); wnorm_e.flush(); engr.flush();
   }
+  static constexpr bool kListAhead = false;  // the list walk's entry look-ahead
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
                                         double* xi, int* bi, double& R) {
@@ -596,6 +607,7 @@ struct WVel {
   __device__ __forceinline__ void flush() {
     dv[0].flush(); dv[1].flush(); dv[2].flush(); wnorm.flush();
   }
+  static constexpr bool kListAhead = true;  // the list walk's entry look-ahead
   __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   double vi_d[3];
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double*, TimeState*,
@@ -945,8 +957,12 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     const uint2* ent = L.e + (size_t)i * LCAP;
     const T delT = T(g.del);
     int q = 0;
-    // list entries are streamed (evict-first): the particle records stay cached
+    // the next window's entry is loaded one window ahead, so that its load
+    // (mostly an L2 or DRAM access: the lists are read once per sweep) is
+    // in flight while the current window's pairs are summed
+    constexpr bool ahead = PLUME_LIST_AHEAD && S::kListAhead;
     uint2 en = list_load(ent);
+    uint2 nx = ahead ? list_load(ent + (c > 1 ? 1 : 0)) : en;
     uint32_t mask = en.y;
     bool own;
     T ox, oy, oz;
@@ -961,7 +977,12 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
       if (mask == 0) {  // stored windows are never empty: one step suffices
         if constexpr (sizeof(T) == 4) s.flush();  // one partial per window
         if (++q >= c) break;
-        en = list_load(ent + q);
+        if (ahead) {
+          en = nx;
+          nx = list_load(ent + min(q + 1, (int)c - 1));  // the last one again at the end
+        } else {
+          en = list_load(ent + q);
+        }
         mask = en.y;
         decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
         ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
