@@ -439,7 +439,10 @@ struct WDens {
   __device__ __forceinline__ void flush() {
     rho1.flush(); rho2.flush(); wnorm_e.flush(); engr.flush();
   }
-  static constexpr bool kListAhead = false;  // the list walk's entry look-ahead
+#ifndef PLUME_DENS_AHEAD
+#define PLUME_DENS_AHEAD 0
+#endif
+  static constexpr bool kListAhead = PLUME_DENS_AHEAD;  // the list walk's entry look-ahead
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
                                         double* xi, int* bi, double& R) {
@@ -803,8 +806,9 @@ struct NList {
   uint16_t* cnt;   // windows per particle, or NL_OVERFLOW
 };
 
-// like for_segments, with the bucket offset of the segment as a code
-// (dbx+1)*9 + (dby+1)*3 + (dbz+1), db = segment bucket - own bucket
+// like for_segments, with the bucket offset of the segment as a code of
+// three 2-bit fields, (dbx+1) | (dby+1) << 2 | (dbz+1) << 4, db = segment
+// bucket - own bucket (OWN_CODE: the own bucket)
 template <typename T, class F>
 __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* __restrict__ cs,
                                                   const float* xr, const int* bi, double R, F&& f) {
@@ -820,7 +824,7 @@ __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* 
       while (cx <= hi[0]) {
         const int bx = cx / g.s;
         const int e = min(hi[0], bx * g.s + g.s - 1);
-        const int code = (bx - bi[0] + 1) * 9 + (by - bi[1] + 1) * 3 + (bz - bi[2] + 1);
+        const int code = (bx - bi[0] + 1) | (by - bi[1] + 1) << 2 | (bz - bi[2] + 1) << 4;
         f(cs[rowbase + cx], cs[rowbase + e + 1], code);
         cx = e + 1;
       }
@@ -830,14 +834,38 @@ __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* 
 
 // delT: the bucket edge in the sweep's type, formed once per particle (the
 // FP64 pipe of sm_103a is narrow: no double arithmetic per window)
+constexpr int OWN_CODE = 1 | 1 << 2 | 1 << 4;
 template <typename T>
 __device__ __forceinline__ void decode_offsets(T delT, int code, bool& own, T& ox, T& oy, T& oz) {
-  own = (code == 13);
+  own = (code == OWN_CODE);
   constexpr bool REL = sizeof(T) == 4;
-  const int dbx = code / 9 - 1, dby = (code / 3) % 3 - 1, dbz = code % 3 - 1;
+  const int dbx = (code & 3) - 1, dby = ((code >> 2) & 3) - 1, dbz = (code >> 4) - 1;
   ox = REL ? T(-dbx) * delT : T(0);
   oy = REL ? T(-dby) * delT : T(0);
   oz = REL ? T(-dbz) * delT : T(0);
+}
+
+// FP32 list test of the nb <= 32 candidates from wb on (P records): bit q
+// set when max_k |xsh_k - x_k| <= min(Ti, max(kB |h_j| + kA, kC)) -- one
+// threshold per candidate, min(list and CUTOFF2 boxes, support box), the
+// first exactly as the sweeps assume, the support term (which the sweeps
+// test again) with a wider margin.  Branch-free, loads issued 4 at a time.
+__device__ __forceinline__ uint32_t window_mask(const Packed& K, uint32_t wb, int nb, const float* xsh, float Ti,
+                                                float kA, float kB, float kC) {
+  uint32_t mask = 0;
+  for (int q = 0; q < nb; q += 4) {
+    float4 pr[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) pr[u] = (q + u < nb) ? K.P[wb + q + u] : make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float dx0 = fabsf(xsh[0] - pr[u].x), dx1 = fabsf(xsh[1] - pr[u].y), dx2 = fabsf(xsh[2] - pr[u].z);
+      const float m = fmaxf(dx0, fmaxf(dx1, dx2));
+      const float thr = fminf(Ti, fmaxf(fmaf(kB, fabsf(pr[u].w), kA), kC));
+      mask |= (uint32_t)(m <= thr) << (q + u);
+    }
+  }
+  return mask & ((nb == 32) ? 0xffffffffu : ((1u << nb) - 1u));
 }
 
 // union filter of the momentum, density and velocity sweeps
@@ -888,21 +916,7 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
       const int nb = (int)min(32u, j1 - wb);
       uint32_t mask = 0;
       if constexpr (sizeof(T) == 4) {
-        // branch-free tests, record loads issued 4 at a time
-        for (int q = 0; q < nb; q += 4) {
-          float4 pr[4];
-#pragma unroll
-          for (int u = 0; u < 4; u++)
-            pr[u] = (q + u < nb) ? K.P[wb + q + u] : make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const float dx0 = fabsf(xsh[0] - pr[u].x), dx1 = fabsf(xsh[1] - pr[u].y), dx2 = fabsf(xsh[2] - pr[u].z);
-            const float m = fmaxf(dx0, fmaxf(dx1, dx2));
-            const float thr = fminf(Ti, fmaxf(fmaf(kB, fabsf(pr[u].w), kA), kC));
-            mask |= (uint32_t)(m <= thr) << (q + u);
-          }
-        }
-        mask &= (nb == 32) ? 0xffffffffu : ((1u << nb) - 1u);
+        mask = window_mask(K, wb, nb, xsh, Ti, kA, kB, kC);
       } else {
         for (int q = 0; q < nb; q++) {
           T xj[3], hj;
@@ -915,14 +929,109 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
         }
       }
       if (mask) {
-        // streaming store: the lists are read once per sweep and should not
-        // push the sweeps' particle records out of L2
         if (cnt < LCAP) list_store(out + cnt, make_uint2(wb | ((uint32_t)code << 26), mask));
         cnt++;
       }
     }
   });
   L.cnt[i] = (cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
+}
+
+// FP32 list build with one warp per particle.  The rows (cz, cy) of the
+// particle's cell box are dealt to the lanes 32 at a time; a lane tests the
+// candidates of its row's segments (window_mask, the tests of
+// k_build_lists) and stages the row's non-empty windows in shared memory;
+// an exclusive warp scan of the lanes' window counts places them, so the
+// windows reach the list in the walk's order (row, segment, window) and the
+// list is the one k_build_lists writes.  The rows of a box hold similar
+// numbers of candidates, so a warp's lanes stay busy together, where with
+// one thread per particle the lanes walk different numbers of segments.  A
+// row with more than WB_STAGE non-empty windows marks the particle
+// NL_OVERFLOW (its sweeps walk its rows instead).
+constexpr int WB_WARPS = 4;  // warps per block of 128 threads
+constexpr int WB_STAGE = 8;  // staged windows per row
+template <bool MULTI>
+__global__ void __launch_bounds__(128) k_build_lists_warp(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+                                                          const uint32_t* __restrict__ cs_all,
+                                                          const double* __restrict__ hmax_all,
+                                                          const int* __restrict__ d_real,
+                                                          const uint32_t* __restrict__ real_idx, NList L) {
+  __shared__ uint2 stage[WB_WARPS][WB_STAGE][32];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * WB_WARPS + wid;
+  if (r >= *d_real) return;  // whole warps leave together
+  const int i = (int)real_idx[r];
+  const int m = geo.member(A, i);
+  const Geo& g = geo.of(m);
+  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
+  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
+  const int b = A.bkt[i];
+  int bi[3];
+  bucket_coords<3>(g, b, bi);
+  float xs[3];
+  Pos<3, float>::load(A, W, i, xs);
+  const double hi_d = A.h[i];
+  const float hi = float(hi_d);
+  const float supp = float(o.cutoff2) * hi;
+  const float Lb = float(o.list_factor * W.hlist[i]);
+  const float kmarg2 = (float)(o.ksupport * (1.0 + 4e-6));
+  const float kA = kmarg2 * 0.5f * hi, kB = kmarg2 * 0.5f, kC = kmarg2 * hi;
+  const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
+  const float delT = float(g.del);
+  const float xrf[3] = {W.xr[i], W.yr[i], W.zr[i]};
+  int lo[3], up[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) cell_range(g, a, bi[a], xrf[a], R, lo[a], up[a]);
+  const int ny = up[1] - lo[1] + 1;
+  const int nrows = (ny > 0 && up[0] >= lo[0]) ? max(0, up[2] - lo[2] + 1) * ny : 0;
+  uint2* out = L.e + (size_t)i * LCAP;
+  uint2* st = &stage[wid][0][lane];  // this lane's slots, 32 apart
+  int cnt = 0;
+  bool over = false;
+  for (int r0 = 0; r0 < nrows; r0 += 32) {
+    const int row = r0 + lane;
+    int nw = 0;
+    if (row < nrows) {
+      const int cz = lo[2] + row / ny, cy = lo[1] + row % ny;
+      const int bz = cz / g.s, by = cy / g.s;
+      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      int cx = lo[0];
+      while (cx <= up[0]) {
+        const int bx = cx / g.s;
+        const int e = min(up[0], bx * g.s + g.s - 1);
+        const int code = (bx - bi[0] + 1) | (by - bi[1] + 1) << 2 | (bz - bi[2] + 1) << 4;
+        const uint32_t j0 = cs[rowbase + cx], j1 = cs[rowbase + e + 1];
+        bool own;
+        float ox, oy, oz;
+        decode_offsets<float>(delT, code, own, ox, oy, oz);
+        const float xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
+        const float Ti = own ? supp : fminf(Lb, supp);
+        for (uint32_t wb = j0; wb < j1; wb += 32) {
+          const uint32_t mask = window_mask(K, wb, (int)min(32u, j1 - wb), xsh, Ti, kA, kB, kC);
+          if (mask) {
+            if (nw < WB_STAGE) st[32 * nw] = make_uint2(wb | ((uint32_t)code << 26), mask);
+            nw++;
+          }
+        }
+        cx = e + 1;
+      }
+    }
+    if (__any_sync(0xffffffffu, nw > WB_STAGE)) {
+      over = true;
+      break;
+    }
+    int inc = nw;  // inclusive scan of the lanes' window counts
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    const int first = cnt + inc - nw;
+    for (int k = 0; k < nw; k++)
+      if (first + k < LCAP) list_store(out + first + k, st[32 * k]);
+    cnt += __shfl_sync(0xffffffffu, inc, 31);
+  }
+  if (lane == 0) L.cnt[i] = (over || cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
 }
 
 // the fused listed pair of each sweep (mixed Gaussian path)
@@ -967,8 +1076,11 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
     bool own;
     T ox, oy, oz;
     // listed entries get i's position shifted into the window's bucket
-    decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
-    ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
+    auto shift = [&](int code) {
+      decode_offsets<T>(delT, code, own, ox, oy, oz);
+      ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
+    };
+    shift((int)(en.x >> 26));
     // mixed Gaussian path: each listed candidate in one branch-free piece
     // (its records loaded together, zero outside the support)
     bool fused = false;
@@ -984,8 +1096,7 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
           en = list_load(ent + q);
         }
         mask = en.y;
-        decode_offsets<T>(delT, (int)(en.x >> 26), own, ox, oy, oz);
-        ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
+        shift((int)(en.x >> 26));
       }
       const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
       mask &= mask - 1;
@@ -1115,19 +1226,19 @@ __global__ void __launch_bounds__(128, SweepMinBlocksW<SW>::v)
   } else if (c > 0) {
     uint32_t* q = S.q[wid];
     float4* sh = S.sh[wid];
-    if (lane < 27) {
+    if (lane < 27) {  // lane = 9 kz + 3 ky + kx, code kx | ky << 2 | kz << 4
       bool own;
       T ox, oy, oz;
-      decode_offsets<T>(T(g.del), lane, own, ox, oy, oz);
+      decode_offsets<T>(T(g.del), lane % 3 | (lane / 3 % 3) << 2 | (lane / 9) << 4, own, ox, oy, oz);
       sh[lane] = make_float4(s.xpos()[0] + ox, s.xpos()[1] + oy, s.xpos()[2] + oz, 0.f);
     }
     __syncwarp();
     auto pair = [&](uint32_t e) {
       const uint32_t j = e & NL_JMASK;
       const int code = (int)(e >> 26);
-      const float4 p = sh[code];
+      const float4 p = sh[(code & 3) + 3 * ((code >> 2) & 3) + 9 * (code >> 4)];
       T dx[3], hj;
-      if (s.template filter<true>(j, code == 13, p.x, p.y, p.z, dx, hj)) s.math(j, dx, hj);
+      if (s.template filter<true>(j, code == OWN_CODE, p.x, p.y, p.z, dx, hj)) s.math(j, dx, hj);
     };
     const uint2* ent = L.e + (size_t)i * LCAP;
     int cnt = 0;  // queued candidates (the same in every lane)
