@@ -33,10 +33,7 @@ using namespace plume;
 namespace {
 
 constexpr int NTHREADS = 128;
-static_assert(NTHREADS == 32 * WP_WARPS && WP_WARPS == WB_WARPS, "warp kernels: 4 warps per block");
-#ifndef PLUME_BUILD_WARP
-#define PLUME_BUILD_WARP 0  // default builder of the FP32 lists: 1 k_build_lists_warp, 0 k_build_lists
-#endif
+static_assert(NTHREADS == 32 * WP_WARPS, "warp kernels: 4 warps per block");
 // phases of plume_phase_times: 0 search, 1 adaptive, 2 hmax + lists, 3 momentum,
 // 4 commit_mom, 5 density, 6 commit_dens, 7 velocity, 8 position, 9 dt,
 // 10 total, 11 the momentum pair-sweep kernel alone (part of 3), 12 inlet +
@@ -1187,7 +1184,6 @@ struct plume_ctx {
   // default per precision, PLUME_SWEEP=warp|thread overrides
   bool sweep_warp = false;
   bool list_warp = false;  // mixed list sweeps: one warp per particle (k_sweep3_wl), opt-in
-  bool build_warp = PLUME_BUILD_WARP;  // mixed lists built by k_build_lists_warp (PLUME_LIST_BUILD)
   uint32_t *keys = nullptr, *perm = nullptr, *cs = nullptr;
   uint32_t ncells = 0;
   int keybits = 1;
@@ -1516,12 +1512,8 @@ static void launch_sweeps(plume_ctx* ctx, bool adaptive_now) {
         k_pack_pos<<<nb, NTHREADS, 0, st>>>(ctx->A, ctx->K, ctx->W, ctx->d_count);
         ctx->launches++;
       }
-      if (mixed && ctx->build_warp)  // one warp per particle, lanes over its cell rows
-        k_build_lists_warp<MULTI><<<nbw, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
-                                                            ctx->d_real, ctx->real_idx, ctx->L);
-      else
-        k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
-                                                         ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
+      k_build_lists<T, MULTI><<<nb, NTHREADS, 0, st>>>(ctx->o, gs, ctx->A, ctx->W, ctx->K, ctx->cs, ctx->h27,
+                                                       ctx->d_real, ctx->real_idx, ctx->ts, ctx->L);
       ctx->launches++;
       if (rec) {
         dcopy(rec->L.e, ctx->L.e, sizeof(uint2) * (size_t)LCAP * n, st);
@@ -1873,10 +1865,6 @@ static int create_ctx(const PlumeOptions* opts, const PlumeGrid* grids, int nmem
     if (!strcmp(sw, "thread")) { ctx->sweep_warp = false; ctx->use_lists = false; }
     if (!strcmp(sw, "list")) { ctx->sweep_warp = false; ctx->use_lists = true; }
     if (!strcmp(sw, "list_warp")) { ctx->sweep_warp = false; ctx->use_lists = true; ctx->list_warp = true; }
-  }
-  if (const char* lb = getenv("PLUME_LIST_BUILD")) {  // "warp" or "thread": who builds the FP32 lists
-    if (!strcmp(lb, "warp")) ctx->build_warp = true;
-    if (!strcmp(lb, "thread")) ctx->build_warp = false;
   }
   if (opt->dim == 3 && ctx->use_lists && capacity > (size_t)NL_JMASK) {
     g_create_error = "capacity above the neighbour-list index range (2^26)";

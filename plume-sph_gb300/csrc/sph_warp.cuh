@@ -152,8 +152,8 @@ struct JPos<double> {
 // list sweeps that load the next window's list entry one window ahead
 // (S::kListAhead): on the 134^3 plume at h ~ 1.5 dx the momentum sweep 13.44
 // -> 12.87 ms and the LANS filter 8.02 -> 7.72 ms, while the density sweep
-// (64 registers, no spare one) went 7.87 -> 8.08 ms and keeps the plain load.
-// 0 turns it off everywhere.
+// (64 registers, no spare one) went 7.35 -> 7.79 ms and keeps the plain
+// load.  0 turns it off everywhere.
 #ifndef PLUME_LIST_AHEAD
 #define PLUME_LIST_AHEAD 1
 #endif
@@ -439,10 +439,7 @@ struct WDens {
   __device__ __forceinline__ void flush() {
     rho1.flush(); rho2.flush(); wnorm_e.flush(); engr.flush();
   }
-#ifndef PLUME_DENS_AHEAD
-#define PLUME_DENS_AHEAD 0
-#endif
-  static constexpr bool kListAhead = PLUME_DENS_AHEAD;  // the list walk's entry look-ahead
+  static constexpr bool kListAhead = false;  // the list walk's entry look-ahead
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
                                         double* xi, int* bi, double& R) {
@@ -935,103 +932,6 @@ __global__ void __launch_bounds__(128) k_build_lists(Opt o, Geos<MULTI> geo, Dev
     }
   });
   L.cnt[i] = (cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
-}
-
-// FP32 list build with one warp per particle.  The rows (cz, cy) of the
-// particle's cell box are dealt to the lanes 32 at a time; a lane tests the
-// candidates of its row's segments (window_mask, the tests of
-// k_build_lists) and stages the row's non-empty windows in shared memory;
-// an exclusive warp scan of the lanes' window counts places them, so the
-// windows reach the list in the walk's order (row, segment, window) and the
-// list is the one k_build_lists writes.  The rows of a box hold similar
-// numbers of candidates, so a warp's lanes stay busy together, where with
-// one thread per particle the lanes walk different numbers of segments.  A
-// row with more than WB_STAGE non-empty windows marks the particle
-// NL_OVERFLOW (its sweeps walk its rows instead).
-constexpr int WB_WARPS = 4;  // warps per block of 128 threads
-constexpr int WB_STAGE = 8;  // staged windows per row
-template <bool MULTI>
-__global__ void __launch_bounds__(128) k_build_lists_warp(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
-                                                          const uint32_t* __restrict__ cs_all,
-                                                          const double* __restrict__ hmax_all,
-                                                          const int* __restrict__ d_real,
-                                                          const uint32_t* __restrict__ real_idx, NList L) {
-  __shared__ uint2 stage[WB_WARPS][WB_STAGE][32];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * WB_WARPS + wid;
-  if (r >= *d_real) return;  // whole warps leave together
-  const int i = (int)real_idx[r];
-  const int m = geo.member(A, i);
-  const Geo& g = geo.of(m);
-  const uint32_t* cs = MULTI ? cs_all + g.cell_base : cs_all;
-  const double* hmax = MULTI ? hmax_all + g.bucket_base : hmax_all;
-  const int b = A.bkt[i];
-  int bi[3];
-  bucket_coords<3>(g, b, bi);
-  float xs[3];
-  Pos<3, float>::load(A, W, i, xs);
-  const double hi_d = A.h[i];
-  const float hi = float(hi_d);
-  const float supp = float(o.cutoff2) * hi;
-  const float Lb = float(o.list_factor * W.hlist[i]);
-  const float kmarg2 = (float)(o.ksupport * (1.0 + 4e-6));
-  const float kA = kmarg2 * 0.5f * hi, kB = kmarg2 * 0.5f, kC = kmarg2 * hi;
-  const double R = fmin(o.cutoff2 * hi_d, o.ksupport * fmax(0.5 * (hi_d + hmax[b]), hi_d)) * (1.0 + 1e-10);
-  const float delT = float(g.del);
-  const float xrf[3] = {W.xr[i], W.yr[i], W.zr[i]};
-  int lo[3], up[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) cell_range(g, a, bi[a], xrf[a], R, lo[a], up[a]);
-  const int ny = up[1] - lo[1] + 1;
-  const int nrows = (ny > 0 && up[0] >= lo[0]) ? max(0, up[2] - lo[2] + 1) * ny : 0;
-  uint2* out = L.e + (size_t)i * LCAP;
-  uint2* st = &stage[wid][0][lane];  // this lane's slots, 32 apart
-  int cnt = 0;
-  bool over = false;
-  for (int r0 = 0; r0 < nrows; r0 += 32) {
-    const int row = r0 + lane;
-    int nw = 0;
-    if (row < nrows) {
-      const int cz = lo[2] + row / ny, cy = lo[1] + row % ny;
-      const int bz = cz / g.s, by = cy / g.s;
-      const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
-      int cx = lo[0];
-      while (cx <= up[0]) {
-        const int bx = cx / g.s;
-        const int e = min(up[0], bx * g.s + g.s - 1);
-        const int code = (bx - bi[0] + 1) | (by - bi[1] + 1) << 2 | (bz - bi[2] + 1) << 4;
-        const uint32_t j0 = cs[rowbase + cx], j1 = cs[rowbase + e + 1];
-        bool own;
-        float ox, oy, oz;
-        decode_offsets<float>(delT, code, own, ox, oy, oz);
-        const float xsh[3] = {xs[0] + ox, xs[1] + oy, xs[2] + oz};
-        const float Ti = own ? supp : fminf(Lb, supp);
-        for (uint32_t wb = j0; wb < j1; wb += 32) {
-          const uint32_t mask = window_mask(K, wb, (int)min(32u, j1 - wb), xsh, Ti, kA, kB, kC);
-          if (mask) {
-            if (nw < WB_STAGE) st[32 * nw] = make_uint2(wb | ((uint32_t)code << 26), mask);
-            nw++;
-          }
-        }
-        cx = e + 1;
-      }
-    }
-    if (__any_sync(0xffffffffu, nw > WB_STAGE)) {
-      over = true;
-      break;
-    }
-    int inc = nw;  // inclusive scan of the lanes' window counts
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, inc, d);
-      if (lane >= d) inc += t;
-    }
-    const int first = cnt + inc - nw;
-    for (int k = 0; k < nw; k++)
-      if (first + k < LCAP) list_store(out + first + k, st[32 * k]);
-    cnt += __shfl_sync(0xffffffffu, inc, 31);
-  }
-  if (lane == 0) L.cnt[i] = (over || cnt > LCAP) ? NL_OVERFLOW : (uint16_t)cnt;
 }
 
 // the fused listed pair of each sweep (mixed Gaussian path)

@@ -131,32 +131,6 @@ def test_3d_mixed_precision_density_error():
     assert l1 <= 1e-4, l1
 
 
-def test_mixed_list_builders_give_identical_steps(monkeypatch):
-    """The FP32 neighbour lists built with one thread per particle
-    (k_build_lists) and with one warp per particle, its lanes over the
-    particle's cell rows (k_build_lists_warp), are the same windows in the
-    same order: the sweeps sum in list order, so three mixed steps across
-    the adaptive-h pass of step 50 (h ~ dx -> 1.5 dx) with the wall boundary
-    and the inlet end in the same state, bit for bit."""
-    base = cases.plume_small(seed=4, precision=PREC_MIXED, subcells=5)
-    base.step0 = 48
-    images = cases.wall_images(base)
-    inlet = cases.inlet(base)
-    out = {}
-    for builder in ("thread", "warp"):
-        monkeypatch.setenv("PLUME_LIST_BUILD", builder)
-        s = Solver(base)
-        s.set_wall_images(*images)
-        s.set_inlet(inlet)
-        s.steps(3)
-        out[builder] = s.download().sorted_by_key()
-        s.close()
-    a, b = out["thread"], out["warp"]
-    assert a.n == b.n
-    for f in DOUBLE_FIELDS + BYTE_FIELDS + ("key",):
-        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
-
-
 def _run_to_end(s, t_end, chunk=100):
     """steps until TimeProps::ifend (time >= max_time), like the 1D main loop"""
     t, step, _ = s.time()
