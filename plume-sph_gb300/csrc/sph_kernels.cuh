@@ -38,6 +38,9 @@ __device__ __forceinline__ void cell_range(const Geo& g, int a, int b, float xr,
   hi = min(h, min((b + 2) * g.s - 1, g.G[a] - 1));
 }
 
+#ifndef PLUME_SEG_DIV
+#define PLUME_SEG_DIV 0  // 1: bucket indices by division per row and segment
+#endif
 // Offsets (i's bucket - segment's bucket) * del are passed for the
 // bucket-relative FP32 coordinates of the mixed path; the FP64 path works on
 // absolute coordinates and gets zero offsets.
@@ -62,6 +65,7 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
   }
   constexpr bool REL = sizeof(T) == 4;
   const T delT = T(g.del);
+#if PLUME_SEG_DIV
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
     int bz = cz / g.s;
     T oz = REL ? T(bi[2] - bz) * delT : T(0);
@@ -79,6 +83,30 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
       }
     }
   }
+#else
+  // bucket indices carried along the loops (one division per axis): a
+  // segment ends at its bucket's last cell, so the next one starts a bucket on
+  const int bx0 = lo[0] / g.s, by0 = lo[1] / g.s;
+  int bz = lo[2] / g.s, rz = lo[2] - bz * g.s;
+  for (int cz = lo[2]; cz <= hi[2]; cz++) {
+    T oz = REL ? T(bi[2] - bz) * delT : T(0);
+    int by = by0, ry = lo[1] - by0 * g.s;
+    for (int cy = lo[1]; cy <= hi[1]; cy++) {
+      T oy = REL ? T(bi[1] - by) * delT : T(0);
+      size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
+      int cx = lo[0], bx = bx0;
+      while (cx <= hi[0]) {
+        int e = min(hi[0], bx * g.s + g.s - 1);
+        bool own = (bx == bi[0]) && (by == bi[1]) && (bz == bi[2]);
+        f(cs[rowbase + cx], cs[rowbase + e + 1], own, REL ? T(bi[0] - bx) * delT : T(0), oy, oz);
+        cx = e + 1;
+        bx++;
+      }
+      if (++ry == g.s) { ry = 0; by++; }
+    }
+    if (++rz == g.s) { rz = 0; bz++; }
+  }
+#endif
   }
 }
 

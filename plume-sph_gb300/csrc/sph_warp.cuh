@@ -168,6 +168,14 @@ struct JPos<float> {
 };
 
 // ------------------------------------------------------------ momentum
+// FP32 momentum record and pair: 1 stores h, rho, c, cp halved and m V (the
+// same pair values with fewer operations), 2 also forms |s|^2 as |dx|^2/h^2
+// and folds 1/Pr into the heat term's constant (rounding differs)
+#ifndef PLUME_MOM_FOLD
+#define PLUME_MOM_FOLD 1
+#endif
+constexpr bool kMomHalf = PLUME_MOM_FOLD >= 1;
+constexpr bool kMomFold = PLUME_MOM_FOLD >= 2;
 template <typename T>
 struct WMom {
   const Dev& A;
@@ -252,6 +260,7 @@ struct WMom {
       if (!own && !in_box<3, T>(dx, Lb)) return false;
       if (!in_box<3, T>(dx, supp)) return false;
     }
+    if constexpr (sizeof(T) == 4 && kMomHalf) hj *= 2.0f;  // the record holds h_j / 2
     const T ks = ks_half * (hi + fabs(hj));
     return in_box<3, T>(dx, ks);
   }
@@ -266,21 +275,25 @@ struct WMom {
   __device__ __forceinline__ void listed(uint32_t j, float ox, float oy, float oz) {
     const float4 pj = K.P[j], qj = K.Q[j], rj = K.R[j], sj = K.S[j];
     const float d0 = ox - pj.x, d1 = oy - pj.y, d2 = oz - pj.z;
-    const float h = 0.5f * (hi + pj.w);
+    // kMomHalf: the record holds h_j/2, rho_j/2, c_j/2, cp_j/2 and m_j V_j,
+    // so each mean is one FMA (the same values: halving is exact)
+    const float h = kMomHalf ? fmaf(0.5f, hi, pj.w) : 0.5f * (hi + pj.w);
     const float ih = rcp<float>(h);
     const float s0 = d0 * ih, s1 = d1 * ih, s2 = d2 * ih;
     const float dist_sq = d0 * d0 + d1 * d1 + d2 * d2;
     const float v0 = veli[0] - rj.w, v1 = veli[1] - sj.x, v2 = veli[2] - sj.y;
-    const float sndspdab = 0.5f * (ci + rj.x);
+    const float sndspdab = kMomHalf ? fmaf(0.5f, ci, rj.x) : 0.5f * (ci + rj.x);
     const float vrab = d0 * v0 + d1 * v1 + d2 * v2;
     const float miuab = h * vrab * rcp<float>(dist_sq + ata * h * h);
-    float vis = (vrab < 0.0f) ? (beta * miuab - alpha * sndspdab) * miuab * rcp<float>(0.5f * (rhoi + qj.y)) : 0.0f;
+    const float rhoab = kMomHalf ? fmaf(0.5f, rhoi, qj.y) : 0.5f * (rhoi + qj.y);
+    float vis = (vrab < 0.0f) ? (beta * miuab - alpha * sndspdab) * miuab * rcp<float>(rhoab) : 0.0f;
     const float dotv = v0 * v0 + v1 * v1 + v2 * v2;
     if (lans) vis -= float(EPS_HALF) * dotv * qj.z;
     const float mpvsqij = qj.x * (qj.w + pvsqi + vis);
     const bool in = (j != i) && fabsf(s0) <= 3.0f && fabsf(s1) <= 3.0f && fabsf(s2) <= 3.0f;
     const float ih2 = ih * ih;
-    const float f = in ? KF * (ih2 * ih2) * __expf(-(s0 * s0 + s1 * s1 + s2 * s2)) : 0.0f;
+    const float qq = kMomFold ? dist_sq * ih2 : s0 * s0 + s1 * s1 + s2 * s2;
+    const float f = in ? KF * (ih2 * ih2) * __expf(-qq) : 0.0f;
     const float gm = mpvsqij * f;
     rv[0].sub(gm * s0);
     rv[1].sub(gm * s1);
@@ -289,11 +302,14 @@ struct WMom {
     if (lans) {
       // m_j V_j V_i k_ij (T_i - T_j) f/h with k_ij = 10 eps Cp_ij |dx|^2
       // |v_ij|^2 / (Pr dotvr h c_ab)
-      const float Cp_ij = 0.5f * (rj.z + Cp_i);
+      const float Cp_ij = kMomHalf ? fmaf(0.5f, Cp_i, rj.z) : 0.5f * (rj.z + Cp_i);
       const float dotvr = fabsf(v0 * d0) + fabsf(v1 * d1) + fabsf(v2 * d2);
-      const float kij = 10.0f * float(EPS_HALF) * Cp_ij * dist_sq * dotv *
-                        rcp<float>(float(PRANDTL) * dotvr * h * sndspdab);
-      heat_tran = (dotvr != 0.0f) ? qj.x * qj.z * Vi * kij * (tempi - rj.y) * (f * ih) : 0.0f;
+      const float kij = kMomFold ? float(10.0 * EPS_HALF / PRANDTL) * Cp_ij * dist_sq * dotv *
+                                       rcp<float>(dotvr * h * sndspdab)
+                                 : 10.0f * float(EPS_HALF) * Cp_ij * dist_sq * dotv *
+                                       rcp<float>(float(PRANDTL) * dotvr * h * sndspdab);
+      const float mVj = kMomHalf ? sj.z : qj.x * qj.z;
+      heat_tran = (dotvr != 0.0f) ? mVj * Vi * kij * (tempi - rj.y) * (f * ih) : 0.0f;
     }
     re.add(0.5f * gm * ih * vrab + heat_tran);
   }
@@ -404,25 +420,29 @@ template <>
 __device__ __forceinline__ void WMom<float>::load_j(uint32_t j, float& mj, float& rhoj, float& Vj, float& pVVj,
                                                     float& cj, float& Tj, float& cpj, float* vj) const {
   const float4 q = K.Q[j], r = K.R[j], s = K.S[j];
-  mj = q.x; rhoj = q.y; Vj = q.z; pVVj = q.w;
-  cj = r.x; Tj = r.y; cpj = r.z; vj[0] = r.w;
+  const float u = kMomHalf ? 2.0f : 1.0f;  // halved means in the record
+  mj = q.x; rhoj = u * q.y; Vj = q.z; pVVj = q.w;
+  cj = u * r.x; Tj = r.y; cpj = u * r.z; vj[0] = r.w;
   vj[1] = s.x; vj[2] = s.y;
 }
 
 // momentum record: P (xr,yr,zr,h), Q (m, rho, 1/rho, p/rho^2), R (c,T,cp,vx),
-// S (vy,vz); the quotients are formed in FP64 once per particle
+// S (vy,vz, m/rho); with kMomHalf h, rho, c and cp are stored halved (the
+// pair forms their means with one FMA)
 __global__ void k_pack_mom(Dev A, Packed K, Work W, int lans, const int* __restrict__ d_count) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= *d_count) return;
   // fields narrowed on the integer pipe, V and p V^2 formed in FP32
   const float rho = f32_rz(A.rho[j]), V = 1.0f / rho;
-  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], f32_rz(A.h[j]));
-  K.Q[j] = make_float4(f32_rz(A.mass[j]), rho, V, f32_rz(A.p[j]) * V * V);
+  const float u = kMomHalf ? 0.5f : 1.0f;
+  const float m = f32_rz(A.mass[j]);
+  K.P[j] = make_float4(W.xr[j], W.yr[j], W.zr[j], u * f32_rz(A.h[j]));
+  K.Q[j] = make_float4(m, u * rho, V, f32_rz(A.p[j]) * V * V);
   const double vx = lans ? A.vsx[j] : A.vx[j];
   const double vy = lans ? A.vsy[j] : A.vy[j];
   const double vz = lans ? A.vsz[j] : A.vz[j];
-  K.R[j] = make_float4(f32_rz(A.c[j]), f32_rz(A.T[j]), f32_rz(A.cp[j]), f32_rz(vx));
-  K.S[j] = make_float4(f32_rz(vy), f32_rz(vz), 0.f, 0.f);
+  K.R[j] = make_float4(u * f32_rz(A.c[j]), f32_rz(A.T[j]), u * f32_rz(A.cp[j]), f32_rz(vx));
+  K.S[j] = make_float4(f32_rz(vy), f32_rz(vz), m * V, 0.f);
 }
 
 // ------------------------------------------------------------ density
@@ -812,20 +832,25 @@ __device__ __forceinline__ void for_segments_code(const Geo& g, const uint32_t* 
   int lo[3], hi[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) cell_range(g, a, bi[a], xr[a], R, lo[a], hi[a]);
+  // bucket indices carried along the loops (one division per axis): a
+  // segment ends at its bucket's last cell, so the next one starts a bucket on
+  const int bx0 = lo[0] / g.s, by0 = lo[1] / g.s;
+  int bz = lo[2] / g.s, rz = lo[2] - bz * g.s;
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
-    const int bz = cz / g.s;
+    int by = by0, ry = lo[1] - by0 * g.s;
     for (int cy = lo[1]; cy <= hi[1]; cy++) {
-      const int by = cy / g.s;
       const size_t rowbase = ((size_t)cz * g.G[1] + cy) * (size_t)g.G[0];
-      int cx = lo[0];
+      int cx = lo[0], bx = bx0;
       while (cx <= hi[0]) {
-        const int bx = cx / g.s;
         const int e = min(hi[0], bx * g.s + g.s - 1);
         const int code = (bx - bi[0] + 1) | (by - bi[1] + 1) << 2 | (bz - bi[2] + 1) << 4;
         f(cs[rowbase + cx], cs[rowbase + e + 1], code);
         cx = e + 1;
+        bx++;
       }
+      if (++ry == g.s) { ry = 0; by++; }
     }
+    if (++rz == g.s) { rz = 0; bz++; }
   }
 }
 
