@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 namespace plume {
 
 constexpr double T1_INV_SQRT_PI = 0.564189583547756;  // sph_lib.cc:206

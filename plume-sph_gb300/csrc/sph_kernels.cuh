@@ -38,13 +38,12 @@ __device__ __forceinline__ void cell_range(const Geo& g, int a, int b, float xr,
   hi = min(h, min((b + 2) * g.s - 1, g.G[a] - 1));
 }
 
-#ifndef PLUME_SEG_DIV
-#define PLUME_SEG_DIV 0  // 1: bucket indices by division per row and segment
-#endif
 // Offsets (i's bucket - segment's bucket) * del are passed for the
 // bucket-relative FP32 coordinates of the mixed path; the FP64 path works on
-// absolute coordinates and gets zero offsets.
-template <int D, typename T, class F>
+// absolute coordinates and gets zero offsets.  CARRY: the segments' bucket
+// indices are carried along the loops instead of divided out per row and
+// segment (the same segments).
+template <int D, typename T, bool CARRY = false, class F>
 __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __restrict__ cs, const double* xi,
                                              const int* bi, double R, F&& f) {
   if constexpr (D == 1) {
@@ -65,7 +64,7 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
   }
   constexpr bool REL = sizeof(T) == 4;
   const T delT = T(g.del);
-#if PLUME_SEG_DIV
+  if constexpr (!CARRY) {
   for (int cz = lo[2]; cz <= hi[2]; cz++) {
     int bz = cz / g.s;
     T oz = REL ? T(bi[2] - bz) * delT : T(0);
@@ -83,7 +82,7 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
       }
     }
   }
-#else
+  } else {
   // bucket indices carried along the loops (one division per axis): a
   // segment ends at its bucket's last cell, so the next one starts a bucket on
   const int bx0 = lo[0] / g.s, by0 = lo[1] / g.s;
@@ -106,7 +105,7 @@ __device__ __forceinline__ void for_segments(const Geo& g, const uint32_t* __res
     }
     if (++rz == g.s) { rz = 0; bz++; }
   }
-#endif
+  }
   }
 }
 
