@@ -10,10 +10,11 @@ need_neigh particles x steps / seconds.
 
   value     mixed-precision path, particles resident in HBM, CUDA events
             on the library stream over exactly K steps
-  e2e       the same steps through the C ABI with host buffers: every step
+  e2e       K steps through the C ABI with host buffers: every step
             uploads the particle table from pinned host memory, steps, and
             downloads it (the drop-in use by a host that keeps its own
-            particle table)
+            particle table); its window is centred on the next adaptive-h
+            pass, so it holds passes at the rate of the timed window
   fp64      the FP64 path on the same workload (for the FP64 / mixed ratio)
   roofline  the momentum/energy sweep (dominant kernel)
   cpu_baseline  the CPU oracle (restatement of the reference path) on a
@@ -30,8 +31,10 @@ spends 97 % of its steps there.  The run therefore steps untimed to just
 before step 100 - K/2 (the plume develops, the inlet injects, h adapts at
 step 50), warms up, and times K steps centred on the second adaptive pass:
 the window holds every phase of the reference loop (dt, search, wall
-boundary, adaptive h once, momentum/energy, density, LANS filter, position,
-inlet) at the smoothing lengths of the bulk of the run.
+boundary, adaptive h, momentum/energy, density, LANS filter, position,
+inlet) at the smoothing lengths of the bulk of the run.  With the default
+K = 50 (steps 75-124) it holds one adaptive-h pass per 50 steps, the rate of
+a real run; a shorter K still holds one pass (a heavier share).
 
 `--impl reference` times the reference's CPU path on the host cores: the
 oracle port (OpenMP over all cores) on a bounded sample of the same state,
@@ -478,8 +481,8 @@ def run_reference(args, dist, rank, ws):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -549,6 +552,7 @@ def main():
     inlet = None if args.no_inlet else cases.inlet(case)
     prep, first = timed_window(args.warmup, args.steps)
     last = first + args.steps - 1
+    n_passes = last // SML_INTERVAL - (first - 1) // SML_INTERVAL  # adaptive-h passes in the window
 
     def solver(c):
         s = Solver(c)
@@ -609,7 +613,12 @@ def main():
     # e2e: through the C ABI with pinned host buffers, every step
     # upload -> step -> download
     from plume_gpu.abi import BYTE_FIELDS, DOUBLE_FIELDS
-    e2e_steps = max(2, min(args.steps, 5))
+    # the e2e window: K steps centred on the next adaptive-h pass (untimed
+    # steps up to it), so that it holds passes at the timed window's rate
+    e2e_steps = max(2, args.steps)
+    next_pass = (last // SML_INTERVAL + 1) * SML_INTERVAL
+    sol.steps(max(0, next_pass - e2e_steps // 2 - (last + 1)))
+    e2e_first = sol.time()[1] + 1
     snap = sol.download()
     grow = 0 if inlet is None else 4 * len(inlet["col_vel"]) * (e2e_steps + 1)
     host = pinned_particles(snap, extra=grow)  # pinned copy of the whole particle table
@@ -733,12 +742,14 @@ def main():
                        "timed_steps": [first, last],
                        "window": f"steps {first}-{last} after {prep + args.warmup} untimed steps from the "
                                  f"lattice (h = dx until the adaptive-h pass of step 50); the window "
-                                 f"holds the adaptive-h pass of step {2 * SML_INTERVAL}"},
+                                 f"holds {n_passes} adaptive-h pass(es), one per "
+                                 f"{args.steps / max(1, n_passes):.0f} steps (a run: one per {SML_INTERVAL})"},
             "gpu_launches": launches,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
             "clocks": clk.summary(),
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                    "timed_steps": [e2e_first, e2e_first + e2e_steps - 1]},
             "fp64": fp64,
             "mixed_over_fp64": (value / fp64["value"]) if fp64 else None,
             "l1_density_vs_fp64": accuracy,
