@@ -75,10 +75,10 @@ MOM_BYTES_WRITE = 4 * 8
 # LANS and heat terms): 80 FLOP + 2 SFU
 MOM_FLOP_PER_PAIR = 80
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the
-# momentum sweep on the small plume with 5^3 cells per bucket at step 99
-# (h ~ 1.5 dx, the regime of the timed window): 478.8 MB + 21.3 MB for
+# momentum sweep on the small plume with 4^3 cells per bucket at step 99
+# (h ~ 1.5 dx, the regime of the timed window): 397.9 MB + 16.8 MB for
 # 778,952 particles
-MOM_DRAM_BYTES_PER_PARTICLE = 500.03e6 / 778952
+MOM_DRAM_BYTES_PER_PARTICLE = 414.7e6 / 778952
 
 
 def load_peaks():
