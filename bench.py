@@ -77,7 +77,8 @@ MOM_FLOP_PER_PAIR = 80
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the
 # momentum sweep on the small plume with 4^3 cells per bucket at step 99
 # (h ~ 1.5 dx, the regime of the timed window): 397.9 MB + 16.8 MB for
-# 778,952 particles
+# 778,952 particles, most of it the neighbour lists (8 B per window, read
+# once per sweep), which the algorithmic bytes above do not count
 MOM_DRAM_BYTES_PER_PARTICLE = 414.7e6 / 778952
 
 
