@@ -124,6 +124,7 @@ struct AdjIn {
 struct VMom {
   WMom<double> f;
   static constexpr bool kListAhead = false;  // the list walk's plain entry loads
+  static constexpr bool kSkipDecode = false;
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
@@ -368,6 +369,7 @@ struct VMom {
 struct VDens {
   WDens<double> f;
   static constexpr bool kListAhead = false;  // the list walk's plain entry loads
+  static constexpr bool kSkipDecode = false;
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;
@@ -446,6 +448,7 @@ struct VDens {
 struct VVel {
   WVel<double> f;
   static constexpr bool kListAhead = false;  // the list walk's plain entry loads
+  static constexpr bool kSkipDecode = false;
   __device__ __forceinline__ const double* xpos() const { return f.xs; }
   const Adj& B;
   const AdjIn& in;

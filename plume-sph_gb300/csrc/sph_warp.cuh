@@ -191,6 +191,7 @@ struct WMom {
     rv[0].flush(); rv[1].flush(); rv[2].flush(); re.flush();
   }
   static constexpr bool kListAhead = true;  // the list walk's entry look-ahead
+  static constexpr bool kSkipDecode = false;  // the list walk keeps a repeated bucket's offsets
   __device__ WMom(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   // i-side set-up; returns false (with the status set) when i is skipped
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState* ts,
@@ -273,6 +274,14 @@ struct WMom {
   // i) contributes exactly zero through f = 0.  o[] is i's position shifted
   // into j's bucket.  W = pi^-3/2 ih^3 e^-|s|^2, f = -2 ih W.
   __device__ __forceinline__ void listed(uint32_t j, float ox, float oy, float oz) {
+    if (lans)
+      listed_l<true>(j, ox, oy, oz);
+    else
+      listed_l<false>(j, ox, oy, oz);
+  }
+  // LANS: the LANS terms (o.lans), a compile-time choice in the list loop
+  template <bool LANS>
+  __device__ __forceinline__ void listed_l(uint32_t j, float ox, float oy, float oz) {
     const float4 pj = K.P[j], qj = K.Q[j], rj = K.R[j], sj = K.S[j];
     const float d0 = ox - pj.x, d1 = oy - pj.y, d2 = oz - pj.z;
     // kMomHalf: the record holds h_j/2, rho_j/2, c_j/2, cp_j/2 and m_j V_j,
@@ -288,7 +297,7 @@ struct WMom {
     const float rhoab = kMomHalf ? fmaf(0.5f, rhoi, qj.y) : 0.5f * (rhoi + qj.y);
     float vis = (vrab < 0.0f) ? (beta * miuab - alpha * sndspdab) * miuab * rcp<float>(rhoab) : 0.0f;
     const float dotv = v0 * v0 + v1 * v1 + v2 * v2;
-    if (lans) vis -= float(EPS_HALF) * dotv * qj.z;
+    if constexpr (LANS) vis -= float(EPS_HALF) * dotv * qj.z;
     const float mpvsqij = qj.x * (qj.w + pvsqi + vis);
     const bool in = (j != i) && fabsf(s0) <= 3.0f && fabsf(s1) <= 3.0f && fabsf(s2) <= 3.0f;
     const float ih2 = ih * ih;
@@ -299,7 +308,7 @@ struct WMom {
     rv[1].sub(gm * s1);
     rv[2].sub(gm * s2);
     float heat_tran = 0.0f;
-    if (lans) {
+    if constexpr (LANS) {
       // m_j V_j V_i k_ij (T_i - T_j) f/h with k_ij = 10 eps Cp_ij |dx|^2
       // |v_ij|^2 / (Pr dotvr h c_ab)
       const float Cp_ij = kMomHalf ? fmaf(0.5f, Cp_i, rj.z) : 0.5f * (rj.z + Cp_i);
@@ -460,6 +469,7 @@ struct WDens {
     rho1.flush(); rho2.flush(); wnorm_e.flush(); engr.flush();
   }
   static constexpr bool kListAhead = false;  // the list walk's entry look-ahead
+  static constexpr bool kSkipDecode = false;  // the list walk keeps a repeated bucket's offsets
   __device__ WDens(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double* hmax, TimeState*,
                                         double* xi, int* bi, double& R) {
@@ -628,6 +638,7 @@ struct WVel {
     dv[0].flush(); dv[1].flush(); dv[2].flush(); wnorm.flush();
   }
   static constexpr bool kListAhead = true;  // the list walk's entry look-ahead
+  static constexpr bool kSkipDecode = true;  // the list walk keeps a repeated bucket's offsets
   __device__ WVel(const Dev& A_, const Packed& K_, const Opt& o_) : A(A_), K(K_), o(o_) {}
   double vi_d[3];
   __device__ __forceinline__ bool setup(int ii, const Geo& g, const Work& W, const double*, TimeState*,
@@ -965,11 +976,61 @@ __device__ __forceinline__ void listed_pair(WVel<float>& s, uint32_t j, float ox
   s.listed(j, ox, oy, oz);
 }
 
-// sweep over the lists (thread per particle, over the compacted need_neigh
-// indices); particles whose list overflowed walk their rows.  The window and
+// The stored windows of particle i (c of them), their set bits in order:
+// pair(j, own, ox, oy, oz) per candidate, o = i's position shifted into the
+// window's bucket.  The bit loop is flattened: every iteration hands each
+// thread one pair, so the threads of a warp stay converged while they have
+// pairs left.
+template <typename T, class S, class F>
+__device__ __forceinline__ void walk_windows(S& s, int i, const Geo& g, int c, const NList& L, F&& pair) {
+  const uint2* ent = L.e + (size_t)i * LCAP;
+  const T delT = T(g.del);
+  int q = 0;
+  // the next window's entry is loaded one window ahead, so that its load
+  // (mostly an L2 or DRAM access: the lists are read once per sweep) is
+  // in flight while the current window's pairs are summed
+  constexpr bool ahead = PLUME_LIST_AHEAD && S::kListAhead;
+  uint2 en = list_load(ent);
+  uint2 nx = ahead ? list_load(ent + (c > 1 ? 1 : 0)) : en;
+  uint32_t mask = en.y;
+  bool own;
+  T ox, oy, oz;
+  auto shift = [&](int code) {
+    decode_offsets<T>(delT, code, own, ox, oy, oz);
+    ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
+  };
+  int pcode = (int)(en.x >> 26);
+  shift(pcode);
+  while (true) {
+    if (mask == 0) {  // stored windows are never empty: one step suffices
+      if constexpr (sizeof(T) == 4) s.flush();  // one partial per window
+      if (++q >= c) break;
+      if (ahead) {
+        en = nx;
+        nx = list_load(ent + min(q + 1, c - 1));  // the last one again at the end
+      } else {
+        en = list_load(ent + q);
+      }
+      mask = en.y;
+      const int code = (int)(en.x >> 26);
+      if (!S::kSkipDecode || code != pcode) {  // windows of one bucket share their offsets
+        shift(code);
+        pcode = code;
+      }
+    }
+    const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
+    mask &= mask - 1;
+    pair(j, own, ox, oy, oz);
+  }
+}
+
 // Visits the candidates of particle i in the walk's order: the particle's
 // stored windows (set bits, in order), or the cell rows when its windows
-// overflowed; s.math(j, dx, hj) for every candidate s.filter passes.
+// overflowed.  The mixed Gaussian path takes each listed candidate in one
+// branch-free piece (its records loaded together, zero outside the
+// support), with the momentum sweep's LANS terms chosen once per particle,
+// outside the loop; otherwise s.math(j, dx, hj) for every candidate
+// s.filter passes.
 template <typename T, class S>
 __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint32_t* __restrict__ cs,
                                           const double* xi, const int* bi, double R, const NList& L) {
@@ -986,54 +1047,31 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
       }
       if constexpr (sizeof(T) == 4) s.flush();  // one partial per row segment
     });
-  } else if (c > 0) {
-    const uint2* ent = L.e + (size_t)i * LCAP;
-    const T delT = T(g.del);
-    int q = 0;
-    // the next window's entry is loaded one window ahead, so that its load
-    // (mostly an L2 or DRAM access: the lists are read once per sweep) is
-    // in flight while the current window's pairs are summed
-    constexpr bool ahead = PLUME_LIST_AHEAD && S::kListAhead;
-    uint2 en = list_load(ent);
-    uint2 nx = ahead ? list_load(ent + (c > 1 ? 1 : 0)) : en;
-    uint32_t mask = en.y;
-    bool own;
-    T ox, oy, oz;
-    // listed entries get i's position shifted into the window's bucket
-    auto shift = [&](int code) {
-      decode_offsets<T>(delT, code, own, ox, oy, oz);
-      ox += s.xpos()[0]; oy += s.xpos()[1]; oz += s.xpos()[2];
-    };
-    shift((int)(en.x >> 26));
-    // mixed Gaussian path: each listed candidate in one branch-free piece
-    // (its records loaded together, zero outside the support)
-    bool fused = false;
-    if constexpr (sizeof(T) == 4) fused = s.o.kernel != 1;
-    while (true) {
-      if (mask == 0) {  // stored windows are never empty: one step suffices
-        if constexpr (sizeof(T) == 4) s.flush();  // one partial per window
-        if (++q >= c) break;
-        if (ahead) {
-          en = nx;
-          nx = list_load(ent + min(q + 1, (int)c - 1));  // the last one again at the end
-        } else {
-          en = list_load(ent + q);
-        }
-        mask = en.y;
-        shift((int)(en.x >> 26));
+    return;
+  }
+  if (c == 0) return;
+  if constexpr (sizeof(T) == 4) {
+    if (s.o.kernel != 1) {
+      if constexpr (std::is_same<S, WMom<float>>::value) {
+        if (s.lans)
+          walk_windows<T>(s, i, g, c, L, [&](uint32_t j, bool, float ox, float oy, float oz) {
+            s.template listed_l<true>(j, ox, oy, oz);
+          });
+        else
+          walk_windows<T>(s, i, g, c, L, [&](uint32_t j, bool, float ox, float oy, float oz) {
+            s.template listed_l<false>(j, ox, oy, oz);
+          });
+      } else {
+        walk_windows<T>(s, i, g, c, L,
+                        [&](uint32_t j, bool, float ox, float oy, float oz) { listed_pair(s, j, ox, oy, oz); });
       }
-      const uint32_t j = (en.x & NL_JMASK) + (uint32_t)(__ffs(mask) - 1);
-      mask &= mask - 1;
-      if constexpr (sizeof(T) == 4) {
-        if (fused) {
-          listed_pair(s, j, ox, oy, oz);
-          continue;
-        }
-      }
-      T dx[3], hj;
-      if (s.template filter<true>(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
+      return;
     }
   }
+  walk_windows<T>(s, i, g, c, L, [&](uint32_t j, bool own, T ox, T oy, T oz) {
+    T dx[3], hj;
+    if (s.template filter<true>(j, own, ox, oy, oz, dx, hj)) s.math(j, dx, hj);
+  });
 }
 
 // bit loops are flattened so that every iteration hands each thread exactly
