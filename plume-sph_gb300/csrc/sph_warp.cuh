@@ -1074,32 +1074,34 @@ __device__ __forceinline__ void list_walk(S& s, int i, const Geo& g, const uint3
   });
 }
 
-// bit loops are flattened so that every iteration hands each thread exactly
-// one pair (threads of a warp stay converged while they have pairs left).
-// minimum resident blocks per SM of each list sweep (caps its registers;
-// measured on the 134^3 plume: momentum 6 blocks = 80 registers, 5.41 ms
-// against 7.08 ms uncapped at 102 registers and 8.01 ms at 64 with spills;
-// density and LANS filter 8 blocks = 64 registers, 8 % faster than 7)
+// minimum resident blocks per SM of each list sweep (caps its registers),
+// measured on the 134^3 plume at h ~ 1.5 dx (default window, 4^3 cells, ms
+// per step): momentum 7 blocks = 72 registers 9.64 (6 = 80 registers 10.07);
+// density 12 blocks = 40 registers 6.04 (8 = 64: 6.83, 10 = 48: 6.15);
+// LANS filter 10 blocks = 48 registers 6.02 (8 = 64: 6.46, 11 = 40: 6.36).
+// The spills the lower caps bring cost less than the latency the extra
+// warps hide.
 #ifndef PLUME_MINB_MOM
-#define PLUME_MINB_MOM 6
+#define PLUME_MINB_MOM 7
 #endif
 #ifndef PLUME_MINB_DENS
-#define PLUME_MINB_DENS 8
+#define PLUME_MINB_DENS 12
 #endif
 #ifndef PLUME_MINB_VEL
-#define PLUME_MINB_VEL 8
+#define PLUME_MINB_VEL 10
 #endif
-template <template <typename> class SW>
+// (the FP64 sweeps keep 6, 8 and 8 blocks: 80 and 64 registers)
+template <typename T, template <typename> class SW>
 struct SweepMinBlocks { static constexpr int v = 1; };
-template <>
-struct SweepMinBlocks<WMom> { static constexpr int v = PLUME_MINB_MOM; };
-template <>
-struct SweepMinBlocks<WDens> { static constexpr int v = PLUME_MINB_DENS; };
-template <>
-struct SweepMinBlocks<WVel> { static constexpr int v = PLUME_MINB_VEL; };
+template <typename T>
+struct SweepMinBlocks<T, WMom> { static constexpr int v = sizeof(T) == 4 ? PLUME_MINB_MOM : 6; };
+template <typename T>
+struct SweepMinBlocks<T, WDens> { static constexpr int v = sizeof(T) == 4 ? PLUME_MINB_DENS : 8; };
+template <typename T>
+struct SweepMinBlocks<T, WVel> { static constexpr int v = sizeof(T) == 4 ? PLUME_MINB_VEL : 8; };
 
 template <typename T, template <typename> class SW, bool MULTI>
-__global__ void __launch_bounds__(128, SweepMinBlocks<SW>::v) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
+__global__ void __launch_bounds__(128, SweepMinBlocks<T, SW>::v) k_sweep3_list(Opt o, Geos<MULTI> geo, Dev A, Work W, Packed K,
                                                      const uint32_t* __restrict__ cs_all,
                                                      const double* __restrict__ hmax_all,
                                                      const int* __restrict__ d_real,
