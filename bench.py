@@ -203,6 +203,14 @@ def timed_window(warmup: int, steps: int, interval: int = SML_INTERVAL):
     return first - warmup - 1, first
 
 
+def e2e_window(last: int, steps: int, interval: int = SML_INTERVAL) -> int:
+    """first step of the e2e leg's window: K steps centred on the next
+    adaptive-h pass after the timed window (ending at step `last`), so that
+    it holds passes at the timed window's rate"""
+    next_pass = (last // interval + 1) * interval
+    return max(last + 1, next_pass - steps // 2)
+
+
 def cpu_state(case):
     """the CPU sample's state: the workload after one adaptive-h pass (the
     smoothing lengths of the bulk of the run), computed by the oracle"""
@@ -617,8 +625,7 @@ def main():
     # the e2e window: K steps centred on the next adaptive-h pass (untimed
     # steps up to it), so that it holds passes at the timed window's rate
     e2e_steps = max(2, args.steps)
-    next_pass = (last // SML_INTERVAL + 1) * SML_INTERVAL
-    sol.steps(max(0, next_pass - e2e_steps // 2 - (last + 1)))
+    sol.steps(e2e_window(last, e2e_steps) - (last + 1))
     e2e_first = sol.time()[1] + 1
     snap = sol.download()
     grow = 0 if inlet is None else 4 * len(inlet["col_vel"]) * (e2e_steps + 1)
