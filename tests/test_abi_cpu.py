@@ -115,9 +115,14 @@ def test_plume_builder_geometry():
 
 
 def test_config2_size():
+    """the benchmark's workload, pinned: 134^3 air particles of the 20 km
+    cube at 150 m, the ghosts and the vent duct, the wall images of its
+    ground and the inlet's duct columns"""
     c = cases.plume_config2()
-    air = int(c.particles.need_neigh().sum())
-    assert 2.3e6 < air < 2.5e6
+    assert int(c.particles.need_neigh().sum()) == 2388148
+    assert c.particles.n == 3091228
+    assert len(cases.wall_images(c)[0]) == 85248
+    assert len(cases.inlet(c)["col_vel"]) == 12
 
 
 def test_riemann_ensemble_builder():
