@@ -152,8 +152,9 @@ struct JPos<double> {
 // list sweeps that load the next window's list entry one window ahead
 // (S::kListAhead): on the 134^3 plume at h ~ 1.5 dx the momentum sweep 13.44
 // -> 12.87 ms and the LANS filter 8.02 -> 7.72 ms, while the density sweep
-// (64 registers, no spare one) went 7.35 -> 7.79 ms and keeps the plain
-// load.  0 turns it off everywhere.
+// went 7.35 -> 7.79 ms and keeps the plain load (all measured with the
+// earlier register caps, 6, 8 and 8 blocks per SM).  0 turns it off
+// everywhere.
 #ifndef PLUME_LIST_AHEAD
 #define PLUME_LIST_AHEAD 1
 #endif
